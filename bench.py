@@ -1,0 +1,361 @@
+"""Benchmark of the reduction / fused-ufunc hot path (HBM GB/s).
+
+Workload (one "step"): over a 16384 x 16384 f32 array of N(0,1) values
+(SplitMix64 seed 3) and a 16384 x 16384 i64 array uniform in [-2^20, 2^20)
+(seed 4), in the row-major layout and as the transposed-stride view
+(shape swapped, strides (1, 16384)):
+  f32 sum / mean / max  x axis 0, 1 x 2 views   (12 reductions)
+  i64 sum / max         x axis 0, 1 x 2 views   ( 8 reductions)
+  fused y = exp(0.5 * x - 0.25) over the f32 array (1 ufunc pass)
+Each is one kernel launch. Algorithmic bytes = every input element read once
+plus every output written once. Inputs are 1 GiB and 2 GiB (far larger than
+the 129 MB L2), so no L2 flush is needed between steps.
+
+Printed JSON (one line, rank 0): value = device-resident GB/s of the whole
+step; e2e = the same bytes through the C ABI with pinned HOST buffers (host
+-> device copies of both arrays and device -> host copies of every result
+inside the timed region); roofline = the dominant kernel class against the
+measured HBM peak; cpu_baseline = the CPU oracle (numrs2 restatement) on a
+bounded row slab of the same workload, all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+R = C_ = 16384
+F32_SEED, I64_SEED = 3, 4
+A_SCALE, B_SHIFT = 0.5, -0.25
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region."""
+
+    def __init__(self, gpu: int):
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_ops(K, x32, x64):
+    """The step's launches as (class, bytes, callable)."""
+    from numrs_gb300 import _lib as L
+    ops = []
+    n = R * C_
+    views32 = [("rm", x32), ("tr", x32.t())]
+    views64 = [("rm", x64), ("tr", x64.t())]
+    for vname, v in views32:
+        for op, code in (("sum", L.SUM), ("mean", L.MEAN), ("max", L.MAX)):
+            for axis in (0, 1):
+                # which kernel serves it: lanes contiguous -> rows kernel
+                lanes_contig = (axis == 1) == (vname == "rm")
+                cls = "fold_rows_tma" if lanes_contig else "fold_cols_tma"
+                ops.append((f"{cls}/f32", n * 4 + 16384 * 4,
+                            (lambda v=v, code=code, axis=axis: K.reduce(v, code, axis))))
+    for vname, v in views64:
+        for op, code in (("sum", L.SUM), ("max", L.MAX)):
+            for axis in (0, 1):
+                lanes_contig = (axis == 1) == (vname == "rm")
+                cls = "fold_rows_tma" if lanes_contig else "fold_cols_tma"
+                ops.append((f"{cls}/i64", n * 8 + 16384 * 8,
+                            (lambda v=v, code=code, axis=axis: K.reduce(v, code, axis))))
+    y = x32.new_empty(x32.shape)
+    ops.append(("exp_affine_vec/f32", n * 8, (lambda: K.exp_affine(x32, A_SCALE, B_SHIFT, out=y))))
+    return ops, y
+
+
+def cpu_sample(steps: int | None, min_seconds: float, x32_np, x64_np):
+    """Times the oracle (numrs2's CPU kernels restated) on the row slab."""
+    from oracle import Oracle
+    from oracle import oracle as O
+    ora = Oracle()
+    rows = x32_np.shape[0]
+    nbytes = 0
+    calls = []
+    for v in (x32_np, x32_np.T):
+        for code in (O.SUM, O.MEAN, O.MAX):
+            for axis in (0, 1):
+                calls.append((v, code, axis))
+                nbytes += v.size * 4 + (v.shape[1 - axis]) * 4
+    for v in (x64_np, x64_np.T):
+        for code in (O.SUM, O.MAX):
+            for axis in (0, 1):
+                calls.append((v, code, axis))
+                nbytes += v.size * 8 + (v.shape[1 - axis]) * 8
+    nbytes += x32_np.size * 8
+
+    def one_pass():
+        for v, code, axis in calls:
+            ora.axis(code, v, axis)
+        ora.exp_affine(x32_np, A_SCALE, B_SHIFT)
+
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        one_pass()
+        times.append(time.perf_counter() - t0)
+        if steps is not None and len(times) >= steps:
+            break
+        if steps is None and time.perf_counter() - t_start >= min_seconds:
+            break
+    return nbytes, times, ora.num_threads(), f"{rows}x{x32_np.shape[1]} row slab of both arrays, all 21 ops"
+
+
+def run_reference(args):
+    """`--impl reference`: the CPU restatement of numrs2's kernels, all host threads."""
+    import numpy as np
+    from numrs_gb300 import rng
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rows = args.cpu_rows
+    n = rows * C_
+    x64 = rng.int_range(I64_SEED, n).reshape(rows, C_)
+    x32 = np.random.default_rng(F32_SEED).standard_normal(n).astype(np.float32).reshape(rows, C_)
+    nbytes, times, cores, sample = cpu_sample(args.warmup + args.steps, 0, x32, x64)
+    t = sum(times[args.warmup:])
+    val = nbytes * args.steps / t / 1e9
+    line = {"impl": "reference", "metric": "reduce GB/s", "value": round(val, 2), "unit": "GB/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": {"workload": f"axis-0/1 sum/mean/max f32 + sum/max i64 (row-major and transposed) "
+                                   f"+ fused exp(0.5x-0.25), {rows}x16384 slab per step",
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": round(val, 2), "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(val, 2), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from numrs_gb300 import _lib as L
+    from numrs_gb300 import kernels as K
+    lib = L.load()
+
+    x32 = torch.empty((R, C_), dtype=torch.float32, device="cuda")
+    x64 = torch.empty((R, C_), dtype=torch.int64, device="cuda")
+    K.fill_random(x32, L.RNG_NORMAL, F32_SEED, 0.0, 1.0)
+    K.fill_random(x64, L.RNG_INT, I64_SEED, -(1 << 20), float(1 << 21))
+    ops, y = build_ops(K, x32, x64)
+    step_bytes = sum(b for _, b, _ in ops)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        for _, _, fn in ops:
+            fn()
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in ops]
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    time.sleep(0.3)
+    barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    launches = 0
+    for s_i in range(args.steps):
+        for i, (cls, _, fn) in enumerate(ops):
+            ev[s_i][i][0].record(stream)
+            fn()
+            ev[s_i][i][1].record(stream)
+            launches += 1
+    t_end.record(stream)
+    barrier()
+    per_class: dict[str, list[float]] = {}
+    for s_i in range(args.steps):
+        for i, (cls, _, _) in enumerate(ops):
+            per_class.setdefault(cls, []).append(ev[s_i][i][0].elapsed_time(ev[s_i][i][1]))
+    clk = clocks.stop()
+    ms_total = t_start.elapsed_time(t_end)
+    if dist is not None:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_per_step = ms_total / args.steps
+    value = step_bytes * world / (ms_per_step / 1e3) / 1e9
+
+    peak, peak_kind = _peaks()
+    # per kernel class: algorithmic bytes per launch / mean launch time
+    bytes_of = {}
+    for cls, b, _ in ops:
+        bytes_of.setdefault(cls, []).append(b)
+    kernels = {}
+    for cls, ts in per_class.items():
+        avg_ms = sum(ts) / len(ts)
+        avg_b = sum(bytes_of[cls]) / len(bytes_of[cls])
+        gbs = avg_b / (avg_ms / 1e3) / 1e9
+        kernels[cls] = {"launches_per_step": len(bytes_of[cls]), "avg_ms": round(avg_ms, 4),
+                        "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
+                        "share": round(sum(ts) / sum(sum(v) for v in per_class.values()), 4)}
+    dom = max(kernels, key=lambda c: kernels[c]["share"])
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+
+    out = {"metric": "reduce GB/s", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
+           "data": "synthetic (SplitMix64, seeds 3/4)",
+           "config": {"workload": "16384x16384 f32 N(0,1) + i64 U[-2^20,2^20): axis-0/1 sum/mean/max (f32), "
+                                  "sum/max (i64), row-major and transposed-stride views, + fused "
+                                  "exp(0.5x-0.25); one step = 21 launches",
+                      "bytes_per_step": step_bytes, "l2": "no flush: inputs (1 GiB, 2 GiB) > 129 MB L2",
+                      "parallelism": f"replicas x{world}"},
+           "gpu_launches": launches,
+           "roofline": {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_gbs"],
+                        "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                        "frac": kernels[dom]["frac"], "traffic": traffic},
+           "kernels": kernels, "clocks": clk}
+
+    # ---- end to end through the C ABI with pinned host buffers --------------
+    if not args.no_e2e:
+        h = K.handle()
+        nb32, nb64 = R * C_ * 4, R * C_ * 8
+        hp32, hp64, hy = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        L.check(lib.nrs_host_alloc(h, nb32, C.byref(hp32)), h)
+        L.check(lib.nrs_host_alloc(h, nb64, C.byref(hp64)), h)
+        L.check(lib.nrs_host_alloc(h, nb32, C.byref(hy)), h)
+        L.check(lib.nrs_memcpy_d2h(h, hp32, C.c_void_p(x32.data_ptr()), nb32), h)
+        L.check(lib.nrs_memcpy_d2h(h, hp64, C.c_void_p(x64.data_ptr()), nb64), h)
+        L.check(lib.nrs_synchronize(h), h)
+        outs = []
+        red_outs = []
+
+        def e2e_step():
+            L.check(lib.nrs_memcpy_h2d(h, C.c_void_p(x32.data_ptr()), hp32, nb32), h)
+            L.check(lib.nrs_memcpy_h2d(h, C.c_void_p(x64.data_ptr()), hp64, nb64), h)
+            res = [fn() for _, _, fn in ops]
+            d2h = 0
+            for r in res[:-1]:
+                host = torch.empty(r.shape, dtype=r.dtype, pin_memory=True)
+                L.check(lib.nrs_memcpy_d2h(h, C.c_void_p(host.data_ptr()), C.c_void_p(r.data_ptr()),
+                                           r.numel() * r.element_size()), h)
+                d2h += r.numel() * r.element_size()
+            L.check(lib.nrs_memcpy_d2h(h, hy, C.c_void_p(y.data_ptr()), nb32), h)
+            d2h += nb32
+            L.check(lib.nrs_synchronize(h), h)
+            return d2h
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        e_steps = max(2, min(args.steps, 5))
+        for _ in range(e_steps):
+            d2h = e2e_step()
+        barrier()
+        dt = (time.perf_counter() - t0) / e_steps
+        if dist is not None:
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        out["e2e"] = {"value": round(step_bytes * world / dt / 1e9, 1), "unit": "GB/s",
+                      "h2d_bytes_per_step": nb32 + nb64, "d2h_bytes_per_step": d2h,
+                      "ms_per_step": round(dt * 1e3, 3)}
+        for p in (hp32, hp64, hy):
+            lib.nrs_host_free(h, p)
+
+    # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rows = args.cpu_rows
+        x32n = x32[:rows].cpu().numpy()
+        x64n = x64[:rows].cpu().numpy()
+        nbytes, times, cores, sample = cpu_sample(None, args.cpu_seconds, x32n, x64n)
+        t = sum(times)
+        out["cpu_baseline"] = {"value": round(nbytes * len(times) / t / 1e9, 2), "unit": "GB/s",
+                               "cores": cores, "kind": "port", "sample": sample,
+                               "passes": len(times), "seconds": round(t, 2)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

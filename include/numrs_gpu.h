@@ -1,0 +1,326 @@
+/*
+ * numrs_gpu.h -- C ABI of the GB300 (sm_103a) implementation of NumRS2's
+ * crate-private `kernels` dispatch layer: GEMM, axis/flat reductions and
+ * elementwise/fused ufuncs behind `Array<T>`.
+ *
+ * Every entry point names the reference interface it replaces
+ * (numrs2 0.4.1, paths relative to the crate root). The reference passes Rust
+ * slices (`&[T]`, `&mut [T]`) and closures; this ABI passes plain pointers,
+ * sizes and element strides, and op-code programs instead of closures.
+ *
+ * Conventions
+ *  - All data pointers given to compute entry points are DEVICE pointers
+ *    (cudaMalloc / nrs_malloc / any allocator of the same context); the caller
+ *    owns them. Host data is moved with nrs_memcpy_h2d / nrs_memcpy_d2h.
+ *  - Strides are in ELEMENTS (not bytes), may be 0 for broadcast dimensions,
+ *    and must be non-negative.
+ *  - Work is enqueued on the handle's stream (nrs_set_stream); calls return
+ *    once the work is enqueued. Results are visible after nrs_synchronize or
+ *    any later work on the same stream.
+ *  - Status codes: NRS_OK (0) or a negative nrs_status. Shape/axis/dtype
+ *    errors are reported before anything is launched (the reference raises
+ *    them one layer up as NumRs2Error, src/error/legacy.rs:12-60). A device
+ *    fault or a device-side bounded wait that gave up is reported by the call
+ *    that observed it (NRS_ERR_CUDA / NRS_ERR_TIMEOUT) and by nrs_synchronize.
+ *  - Threading: a handle is used by one host thread at a time; distinct
+ *    handles are independent. The library never falls back to the CPU.
+ */
+#ifndef NUMRS_GPU_H
+#define NUMRS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NRS_ABI_VERSION 1
+
+typedef struct nrs_handle nrs_handle;
+
+/* Element types. The reference dispatches on TypeId through kernels::cast
+ * (src/kernels/cast.rs:35-140); here the dtype is explicit. */
+typedef enum nrs_dtype { NRS_F32 = 0, NRS_F64 = 1, NRS_I32 = 2, NRS_I64 = 3 } nrs_dtype;
+
+typedef enum nrs_status {
+  NRS_OK = 0,
+  NRS_ERR_INVALID = -1,     /* null pointer, bad enum or negative size     */
+  NRS_ERR_SHAPE = -2,       /* ShapeMismatch / DimensionMismatch           */
+  NRS_ERR_DTYPE = -3,       /* operation not defined for this dtype        */
+  NRS_ERR_AXIS = -4,        /* "Axis {} out of bounds for array of ..."     */
+  NRS_ERR_EMPTY = -5,       /* InvalidOperation on an empty array          */
+  NRS_ERR_STRIDE = -6,      /* negative or overflowing stride              */
+  NRS_ERR_CUDA = -7,        /* CUDA runtime error (message: nrs_last_error) */
+  NRS_ERR_TIMEOUT = -8,     /* a device-side bounded wait gave up          */
+  NRS_ERR_ALLOC = -9,       /* workspace allocation failed                 */
+  NRS_ERR_UNSUPPORTED = -10,
+  NRS_ERR_TOO_LARGE = -11   /* size beyond a documented maximum            */
+} nrs_status;
+
+/* ---------------------------------------------------------------------- */
+/* Handle, stream and memory                                                */
+/* ---------------------------------------------------------------------- */
+int nrs_abi_version(void);
+const char* nrs_status_string(int status);
+
+/* Creates a handle bound to `device`, with its own non-blocking stream. */
+int nrs_create(int device, nrs_handle** out);
+int nrs_destroy(nrs_handle* h);
+/* Enqueue on a caller-owned cudaStream_t; NULL means CUDA's default stream. */
+int nrs_set_stream(nrs_handle* h, void* cuda_stream);
+/* Enqueue on the handle's own non-blocking stream (the state after create). */
+int nrs_use_own_stream(nrs_handle* h);
+void* nrs_get_stream(nrs_handle* h);
+/* Waits for the stream, then reports any device-side error flag. */
+int nrs_synchronize(nrs_handle* h);
+/* Message of the last failing call on this handle ("" if none). */
+const char* nrs_last_error(nrs_handle* h);
+
+int nrs_malloc(nrs_handle* h, size_t bytes, void** dptr);
+int nrs_free(nrs_handle* h, void* dptr);
+int nrs_host_alloc(nrs_handle* h, size_t bytes, void** hptr); /* pinned */
+int nrs_host_free(nrs_handle* h, void* hptr);
+int nrs_memcpy_h2d(nrs_handle* h, void* dst, const void* src, size_t bytes);
+int nrs_memcpy_d2h(nrs_handle* h, void* dst, const void* src, size_t bytes);
+
+/* Seeded SplitMix64 input generator, element i = f(mix((seed ^ GAMMA) +
+ * (i+1) * GAMMA)) with the step/mix constants of the reference's test
+ * generator (tests/test_expr_fused_equivalence.rs:96-112).
+ *   NRS_RNG_UNIFORM : p0 + (p1 - p0) * u,  u = (x >> 11) * 2^-53   (f32/f64)
+ *   NRS_RNG_NORMAL  : p0 + p1 * z, Box-Muller on draws 2i, 2i+1      (f32/f64)
+ *   NRS_RNG_INT     : (x >> s) + p0 with s = 64 - log2(p1)           (i64/i32)
+ *   NRS_RNG_OZAKI   : U(-0.5,0.5) * exp(p0 * z), z normal            (f64)  */
+typedef enum nrs_rng { NRS_RNG_UNIFORM = 0, NRS_RNG_NORMAL = 1, NRS_RNG_INT = 2, NRS_RNG_OZAKI = 3 } nrs_rng;
+int nrs_fill_random(nrs_handle* h, int dtype, int dist, uint64_t seed, int64_t n, double p0,
+                    double p1, void* out);
+
+/* ---------------------------------------------------------------------- */
+/* Reductions                                                               */
+/* ---------------------------------------------------------------------- */
+typedef enum nrs_reduce_op {
+  NRS_SUM = 0, NRS_MEAN = 1, NRS_MAX = 2, NRS_MIN = 3, NRS_PROD = 4, NRS_VAR = 5, NRS_STD = 6
+} nrs_reduce_op;
+#define NRS_AXIS_NONE INT64_MIN
+
+/* Reduce an N-D strided view (ndim <= 8) of `x`.
+ *
+ * axis == NRS_AXIS_NONE: flat reduction of all elements in logical order,
+ *   out = 1 element. Replaces kernels::reduce::{sum,mean,var,min,max,prod}_
+ *   {f64,f32} (src/kernels/reduce.rs:204-444; empty -> 0, prod empty -> 1,
+ *   min/max: any NaN -> NaN) and, for i64, Array::sum (src/array/
+ *   operations.rs:303) and math::max/min(None) (src/math/aggregation.rs:160,
+ *   :289). VAR/STD use `ddof` as reduce::var does (divisor n - ddof).
+ * axis >= 0 or negative (counted from the end, as the reference does):
+ *   per-lane fold along `axis`, out = prod(kept dims) elements in row-major
+ *   order of the kept dimensions. Replaces math::sum(axis)
+ *   (src/math/aggregation.rs:416, fold :555-561), math::statistics::mean(axis)
+ *   (src/math/statistics/mod.rs:971), math::max/min(axis)
+ *   (src/math/aggregation.rs:160, :289) and Array::sum_axis
+ *   (src/array/operations.rs:75). Each lane is folded left to right from a
+ *   zero seed (sum/mean), one seed (prod) or its first element (max/min, the
+ *   first NaN short-circuits and is the lane's result bit for bit), so float
+ *   lane sums match the reference's fold order exactly.
+ *   MAX/MIN/MEAN over an empty axis return NRS_ERR_EMPTY (the reference's
+ *   "Cannot find max of empty array"); SUM gives zeros.
+ * dtypes: F32, F64, I64 (I32 for SUM/MAX/MIN/PROD). For I64, MEAN writes f64
+ *   (no reference counterpart: math::mean requires T: Float). */
+int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+               const int64_t* strides, int64_t axis, int64_t ddof, const void* x, void* out);
+
+/* ---------------------------------------------------------------------- */
+/* Elementwise ufunc programs                                               */
+/* ---------------------------------------------------------------------- */
+/* A closure `|x, y| ...` of kernels::elementwise::{binary,unary}_* or an
+ * expr::ExprNode tree (src/expr/owned.rs:204; Leaf/Binary/ScalarRhs/
+ * ScalarLhs/Unary) becomes a postfix program over a small value stack.
+ * Every op rounds once: MUL followed by ADD is two roundings, never an FMA,
+ * as in src/expr/fused_eval.rs:17-21. */
+typedef enum nrs_ufunc_code {
+  NRS_OP_INPUT = 0,  /* push inputs[arg][i]           */
+  NRS_OP_SCALAR = 1, /* push scalar                   */
+  NRS_OP_ADD = 2, NRS_OP_SUB = 3, NRS_OP_MUL = 4, NRS_OP_DIV = 5, /* pop b, pop a, push a op b */
+  NRS_OP_NEG = 6, NRS_OP_ABS = 7, NRS_OP_SQRT = 8, NRS_OP_EXP = 9, NRS_OP_LN = 10, /* unary */
+  NRS_OP_MAX = 11, NRS_OP_MIN = 12
+} nrs_ufunc_code;
+
+typedef struct nrs_ufunc_op {
+  int32_t code;
+  int32_t arg;
+  double scalar;
+} nrs_ufunc_op;
+
+#define NRS_UFUNC_MAX_OPS 32
+#define NRS_UFUNC_MAX_INPUTS 8
+#define NRS_UFUNC_MAX_DIMS 8
+
+/* out[i] = program(inputs[0][i], ...) over the broadcast shape `shape`
+ * (ndim dims). in_strides is n_inputs x ndim element strides (0 on
+ * broadcast dims, i.e. NumPy broadcasting as in *_broadcast,
+ * src/array/operations.rs:370-446); out_strides NULL means row-major
+ * contiguous. Integer dtypes accept ADD/SUB/MUL/DIV/NEG/ABS/MAX/MIN with
+ * wrapping arithmetic (DIV by zero gives 0); EXP/LN/SQRT need F32/F64.
+ * Replaces binary_serial/binary_{f64,f32}/binary_dispatch/unary_dispatch
+ * (src/kernels/elementwise.rs:51-258), Array::map scalar ops
+ * (src/array/operations.rs:182, :450-475), ElementWiseMath::exp
+ * (src/math/elementwise.rs:145), ufuncs::exp (src/ufuncs.rs:398) and
+ * ExprNode::eval (src/expr/owned.rs:557). */
+int nrs_ufunc(nrs_handle* h, int dtype, const nrs_ufunc_op* prog, int prog_len, int ndim,
+              const int64_t* shape, int n_inputs, const void* const* inputs,
+              const int64_t* in_strides, void* out, const int64_t* out_strides);
+
+/* y[i] = exp((a * x[i]) + b), two roundings before the exp, contiguous f32 or
+ * f64: the fused form of `(x * a + b).exp()` (eager: three Array::map/exp
+ * passes; fused: ExprNode Unary(Exp, ScalarRhs(Add, ScalarRhs(Mul, Leaf, a),
+ * b))). One HBM pass: 8 B/elem for f32. */
+int nrs_exp_affine(nrs_handle* h, int dtype, int64_t n, const void* x, double a, double b,
+                   void* y);
+
+/* ---------------------------------------------------------------------- */
+/* GEMM                                                                     */
+/* ---------------------------------------------------------------------- */
+#define NRS_GEMM_ACCUMULATE 1u /* C += A*B (Array::matmul_to, src/array/operations_optimized.rs:385) */
+#define NRS_GEMM_TRANS_A 2u    /* A is stored k x m (lda >= m): a transposed view of A  */
+#define NRS_GEMM_TRANS_B 4u    /* B is stored n x k (ldb >= k): a transposed view of B  */
+
+typedef enum nrs_gemm_variant {
+  NRS_GEMM_AUTO = 0,     /* autotuner choice (plain kernels only; never Ozaki) */
+  NRS_GEMM_DMMA = 1,     /* f64: FP64 tensor-core mma.sync m8n8k4 tiles        */
+  NRS_GEMM_SIMT = 2,     /* f32 / f64: register-tiled CUDA-core GEMM           */
+  NRS_GEMM_GENERIC = 3,  /* any dtype: one thread per C element (ints, checks) */
+  NRS_GEMM_SIMT_SMALL = 4 /* f32: 32x32 tiles for small problems               */
+} nrs_gemm_variant;
+
+/* C := A*B (or C += A*B with NRS_GEMM_ACCUMULATE) for row-major m x k A,
+ * k x n B, m x n C with leading dimensions lda/ldb/ldc.
+ * Replaces kernels::gemm::gemm_2d (src/kernels/gemm.rs:246): m == 0 or
+ * n == 0 is a no-op, k == 0 zero-fills C (overwrite contract, :294-302);
+ * integer dtypes wrap like gemm_generic (:408). */
+int nrs_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, const void* A,
+             int64_t lda, const void* B, int64_t ldb, void* C, int64_t ldc, unsigned flags,
+             int variant);
+
+/* ---------------------------------------------------------------------- */
+/* f64-accurate split GEMM (Ozaki scheme on BF16 tcgen05 tensor cores)      */
+/* ---------------------------------------------------------------------- */
+typedef struct nrs_ozaki_info {
+  int32_t slices;        /* slices per operand actually used                 */
+  int32_t products;      /* slice-pair GEMMs executed                        */
+  int32_t slice_bits;    /* bits carried by each slice after the first       */
+  int32_t k_chunk;       /* K block inside which fp32 accumulation is exact  */
+  double est_rel_error;  /* a-priori bound on |C - AB| / (rowmax|A| colmax|B| k) */
+} nrs_ozaki_info;
+
+/* C := A*B in f64 accuracy from BF16 slice products on tcgen05 tensor cores
+ * with per-row (A) / per-column (B) power-of-two scaling and exact fp32
+ * accumulation inside K blocks, int32 cross-block accumulation and f64
+ * cross-slice accumulation. `slices` = 0 picks the count from the operands'
+ * exponent spread. No reference counterpart: replaces the f64 tier of
+ * gemm_2d (src/kernels/gemm.rs:290) for large problems. Row-major, no
+ * flags. `info` may be NULL. */
+int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, const double* A, int64_t lda,
+                   const double* B, int64_t ldb, double* C, int64_t ldc, int slices,
+                   nrs_ozaki_info* info);
+
+/* ---------------------------------------------------------------------- */
+/* Grouped persistent launch (no reference counterpart; the reference's     */
+/* closest analogue is a caller loop over Array::matmul or batched_gemm,    */
+/* src/array/linalg.rs:56-136, and a loop over reduce::sum_*).              */
+/* ---------------------------------------------------------------------- */
+typedef struct nrs_gemm_desc {
+  int32_t dtype; /* NRS_F32 or NRS_F64 */
+  uint32_t flags; /* NRS_GEMM_ACCUMULATE only */
+  int64_t m, k, n;
+  const void* A;
+  int64_t lda;
+  const void* B;
+  int64_t ldb;
+  void* C;
+  int64_t ldc;
+} nrs_gemm_desc;
+
+typedef struct nrs_rowreduce_desc {
+  int32_t dtype; /* NRS_F32, NRS_F64 or NRS_I64 */
+  int32_t op;    /* NRS_SUM, NRS_MEAN, NRS_MAX, NRS_MIN */
+  int64_t len;
+  const void* x; /* contiguous */
+  void* out;     /* one element */
+} nrs_rowreduce_desc;
+
+typedef struct nrs_plan nrs_plan;
+
+/* Builds the tile/work queue for `n_gemm` GEMMs and `n_red` row reductions
+ * (tile shapes from the autotuner's table, see nrs_tune_gemm) and uploads
+ * it. Descriptors are copied; the data pointers must stay valid while the
+ * plan is used. */
+int nrs_plan_create(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
+                    const nrs_rowreduce_desc* reds, nrs_plan** out);
+/* Runs the whole group as ONE persistent kernel launch. With use_graph != 0
+ * the launch is captured once into a CUDA graph owned by the plan and
+ * replayed on later calls. */
+int nrs_plan_run(nrs_handle* h, nrs_plan* plan, int use_graph);
+/* Number of work items and tiles in the plan. */
+int nrs_plan_stats(nrs_plan* plan, int64_t* work_items, int64_t* gemm_tiles);
+int nrs_plan_destroy(nrs_plan* plan);
+
+/* ---------------------------------------------------------------------- */
+/* Autotuner and learned selector (no reference counterpart)               */
+/* ---------------------------------------------------------------------- */
+#define NRS_TILE_VARIANTS 6 /* tile configurations known to the grouped kernel */
+
+/* Describes grouped-kernel tile variant v: tile rows/cols, dtype support. */
+int nrs_tile_variant_info(int v, int* tile_m, int* tile_n, int* split_k, int* dtype_mask);
+
+/* Exhaustive autotuning of one (dtype, m, k, n, flags) shape: every tile
+ * variant of that dtype is timed as a grouped launch of `batch` copies of
+ * the problem (library-owned random operands, CUDA events on the handle's
+ * stream, one warm-up then `reps` launches). Writes microseconds per problem
+ * to times_us[NRS_TILE_VARIANTS] (-1 where a variant does not apply) and the
+ * fastest variant to *best. flags: NRS_GEMM_TRANS_A / NRS_GEMM_TRANS_B. */
+int nrs_tune_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, unsigned flags,
+                  int64_t batch, int reps, float* times_us, int* best);
+/* Records the tuned variant for a shape bucket, used by nrs_plan_create. */
+int nrs_tuner_set(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, int variant);
+/* Looks a shape bucket up; -1 if untuned. */
+int nrs_tuner_get(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n);
+/* Clears the table. */
+int nrs_tuner_clear(nrs_handle* h);
+
+/* MLP cost model: features[F] -> 2 x hidden ReLU layers -> one predicted
+ * log-time per tile variant. Weights are kept in fp32 (master) and BF16
+ * (the copy every forward pass reads); accumulation is fp32. */
+typedef struct nrs_selector nrs_selector;
+int nrs_selector_create(nrs_handle* h, int n_features, int hidden, int n_out, uint64_t seed,
+                        nrs_selector** out);
+int nrs_selector_destroy(nrs_selector* s);
+/* Parameter count and host copies of the fp32 master weights, layer order
+ * W1[H,F], b1[H], W2[H,H], b2[H], W3[V,H], b3[V]. */
+int64_t nrs_selector_num_params(nrs_selector* s);
+int nrs_selector_get_params(nrs_handle* h, nrs_selector* s, float* host_params);
+int nrs_selector_set_params(nrs_handle* h, nrs_selector* s, const float* host_params);
+/* One forward + backward pass on device buffers: x[B,F], target[B,V],
+ * mask[B,V] (1 where the target is known). Writes y[B,V], the gradient of
+ * the masked mean-squared loss in host layout order to grads (device, one
+ * float per parameter) and the loss to *loss (host). */
+int nrs_selector_forward_backward(nrs_handle* h, nrs_selector* s, int64_t batch, const float* x,
+                                  const float* target, const float* mask, float* y, float* grads,
+                                  float* loss);
+/* Trains with Adam for `epochs` passes over n samples in minibatches of
+ * `batch` (device buffers), entirely on the GPU. Writes the final epoch's
+ * mean loss to *loss. */
+int nrs_selector_train(nrs_handle* h, nrs_selector* s, int64_t n, const float* x,
+                       const float* target, const float* mask, int epochs, int64_t batch,
+                       float lr, uint64_t seed, float* loss);
+/* Predicted per-variant outputs y[n, V] for x[n, F] (device buffers). */
+int nrs_selector_predict(nrs_handle* h, nrs_selector* s, int64_t n, const float* x, float* y);
+/* Installs `s` (F = 7 features, V = NRS_TILE_VARIANTS outputs) as the choice
+ * for GEMM shapes the tuner table lacks when a plan is created; NULL removes
+ * it. Features: log2(m)/14, log2(n)/14, log2(k)/14, dtype (1 = f64),
+ * trans_a, trans_b, log2(number of GEMMs in the plan)/14. The handle does not
+ * own `s`: remove it before nrs_selector_destroy. */
+int nrs_tuner_set_selector(nrs_handle* h, nrs_selector* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NUMRS_GPU_H */

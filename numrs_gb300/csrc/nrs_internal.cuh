@@ -1,0 +1,141 @@
+// Internal definitions shared by the CUDA translation units of libnumrs_gb300.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/numrs_gpu.h"
+
+// ---------------------------------------------------------------------------
+// Handle
+// ---------------------------------------------------------------------------
+// Device-side error word layout: the low byte names the kernel family whose
+// bounded wait gave up, the rest is a site code. 0 = no error.
+enum : uint32_t {
+  NRS_DEVERR_NONE = 0,
+  NRS_DEVERR_REDUCE_TMA = 0x01,
+  NRS_DEVERR_GEMM_TC = 0x02,
+  NRS_DEVERR_GROUPED = 0x03,
+};
+
+struct nrs_tuner_table;
+
+struct nrs_handle {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // Grow-only device workspace for kernels that need scratch memory.
+  void* workspace = nullptr;
+  size_t workspace_bytes = 0;
+  // Device error word written by kernels whose waits are bounded.
+  uint32_t* dev_error = nullptr;
+  std::string last_error;
+  nrs_tuner_table* tuner = nullptr;
+  // Learned selector consulted for shapes the tuner table lacks (not owned).
+  nrs_selector* selector = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// Helpers (runtime.cu)
+// ---------------------------------------------------------------------------
+int nrs_fail(nrs_handle* h, int status, const std::string& msg);
+int nrs_cuda_check(nrs_handle* h, cudaError_t e, const char* what);
+// Ensures the workspace holds at least `bytes`; returns its pointer or null.
+void* nrs_workspace(nrs_handle* h, size_t bytes, int* status);
+size_t nrs_dtype_size(int dtype);
+// Checks launch errors right after a launch.
+int nrs_after_launch(nrs_handle* h, const char* what);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+typedef CUresult (*nrs_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                        const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                        const cuuint32_t*, CUtensorMapInterleave,
+                                        CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                        CUtensorMapFloatOOBfill);
+nrs_encode_tiled_fn nrs_get_encode_tiled();
+
+// Host-side entry points of the other translation units.
+int nrs_plain_gemm_launch(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n,
+                          const void* A, int64_t rsa, int64_t csa, const void* B, int64_t rsb,
+                          int64_t csb, void* C, int64_t ldc, bool accumulate, int variant);
+
+// ---------------------------------------------------------------------------
+// Device helpers: mbarrier and TMA (inline PTX, sm_90+ forms valid on sm_103a)
+// ---------------------------------------------------------------------------
+#define NRS_DEV __device__ __forceinline__
+
+NRS_DEV uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+NRS_DEV void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+NRS_DEV void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+NRS_DEV void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+NRS_DEV void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+NRS_DEV void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// One try_wait probe on `phase`; true once the phase has completed.
+NRS_DEV bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after `limit` probes (each probe itself may suspend
+// the thread for a hardware-defined time). Returns false on give-up.
+NRS_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
+NRS_DEV void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int32_t x, int32_t y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+NRS_DEV void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int32_t x, int32_t y,
+                         int32_t z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+NRS_DEV void prefetch_tensormap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Bounded-wait budget: ~2^22 probes is several seconds of a stalled copy,
+// far beyond any legitimate wait.
+#define NRS_WAIT_LIMIT (1u << 22)

@@ -1,0 +1,581 @@
+// f64-accurate GEMM from BF16 slices on tcgen05 tensor cores (Ozaki scheme).
+//
+// C = A*B with A (m x k) and B (k x n) row-major f64. No reference
+// counterpart: it stands in for the f64 tier of kernels::gemm::gemm_2d
+// (src/kernels/gemm.rs:290) where GB300's FP64 rate (~1.2 TFLOP/s) makes a
+// native FP64 GEMM slow.
+//
+// 1. Scaling: e_a[i] = frexp exponent of max_k |a_ik| (|a_ik| < 2^e_a[i]),
+//    e_b[j] likewise over column j of B. Powers of two: exact.
+// 2. Slicing: x = a_ik * 2^-e_a[i] in (-1, 1) becomes the 126-bit fixed-point
+//    integer X = round(x * 2^126), split into signed digits by
+//    round-to-nearest: digit 0 = round(X / 2^121), then digit t =
+//    round(rest / 2^(121 - 6t)). Every digit lies in [-32, 32], exactly
+//    representable in BF16, and x = sum_t digit_t * 2^-(5 + 6t) up to
+//    2^-(6 + 6(S-1)). Slices are stored K-major ([S][rows][kpad] bf16) for
+//    A and for B^T (the B slicer transposes through shared memory).
+// 3. Products: for every slice pair (s, t) with s + t <= S-1 (the pairs
+//    whose weight 2^-(10 + 6(s+t)) matters), P = A_s * B_t^T on the tensor
+//    cores with FP32 accumulation. |digit products| <= 2^10, so every partial
+//    sum of a K <= 16384 chunk is an integer below 2^24: the FP32
+//    accumulation is EXACT.
+// 4. Cross-slice accumulation: each exact P is added into a per-element
+//    128-bit integer at weight 2^(6(S-1-(s+t))) -- exact, no FP64 op -- and
+//    the last pair of a tile converts it once to f64 and applies
+//    2^(e_a[i] + e_b[j] - 10 - 6(S-1)).
+//
+// The tensor-core kernel is persistent (one CTA per SM) and warp-specialised:
+//   warp 0      : TMA producer, 4-stage ring of A (128x64) + B (256x64) bf16
+//                 tiles, 128-byte swizzle;
+//   warp 1      : TMEM allocator and single-thread tcgen05.mma issuer,
+//                 M=128 N=256 K=16, accumulators double-buffered in TMEM
+//                 (2 x 256 columns);
+//   warps 2..5  : epilogue, tcgen05.ld of the finished accumulator (one TMEM
+//                 lane = one tile row per thread) into the int128 sums.
+// Every mbarrier wait is bounded; on give-up the kernel records an error
+// word, drains its own copies and MMAs (bounded), frees TMEM and returns.
+#include <cmath>
+#include <cstring>
+
+#include "nrs_internal.cuh"
+
+namespace {
+
+constexpr int OZ_BM = 128;
+constexpr int OZ_BN = 256;
+constexpr int OZ_BK = 64;
+constexpr int OZ_STAGES = 4;
+constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;  // 16 KB
+constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 32 KB
+constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
+constexpr int OZ_THREADS = 192;                 // 6 warps
+constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
+constexpr int OZ_KCHUNK = 16384;                // exact fp32 accumulation bound
+constexpr int OZ_MAX_SLICES = 16;
+constexpr int OZ_DIGIT_BITS = 6;
+constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+// ---------------------------------------------------------------------------
+// tcgen05 / TMEM wrappers
+// ---------------------------------------------------------------------------
+NRS_DEV void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+NRS_DEV void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+NRS_DEV void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+NRS_DEV void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+NRS_DEV void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+NRS_DEV void tc_mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+NRS_DEV void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 32 lanes x 32 consecutive 32-bit columns: thread = lane, v[c] = column c.
+NRS_DEV void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor, K-major operand with 128-byte swizzle:
+// rows of 128 B, 8-row core-matrix groups 1024 B apart (SBO), descriptor
+// version 1 (bits 46-47), swizzle mode 2 = 128B (bits 61-63).
+NRS_DEV uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(16 >> 4) << 16;    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+                            ((uint32_t)(OZ_BM >> 4) << 24);
+
+struct OzParams {
+  int64_t m, n, k, kpad;
+  int slices;
+  int kchunks;
+  int n_pairs;     // pairs x kchunks work units per tile
+  int tiles_m, tiles_n;
+  int group_m;     // tile rasterisation group height
+  const int* ea;   // row exponents of A
+  const int* eb;   // column exponents of B
+  __int128* acc;   // m x n exact accumulators
+  double* C;
+  int64_t ldc;
+  int final_shift; // -10 - 6(S-1)
+  uint32_t* err;
+};
+
+// Pair order within a tile: diagonals from the least significant (d = S-1)
+// to the most significant (d = 0), so the last unit of a tile is pair (0,0).
+struct PairOf {
+  int s, t, chunk;
+};
+__device__ __forceinline__ PairOf pair_of(int u, int S, int kchunks) {
+  const int chunk = u % kchunks;
+  int p = u / kchunks;
+  for (int d = S - 1; d >= 0; --d) {
+    if (p < d + 1) return {p, d - p, chunk};
+    p -= d + 1;
+  }
+  return {0, 0, chunk};
+}
+
+__device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm, int& tn) {
+  // Grouped rasterisation: consecutive tiles walk group_m tile rows before
+  // moving along N, so concurrently active tiles share A and B panels in L2.
+  const int per_group = P.group_m * P.tiles_n;
+  const int g = tile / per_group;
+  const int first_m = g * P.group_m;
+  const int gm = (P.tiles_m - first_m) < P.group_m ? (P.tiles_m - first_m) : P.group_m;
+  const int r = tile % per_group;
+  tm = first_m + r % gm;
+  tn = r / gm;
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    ozaki_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                    OzParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
+  uint64_t* empty = full + OZ_STAGES;
+  uint64_t* accf = empty + OZ_STAGES;
+  uint64_t* acce = accf + 2;
+  uint64_t* drain = acce + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_tiles = P.tiles_m * P.tiles_n;
+  const int kblocks_full = (int)((P.kpad + OZ_BK - 1) / OZ_BK);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < OZ_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+    prefetch_tensormap(&mapA);
+    prefetch_tensormap(&mapB);
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_slot, OZ_TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  auto bounded = [&](uint64_t* bar, uint32_t phase, uint32_t site) -> bool {
+    for (uint32_t i = 0; i < NRS_WAIT_LIMIT; ++i) {
+      if (mbar_try_wait(bar, phase)) return true;
+      if (*abort_flag) return false;
+    }
+    *abort_flag = 1;
+    atomicOr(P.err, NRS_DEVERR_GEMM_TC | (site << 8));
+    return false;
+  };
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        int tm, tn;
+        tile_coords(tile, P, tm, tn);
+        for (int u = 0; u < P.n_pairs && ok; ++u) {
+          const PairOf pr = pair_of(u, P.slices, P.kchunks);
+          const int kb0 = pr.chunk * (OZ_KCHUNK / OZ_BK);
+          int kb1 = kb0 + OZ_KCHUNK / OZ_BK;
+          if (kb1 > kblocks_full) kb1 = kblocks_full;
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
+            const int s = it % OZ_STAGES;
+            const uint32_t ph = (it / OZ_STAGES) & 1;
+            if (!bounded(&empty[s], ph ^ 1, 1)) { ok = false; break; }
+            uint8_t* st = smem + s * OZ_STAGE_BYTES;
+            mbar_arrive_expect_tx(&full[s], OZ_STAGE_BYTES);
+            tma_load_3d(st, &mapA, &full[s], kb * OZ_BK, tm * OZ_BM, pr.s);
+            tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, tn * OZ_BN, pr.t);
+          }
+        }
+      }
+      if (!ok) {
+        // Drain: wait (bounded) for the copies still in flight.
+        for (uint32_t j = (it >= OZ_STAGES ? it - OZ_STAGES : 0); j < it; ++j)
+          mbar_wait_bounded(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1, 1u << 16);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t it = 0, ai = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        for (int u = 0; u < P.n_pairs && ok; ++u, ++ai) {
+          const PairOf pr = pair_of(u, P.slices, P.kchunks);
+          const int kb0 = pr.chunk * (OZ_KCHUNK / OZ_BK);
+          int kb1 = kb0 + OZ_KCHUNK / OZ_BK;
+          if (kb1 > kblocks_full) kb1 = kblocks_full;
+          const int buf = ai & 1;
+          const uint32_t aph = (ai >> 1) & 1;
+          if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t d_tmem = tmem_base + buf * OZ_BN;
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
+            const int s = it % OZ_STAGES;
+            const uint32_t ph = (it / OZ_STAGES) & 1;
+            if (!bounded(&full[s], ph, 3)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(smem + s * OZ_STAGE_BYTES);
+            const uint32_t b_addr = a_addr + OZ_A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+              tc_mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
+                          kIdesc, (kb > kb0 || kk > 0) ? 1u : 0u);
+            }
+            tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
+          }
+          if (!ok) break;
+          tc_commit(&accf[buf]);  // accumulator ready once every MMA above completes
+        }
+      }
+      // Make sure no MMA is still running before TMEM is released.
+      tc_commit(drain);
+      mbar_wait_bounded(drain, 0, 1u << 20);
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row_in_tile = q * 32 + lane;
+    uint32_t ai = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+      int tm, tn;
+      tile_coords(tile, P, tm, tn);
+      const int64_t row = (int64_t)tm * OZ_BM + row_in_tile;
+      const bool row_ok = row < P.m;
+      for (int u = 0; u < P.n_pairs; ++u, ++ai) {
+        const PairOf pr = pair_of(u, P.slices, P.kchunks);
+        const int buf = ai & 1;
+        const uint32_t aph = (ai >> 1) & 1;
+        if (!bounded(&accf[buf], aph, 4)) { ok = false; break; }
+        tc_fence_after();
+        const bool first = (u == 0), last = (u == P.n_pairs - 1);
+        const int shift = OZ_DIGIT_BITS * (P.slices - 1 - (pr.s + pr.t));
+        const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + buf * OZ_BN;
+        for (int c = 0; c < OZ_BN / 32; ++c) {
+          uint32_t v[32];
+          tmem_ld32(taddr + c * 32, v);
+          if (!row_ok) continue;
+          const int64_t col0 = (int64_t)tn * OZ_BN + c * 32;
+          __int128* accp = P.acc + row * P.n + col0;
+          int ecol_base = 0;
+          if (last) ecol_base = P.ea[row] + P.final_shift;
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            const int64_t col = col0 + e;
+            if (col >= P.n) continue;
+            const float f = __uint_as_float(v[e]);
+            const __int128 contrib = ((__int128)__float2int_rn(f)) << shift;
+            const __int128 sum = first ? contrib : (accp[e] + contrib);
+            if (!last) {
+              accp[e] = sum;
+            } else {
+              // |sum| < 2^127: keep its top 64 significant bits, convert once.
+              const bool neg = sum < 0;
+              unsigned __int128 mag = neg ? (unsigned __int128)(-sum) : (unsigned __int128)sum;
+              const uint64_t hi = (uint64_t)(mag >> 64);
+              int sh = 0;
+              if (hi) sh = 64 - __clzll((long long)hi);
+              const uint64_t top = (uint64_t)(mag >> sh);
+              double val = (double)top;
+              val = ldexp(val, sh + ecol_base + P.eb[col]);
+              P.C[row * P.ldc + col] = neg ? -val : val;
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, OZ_TMEM_COLS);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Scaling exponents and slicing
+// ---------------------------------------------------------------------------
+// frexp-style exponent of max |x| over a row (one warp per row).
+__global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda,
+                              int* __restrict__ ea) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= m) return;
+  uint64_t mx = 0;
+  for (int64_t j = lane; j < k; j += 32) {
+    uint64_t b = (uint64_t)__double_as_longlong(A[row * lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = b > mx ? b : mx;
+  }
+  for (int off = 16; off; off >>= 1) {
+    uint64_t o = __shfl_xor_sync(0xffffffffu, mx, off);
+    mx = o > mx ? o : mx;
+  }
+  if (lane == 0) {
+    int e = (int)(mx >> 52) - 1022;  // |max| < 2^e
+    if ((mx >> 52) == 0) e = -1021;  // zero or subnormal
+    ea[row] = e;
+  }
+}
+
+// Column exponents of B (k x n row-major): thread per column.
+__global__ void col_exponents(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
+                              int* __restrict__ eb) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= n) return;
+  uint64_t mx = 0;
+  for (int64_t i = 0; i < k; ++i) {
+    uint64_t b = (uint64_t)__double_as_longlong(B[i * ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = b > mx ? b : mx;
+  }
+  int e = (int)(mx >> 52) - 1022;
+  if ((mx >> 52) == 0) e = -1021;
+  eb[col] = e;
+}
+
+// Signed 6-bit digits of x * 2^-e (|x| < 2^e): see the file header.
+__device__ __forceinline__ void digits(double x, int e, int S, int16_t* out) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const bool neg = bits >> 63;
+  const int biased = (int)((bits >> 52) & 0x7FF);
+  uint64_t mant = bits & 0xFFFFFFFFFFFFFULL;
+  int E;
+  if (biased == 0) {
+    E = -1022 - 52;  // subnormal: x = mant * 2^-1074
+  } else {
+    mant |= 1ULL << 52;
+    E = biased - 1023 - 52;  // x = mant * 2^E
+  }
+  // X = x * 2^(126 - e) = mant * 2^(E + 126 - e)
+  const int sh = E + 126 - e;
+  __int128 X;
+  if (mant == 0) {
+    X = 0;
+  } else if (sh >= 0) {
+    X = (__int128)mant << sh;  // sh <= 73 because |x| < 2^e
+  } else if (sh > -64) {
+    X = (__int128)((mant + (1ULL << (-sh - 1))) >> (-sh));
+  } else {
+    X = 0;
+  }
+  if (neg) X = -X;
+  int p = 121;
+  for (int t = 0; t < S; ++t, p -= OZ_DIGIT_BITS) {
+    const __int128 d = (X + ((__int128)1 << (p - 1))) >> p;  // round to nearest (ties up)
+    X -= d << p;
+    out[t] = (int16_t)d;
+  }
+}
+
+__device__ __forceinline__ uint16_t bf16_of_int(int v) {
+  // |v| <= 32: exact in bf16; build it from the fp32 bit pattern.
+  const float f = (float)v;
+  return (uint16_t)(__float_as_uint(f) >> 16);
+}
+
+// A (m x k) -> slices [S][m][kpad], K-major; zero beyond k.
+__global__ void slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda,
+                           int64_t kpad, const int* __restrict__ ea, int S,
+                           uint16_t* __restrict__ out) {
+  const int64_t total = m * kpad;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / kpad, j = idx % kpad;
+    int16_t d[OZ_MAX_SLICES];
+    if (j < k) {
+      digits(A[i * lda + j], ea[i], S, d);
+    } else {
+      for (int t = 0; t < S; ++t) d[t] = 0;
+    }
+    for (int t = 0; t < S; ++t) out[(int64_t)t * m * kpad + idx] = bf16_of_int(d[t]);
+  }
+}
+
+// B (k x n row-major) -> slices of B^T [S][n][kpad], transposed through a
+// 32 x 32 shared tile so both the read of B and the write of B^T coalesce.
+__global__ void slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
+                           int64_t kpad, const int* __restrict__ eb, int S,
+                           uint16_t* __restrict__ out) {
+  __shared__ uint16_t tile[OZ_MAX_SLICES][32][33];
+  const int64_t k0 = (int64_t)blockIdx.y * 32, n0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t kk = k0 + r, nn = n0 + tx;
+    int16_t d[OZ_MAX_SLICES];
+    if (kk < k && nn < n) {
+      digits(B[kk * ldb + nn], eb[nn], S, d);
+    } else {
+      for (int t = 0; t < S; ++t) d[t] = 0;
+    }
+    for (int t = 0; t < S; ++t) tile[t][r][tx] = bf16_of_int(d[t]);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t nn = n0 + r, kk = k0 + tx;
+    if (nn < n && kk < kpad)
+      for (int t = 0; t < S; ++t) out[(int64_t)t * n * kpad + nn * kpad + kk] = tile[t][tx][r];
+  }
+}
+
+bool make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t rows, int S,
+                    uint32_t box_rows) {
+  auto enc = nrs_get_encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows, (cuuint64_t)S};
+  const cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)(kpad * rows * 2)};
+  const cuuint32_t box[3] = {OZ_BK, box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, const double* A,
+                              int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
+                              int slices, nrs_ozaki_info* info) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  if (m < 0 || k < 0 || n < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative GEMM dimension");
+  if (lda < (k > 0 ? k : 1) || ldb < (n > 0 ? n : 1) || ldc < (n > 0 ? n : 1))
+    return nrs_fail(h, NRS_ERR_SHAPE, "leading dimension too small");
+  if (slices < 0 || slices > OZ_MAX_SLICES)
+    return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
+  const int S = slices == 0 ? 9 : slices;
+  const int64_t kpad = ((k + 7) / 8) * 8;
+  const int kchunks = (int)((kpad + OZ_KCHUNK - 1) / OZ_KCHUNK);
+  const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
+  if (info) {
+    info->slices = S;
+    info->products = n_pairs;
+    info->slice_bits = OZ_DIGIT_BITS;
+    info->k_chunk = OZ_KCHUNK;
+    // truncation of both operands: 2 * 2^-(6 + 6(S-1)) relative to rowmax*colmax per term
+    info->est_rel_error = std::ldexp(2.0, -(6 + OZ_DIGIT_BITS * (S - 1)));
+  }
+  if (m == 0 || n == 0) return NRS_OK;
+  if (!A || !B || !C) return nrs_fail(h, NRS_ERR_INVALID, "null operand");
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
+  if (m > (1LL << 31) || n > (1LL << 31) || kpad > (1LL << 31))
+    return nrs_fail(h, NRS_ERR_TOO_LARGE, "dimension beyond 2^31");
+
+  // Workspace: exponents | A slices | B slices | int128 accumulators.
+  auto al = [](size_t v) { return (v + 1023) & ~size_t(1023); };
+  const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4);
+  const size_t sa_b = al((size_t)S * m * kpad * 2), sb_b = al((size_t)S * n * kpad * 2);
+  const size_t acc_b = al((size_t)m * n * 16);
+  uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + sa_b + sb_b + acc_b, &st);
+  if (!ws) return st;
+  int* ea = (int*)ws;
+  int* eb = (int*)(ws + ea_b);
+  uint16_t* sa = (uint16_t*)(ws + ea_b + eb_b);
+  uint16_t* sb = (uint16_t*)(ws + ea_b + eb_b + sa_b);
+  __int128* acc = (__int128*)(ws + ea_b + eb_b + sa_b + sb_b);
+  cudaStream_t s = h->stream;
+
+  row_exponents<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(A, m, k, lda, ea);
+  col_exponents<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, k, n, ldb, eb);
+  int grid = h->num_sms * 8;
+  slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
+  dim3 g2((unsigned)((n + 31) / 32), (unsigned)((kpad + 31) / 32));
+  slice_cols<<<g2, 256, 0, s>>>(B, k, n, ldb, kpad, eb, S, sb);
+  if ((st = nrs_after_launch(h, "ozaki slicing"))) return st;
+
+  CUtensorMap mapA, mapB;
+  if (!make_slice_map(&mapA, sa, kpad, m, S, OZ_BM) || !make_slice_map(&mapB, sb, kpad, n, S, OZ_BN))
+    return nrs_fail(h, NRS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the slices");
+
+  OzParams P{};
+  P.m = m;
+  P.n = n;
+  P.k = k;
+  P.kpad = kpad;
+  P.slices = S;
+  P.kchunks = kchunks;
+  P.n_pairs = n_pairs;
+  P.tiles_m = (int)((m + OZ_BM - 1) / OZ_BM);
+  P.tiles_n = (int)((n + OZ_BN - 1) / OZ_BN);
+  P.group_m = 12;
+  P.ea = ea;
+  P.eb = eb;
+  P.acc = acc;
+  P.C = C;
+  P.ldc = ldc;
+  P.final_shift = -10 - OZ_DIGIT_BITS * (S - 1);
+  P.err = h->dev_error;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if ((st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     OZ_SMEM),
+                             "cudaFuncSetAttribute(ozaki)")))
+      return st;
+    attr_set = true;
+  }
+  const int n_tiles = P.tiles_m * P.tiles_n;
+  const int ctas = n_tiles < h->num_sms ? n_tiles : h->num_sms;
+  ozaki_tc_kernel<<<ctas, OZ_THREADS, OZ_SMEM, s>>>(mapA, mapB, P);
+  return nrs_after_launch(h, "ozaki_tc_kernel");
+}

@@ -1,0 +1,708 @@
+// Axis folds and flat reductions.
+//
+// Axis folds (math::sum/mean/max/min(axis), Array::sum_axis) fold every
+// output lane sequentially, left to right, exactly as the reference's lane
+// loops do (src/math/aggregation.rs:555-561, src/math/statistics/mod.rs:1066,
+// src/math/aggregation.rs:250-263, src/array/operations.rs:137-153), so float
+// results carry the reference's rounding bit for bit. Sequential lanes give
+// far fewer independent loads than a tree, so the HBM stream is decoupled from
+// the folding threads with a TMA pipeline: a CTA owns a block of lanes and
+// walks the reduced axis through STAGES shared-memory tiles whose copies are
+// in flight while earlier tiles are folded.
+//
+//  * fold_cols_tma : lanes are adjacent in memory (stride 1), the axis is
+//                    strided -- e.g. axis 0 of a row-major matrix, or axis 1
+//                    of its transposed view. Tile = 256 B of lanes x 32 rows;
+//                    thread t folds column t of every tile.
+//  * fold_rows_tma : each lane is contiguous along the axis -- axis 1 of a
+//                    row-major matrix, axis 0 of its transposed view. Tile =
+//                    128 B along the axis x 64 lanes with the 128-byte
+//                    swizzle, so thread t reading its own row with 16-byte
+//                    loads is bank-conflict free.
+//  * fold_generic  : any strides, one thread per lane (small or unaligned
+//                    views).
+//
+// Flat reductions (kernels::reduce, src/kernels/reduce.rs:204-444) keep the
+// reference's 8192-element chunking: each chunk is summed by a lane-striped
+// tree, chunk partials go to workspace, and a single CTA folds them in chunk
+// order.
+#include <cfloat>
+#include <type_traits>
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "reduce_common.cuh"
+
+using namespace nrs_red;
+
+namespace {
+
+constexpr int kChunk = 8192;        // PARALLEL_CHUNK, src/kernels/mod.rs:92
+constexpr int kParallelMin = 10000; // PARALLEL_MIN_LEN, src/kernels/mod.rs:74
+constexpr int kVarParallelMin = 40000;  // VAR_PARALLEL_MIN_LEN, src/kernels/reduce.rs:202
+
+// ---------------------------------------------------------------------------
+// Generic strided fold: one thread per output lane.
+// ---------------------------------------------------------------------------
+struct KeptDims {
+  int n;
+  int64_t size[NRS_UFUNC_MAX_DIMS];
+  int64_t stride[NRS_UFUNC_MAX_DIMS];
+};
+
+template <typename T, int OP>
+__global__ void fold_generic(const T* __restrict__ x, KeptDims kd, int64_t n_out, int64_t alen,
+                             int64_t astride, typename OutOf<T, OP>::type* __restrict__ out) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
+       o += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = o, base = 0;
+    for (int d = kd.n - 1; d >= 0; --d) {
+      int64_t c = rem % kd.size[d];
+      rem /= kd.size[d];
+      base += c * kd.stride[d];
+    }
+    const T* p = x + base;
+    T acc = Fold<T, OP>::init();
+    for (int64_t j = 0; j < alen; ++j) acc = Fold<T, OP>::step(acc, p[j * astride]);
+    out[o] = finish<T, OP>(acc, alen);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA pipelines
+// ---------------------------------------------------------------------------
+// Shared-memory layout: STAGES tiles (1024-byte aligned) then STAGES mbarriers.
+template <int TILE_BYTES, int STAGES>
+struct PipeSmem {
+  static constexpr int kBytes = TILE_BYTES * STAGES + 8 * STAGES + 1024;  // + alignment slack
+};
+
+// Lanes adjacent (stride 1), axis strided. Tensor map dims (lanes, axis,
+// batch), box (LW, RB, 1), no swizzle: tile row r holds lanes [l0, l0+LW) of
+// axis position y0 + r.
+template <typename T, int OP, int STAGES>
+__global__ void __launch_bounds__(256 / sizeof(T))
+    fold_cols_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
+                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err) {
+  constexpr int LW = 256 / sizeof(T);  // lanes per tile (= threads)
+  constexpr int RB = 32;               // axis positions per tile
+  constexpr int TILE = LW * RB * sizeof(T);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TILE * STAGES);
+  __shared__ int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * LW;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + RB - 1) / RB;
+
+  if (t == 0) {
+    prefetch_tensormap(&map);
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int s = 0; s < STAGES && s < n_tiles; ++s) {
+      mbar_arrive_expect_tx(&full[s], TILE);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
+    }
+  }
+  T acc = Fold<T, OP>::init();
+  int64_t it = 0;
+  for (; it < n_tiles; ++it) {
+    const int s = (int)(it % STAGES);
+    const uint32_t phase = (uint32_t)((it / STAGES) & 1);
+    if (!mbar_wait_bounded(&full[s], phase, NRS_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) break;
+    const T* tile = reinterpret_cast<const T*>(smem + s * TILE);
+    const int64_t y0 = it * RB;
+    const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
+    if (cnt == RB) {
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc = Fold<T, OP>::step(acc, tile[r * LW + t]);
+    } else {
+      for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, tile[r * LW + t]);
+    }
+    __syncthreads();  // every thread is done with stage s
+    if (t == 0 && it + STAGES < n_tiles) {
+      mbar_arrive_expect_tx(&full[s], TILE);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)((it + STAGES) * RB),
+                  batch);
+    }
+  }
+  if (abort_flag) {
+    // Drain: wait (bounded) for every copy this CTA issued and has not consumed.
+    if (t == 0) {
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (1u << 8));
+      for (int64_t j = it; j < n_tiles && j < it + STAGES; ++j)
+        mbar_wait_bounded(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), NRS_WAIT_LIMIT);
+    }
+    return;
+  }
+  const int64_t lane = l0 + t;
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen);
+}
+
+// Lanes contiguous along the axis. Tensor map dims (axis, lanes, batch), box
+// (128 B of axis, 64 lanes, 1), 128-byte swizzle: 16-byte chunk j of tile
+// row r sits at r*128 + ((j ^ (r & 7)) * 16).
+template <typename T, int OP, int STAGES>
+__global__ void __launch_bounds__(64)
+    fold_rows_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
+                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err) {
+  constexpr int LN = 64;                  // lanes per tile (= threads)
+  constexpr int XB = 128 / sizeof(T);     // axis elements per tile row
+  constexpr int PER16 = 16 / sizeof(T);   // elements per 16-byte chunk
+  constexpr int TILE = LN * 128;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TILE * STAGES);
+  __shared__ int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * LN;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + XB - 1) / XB;
+
+  if (t == 0) {
+    prefetch_tensormap(&map);
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int s = 0; s < STAGES && s < n_tiles; ++s) {
+      mbar_arrive_expect_tx(&full[s], TILE);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
+    }
+  }
+  T acc = Fold<T, OP>::init();
+  const int sw = t & 7;
+  int64_t it = 0;
+  for (; it < n_tiles; ++it) {
+    const int s = (int)(it % STAGES);
+    const uint32_t phase = (uint32_t)((it / STAGES) & 1);
+    if (!mbar_wait_bounded(&full[s], phase, NRS_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) break;
+    const uint8_t* row = smem + s * TILE + t * 128;
+    const int64_t x0 = it * XB;
+    const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
+    if (cnt == XB) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const T* c = reinterpret_cast<const T*>(row + ((j ^ sw) << 4));
+        T v[PER16];
+        if constexpr (sizeof(T) == 4) {
+          float4 q = *reinterpret_cast<const float4*>(c);
+          memcpy(v, &q, 16);
+        } else {
+          double2 q = *reinterpret_cast<const double2*>(c);
+          memcpy(v, &q, 16);
+        }
+#pragma unroll
+        for (int e = 0; e < PER16; ++e) acc = Fold<T, OP>::step(acc, v[e]);
+      }
+    } else {
+      for (int e = 0; e < cnt; ++e) {
+        const int j = e / PER16;
+        const T* c = reinterpret_cast<const T*>(row + ((j ^ sw) << 4));
+        acc = Fold<T, OP>::step(acc, c[e % PER16]);
+      }
+    }
+    __syncthreads();
+    if (t == 0 && it + STAGES < n_tiles) {
+      mbar_arrive_expect_tx(&full[s], TILE);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)((it + STAGES) * XB), (int32_t)l0,
+                  batch);
+    }
+  }
+  if (abort_flag) {
+    if (t == 0) {
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (2u << 8));
+      for (int64_t j = it; j < n_tiles && j < it + STAGES; ++j)
+        mbar_wait_bounded(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), NRS_WAIT_LIMIT);
+    }
+    return;
+  }
+  const int64_t lane = l0 + t;
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen);
+}
+
+constexpr int kStages = 8;
+
+// ---------------------------------------------------------------------------
+// Flat reductions
+// ---------------------------------------------------------------------------
+// Per-chunk partials. Thread t folds elements t, t+256, ... of its chunk
+// (lane-striped, the shape of a SIMD sum), then the block combines. MIN/MAX
+// fold with a NaN flag and ignore NaNs in the value, as chunk_min/chunk_max
+// do (src/kernels/reduce.rs:337-350). SSD folds (x - mean)^2.
+template <typename T, int OP, bool SSD>
+__global__ void __launch_bounds__(256)
+    flat_partials(const T* __restrict__ x, int64_t n, int64_t chunk, const T* mean_ptr,
+                  Partial<T>* __restrict__ part) {
+  __shared__ T sh[8];
+  __shared__ int shn[8];
+  const int64_t nchunks = (n + chunk - 1) / chunk;
+  const T mean = SSD ? *mean_ptr : T(0);
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const int64_t lo = c * chunk;
+    const int64_t len = (n - lo) < chunk ? (n - lo) : chunk;
+    T acc = Fold<T, OP>::init();
+    int nan = 0;
+    for (int64_t i = threadIdx.x; i < len; i += 256) {
+      T v = x[lo + i];
+      if constexpr (SSD) {
+        T d = v - mean;
+        v = d * d;
+      }
+      if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+        nan |= is_nan(v);
+        if (!is_nan(v)) acc = Fold<T, OP>::step(acc, v);
+      } else {
+        acc = Fold<T, OP>::step(acc, v);
+      }
+    }
+    T r = block_combine<T, OP>(acc, sh);
+    int anynan = __syncthreads_or(nan);
+    (void)shn;
+    if (threadIdx.x == 0) part[c] = Partial<T>{r, anynan};
+  }
+}
+
+// Folds the chunk partials in chunk order (the reference's sequential fold of
+// the collected Vec). Runs of consecutive partials per thread first when there
+// are more than 1024 chunks; 1024 or fewer are folded by one thread in order.
+// `fin_op` says what to write: the folded value (SUM/MAX/MIN/PROD), the mean
+// (MEAN; f64 for integers), the mean into `mean_out` for the variance's second
+// pass (-1), or VAR/STD from the folded squared deviations.
+template <typename T, int OP>
+__global__ void __launch_bounds__(1024)
+    flat_finish(const Partial<T>* __restrict__ part, int64_t nchunks, int64_t n, int fin_op,
+                double ddof, T* mean_out, void* out) {
+  __shared__ T run[1024];
+  __shared__ int runnan[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (nchunks + 1023) / 1024;
+  T acc = Fold<T, OP>::init();
+  int nan = 0;
+  for (int64_t i = t * per; i < (t + 1) * per && i < nchunks; ++i) {
+    acc = Fold<T, OP>::step(acc, part[i].v);
+    nan |= part[i].nan;
+  }
+  run[t] = acc;
+  runnan[t] = nan;
+  __syncthreads();
+  if (t != 0) return;
+  T r = Fold<T, OP>::init();
+  int anynan = 0;
+  for (int i = 0; i < 1024; ++i) {
+    if ((int64_t)i * per >= nchunks) break;
+    r = Fold<T, OP>::step(r, run[i]);
+    anynan |= runnan[i];
+  }
+  if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+    if constexpr (std::is_floating_point<T>::value) {
+      if (anynan) r = (T)NAN;
+    }
+    static_cast<T*>(out)[0] = r;
+  } else if constexpr (OP == NRS_SUM) {
+    if (fin_op == NRS_SUM) {
+      static_cast<T*>(out)[0] = r;
+    } else if (fin_op == NRS_MEAN) {
+      if constexpr (std::is_floating_point<T>::value)
+        static_cast<T*>(out)[0] = r / (T)n;
+      else
+        static_cast<double*>(out)[0] = (double)r / (double)n;
+    } else if constexpr (std::is_floating_point<T>::value) {
+      if (fin_op == -1) {
+        *mean_out = r / (T)n;
+      } else {  // VAR / STD from the sum of squared deviations
+        T var = r / ((T)n - (T)ddof);
+        static_cast<T*>(out)[0] = (fin_op == NRS_STD) ? sqrt(var) : var;
+      }
+    }
+  } else {
+    static_cast<T*>(out)[0] = r;
+  }
+}
+
+template <typename T>
+__global__ void write_scalar(T* out, T v) { out[0] = v; }
+
+// Logical-order gather of a non-contiguous view into a contiguous buffer
+// (kernels::borrow::operand, src/kernels/borrow.rs:59).
+template <typename T>
+__global__ void gather_view(const T* __restrict__ x, KeptDims kd, int64_t n, T* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = i, off = 0;
+    for (int d = kd.n - 1; d >= 0; --d) {
+      int64_t c = rem % kd.size[d];
+      rem /= kd.size[d];
+      off += c * kd.stride[d];
+    }
+    y[i] = x[off];
+  }
+}
+
+template <typename T>
+__global__ void fill_value(T* out, int64_t n, T v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Host dispatch
+// ---------------------------------------------------------------------------
+CUtensorMapDataType tma_dtype(int dtype) {
+  switch (dtype) {
+    case NRS_F32: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    case NRS_F64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    case NRS_I32: return CU_TENSOR_MAP_DATA_TYPE_INT32;
+    default: return CU_TENSOR_MAP_DATA_TYPE_INT64;
+  }
+}
+
+struct AxisProblem {
+  int dtype, op;
+  const void* x;
+  void* out;
+  int64_t alen, astride;
+  KeptDims kept;  // collapsed kept dims, outer to inner
+  int64_t n_out;
+};
+
+template <typename T, int OP>
+int launch_generic(nrs_handle* h, const AxisProblem& p) {
+  int64_t blocks = (p.n_out + 255) / 256;
+  int grid = (int)(blocks < (int64_t)h->num_sms * 16 ? blocks : (int64_t)h->num_sms * 16);
+  if (grid < 1) grid = 1;
+  fold_generic<T, OP><<<grid, 256, 0, h->stream>>>(
+      (const T*)p.x, p.kept, p.n_out, p.alen, p.astride, (typename OutOf<T, OP>::type*)p.out);
+  return nrs_after_launch(h, "fold_generic");
+}
+
+// Builds a 3-D tensor map (dim0 contiguous). Returns false if TMA rules are
+// not met (base or strides not multiples of 16 bytes, sizes beyond limits).
+bool make_map(CUtensorMap* map, int dtype, const void* base, const uint64_t dims[3],
+              const uint64_t strides_bytes[2], const uint32_t box[3], CUtensorMapSwizzle sw) {
+  auto enc = nrs_get_encode_tiled();
+  if (!enc) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+  for (int i = 0; i < 2; ++i)
+    if ((strides_bytes[i] & 15) != 0 || strides_bytes[i] >= (1ull << 40) || strides_bytes[i] == 0)
+      return false;
+  for (int i = 0; i < 3; ++i)
+    if (dims[i] == 0 || dims[i] > (1ull << 32)) return false;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, tma_dtype(dtype), 3, const_cast<void*>(base), dims, strides_bytes, box,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Tries the TMA kernels for a (batch, lanes) x axis problem. Returns
+// NRS_ERR_UNSUPPORTED (nothing launched) when the view does not qualify.
+template <typename T, int OP>
+int launch_tma(nrs_handle* h, const AxisProblem& p) {
+  const int es = sizeof(T);
+  const KeptDims& k = p.kept;
+  if (k.n < 1 || k.n > 2 || p.alen < 1) return NRS_ERR_UNSUPPORTED;
+  const int64_t lanes = k.size[k.n - 1], lstride = k.stride[k.n - 1];
+  const int64_t batch = (k.n == 2) ? k.size[0] : 1;
+  const int64_t bstride = (k.n == 2) ? k.stride[0] : 0;
+  if (batch > 65535) return NRS_ERR_UNSUPPORTED;
+  CUtensorMap map;
+  const size_t tile_bytes = 8192;
+  const size_t smem = PipeSmem<8192, kStages>::kBytes;
+  using OutT = typename OutOf<T, OP>::type;
+  if (lstride == 1 && p.astride > 1) {
+    // Columns: dims (lanes, axis, batch).
+    const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
+    uint64_t sb = (uint64_t)(batch > 1 ? bstride : p.astride * p.alen) * es;
+    const uint64_t strides[2] = {(uint64_t)p.astride * es, sb};
+    const uint32_t box[3] = {(uint32_t)(256 / es), 32, 1};
+    if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
+      return NRS_ERR_UNSUPPORTED;
+    auto kern = fold_cols_tma<T, OP, kStages>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((unsigned)((lanes + 256 / es - 1) / (256 / es)), (unsigned)batch);
+    kern<<<grid, 256 / es, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
+    return nrs_after_launch(h, "fold_cols_tma");
+  }
+  if (p.astride == 1 && lstride > 1) {
+    // Rows: dims (axis, lanes, batch), 128-byte swizzle.
+    const uint64_t dims[3] = {(uint64_t)p.alen, (uint64_t)lanes, (uint64_t)batch};
+    uint64_t sb = (uint64_t)(batch > 1 ? bstride : lstride * lanes) * es;
+    const uint64_t strides[2] = {(uint64_t)lstride * es, sb};
+    const uint32_t box[3] = {(uint32_t)(128 / es), 64, 1};
+    if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+      return NRS_ERR_UNSUPPORTED;
+    auto kern = fold_rows_tma<T, OP, kStages>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
+    return nrs_after_launch(h, "fold_rows_tma");
+  }
+  (void)tile_bytes;
+  return NRS_ERR_UNSUPPORTED;
+}
+
+template <typename T, int OP>
+int dispatch_axis_t(nrs_handle* h, const AxisProblem& p) {
+  // The TMA pipelines pay off once lanes are long enough to fill a pipeline.
+  if (p.alen >= 256 && p.n_out >= 64) {
+    int st = launch_tma<T, OP>(h, p);
+    if (st != NRS_ERR_UNSUPPORTED) return st;
+  }
+  return launch_generic<T, OP>(h, p);
+}
+
+template <typename T>
+int dispatch_axis_ops(nrs_handle* h, const AxisProblem& p) {
+  switch (p.op) {
+    case NRS_SUM: return dispatch_axis_t<T, NRS_SUM>(h, p);
+    case NRS_MEAN: return dispatch_axis_t<T, NRS_MEAN>(h, p);
+    case NRS_MAX: return dispatch_axis_t<T, NRS_MAX>(h, p);
+    case NRS_MIN: return dispatch_axis_t<T, NRS_MIN>(h, p);
+    case NRS_PROD: return dispatch_axis_t<T, NRS_PROD>(h, p);
+    default: return nrs_fail(h, NRS_ERR_UNSUPPORTED, "axis VAR/STD are not provided");
+  }
+}
+
+// Flat reduction of a contiguous buffer.
+template <typename T>
+int flat_reduce(nrs_handle* h, int op, int64_t n, int64_t ddof, const T* x, void* out) {
+  // Tiering (src/kernels/reduce.rs): SUM/MEAN one simd_sum below 10k, else
+  // 8192 chunks; VAR below 40k one pass each, else chunks; MIN/MAX and PROD
+  // chunking does not change their result, so they always use 8192 chunks.
+  int64_t chunk;
+  if (op == NRS_VAR || op == NRS_STD)
+    chunk = (n < kVarParallelMin) ? (n > 0 ? n : 1) : kChunk;
+  else if (op == NRS_SUM || op == NRS_MEAN)
+    chunk = (n < kParallelMin) ? (n > 0 ? n : 1) : kChunk;
+  else
+    chunk = kChunk;
+  const int64_t nchunks = n > 0 ? (n + chunk - 1) / chunk : 0;
+  int st;
+  size_t need = (size_t)(nchunks + 1) * sizeof(Partial<T>) + 256;
+  uint8_t* ws = (uint8_t*)nrs_workspace(h, need, &st);
+  if (!ws) return st;
+  Partial<T>* part = reinterpret_cast<Partial<T>*>(ws);
+  T* mean_slot = reinterpret_cast<T*>(ws + (size_t)(nchunks + 1) * sizeof(Partial<T>));
+  int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
+  if (grid < 1) grid = 1;
+  if (n == 0) {
+    T v = (op == NRS_PROD) ? T(1) : T(0);
+    write_scalar<T><<<1, 1, 0, h->stream>>>((T*)out, v);
+    return nrs_after_launch(h, "write_scalar");
+  }
+  switch (op) {
+    case NRS_SUM:
+    case NRS_MEAN:
+      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    case NRS_VAR:
+    case NRS_STD:
+      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, -1, 0.0, mean_slot, nullptr);
+      flat_partials<T, NRS_SUM, true><<<grid, 256, 0, h->stream>>>(x, n, chunk, mean_slot, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, (double)ddof, nullptr, out);
+      break;
+    case NRS_MAX:
+      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_MAX><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    case NRS_MIN:
+      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_MIN><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    case NRS_PROD:
+      flat_partials<T, NRS_PROD, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_PROD><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    default:
+      return nrs_fail(h, NRS_ERR_INVALID, "unknown reduce op");
+  }
+  return nrs_after_launch(h, "flat reduction");
+}
+
+// Integer flat reductions: any order is exact. MEAN writes f64.
+template <typename T>
+int flat_reduce_int(nrs_handle* h, int op, int64_t n, const T* x, void* out) {
+  if (op != NRS_SUM && op != NRS_MAX && op != NRS_MIN && op != NRS_PROD && op != NRS_MEAN)
+    return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
+  if (n == 0) {
+    if (op == NRS_MEAN) {
+      write_scalar<double><<<1, 1, 0, h->stream>>>((double*)out, 0.0);
+    } else {
+      write_scalar<T><<<1, 1, 0, h->stream>>>((T*)out, op == NRS_PROD ? T(1) : T(0));
+    }
+    return nrs_after_launch(h, "write_scalar");
+  }
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  int st;
+  Partial<T>* part = (Partial<T>*)nrs_workspace(h, (size_t)(nchunks + 1) * sizeof(Partial<T>), &st);
+  if (!part) return st;
+  int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
+  switch (op) {
+    case NRS_SUM:
+      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_SUM, 0.0, nullptr, out);
+      break;
+    case NRS_MEAN:
+      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MEAN, 0.0, nullptr, out);
+      break;
+    case NRS_MAX:
+      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      flat_finish<T, NRS_MAX><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MAX, 0.0, nullptr, out);
+      break;
+    case NRS_MIN:
+      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      flat_finish<T, NRS_MIN><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MIN, 0.0, nullptr, out);
+      break;
+    default:
+      flat_partials<T, NRS_PROD, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      flat_finish<T, NRS_PROD><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_PROD, 0.0, nullptr, out);
+      break;
+  }
+  return nrs_after_launch(h, "flat integer reduction");
+}
+
+}  // namespace
+
+extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+                          const int64_t* strides, int64_t axis, int64_t ddof, const void* x,
+                          void* out) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  if (ndim < 0 || ndim > NRS_UFUNC_MAX_DIMS || (ndim > 0 && (!shape || !strides)) || !out)
+    return nrs_fail(h, NRS_ERR_INVALID, "bad ndim/shape/strides/out");
+  if (op < NRS_SUM || op > NRS_STD) return nrs_fail(h, NRS_ERR_INVALID, "unknown reduce op");
+  const size_t es = nrs_dtype_size(dtype);
+  if (!es) return nrs_fail(h, NRS_ERR_DTYPE, "unknown dtype");
+  const bool is_int = (dtype == NRS_I32 || dtype == NRS_I64);
+  int64_t total = 1;
+  for (int d = 0; d < ndim; ++d) {
+    if (shape[d] < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative dimension");
+    if (strides[d] < 0) return nrs_fail(h, NRS_ERR_STRIDE, "negative stride");
+    total *= shape[d];
+  }
+  if (total > 0 && !x) return nrs_fail(h, NRS_ERR_INVALID, "null input");
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+
+  if (axis == NRS_AXIS_NONE) {
+    if (is_int && (op == NRS_VAR || op == NRS_STD))
+      return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
+    // Non-contiguous views are gathered into logical order first, as
+    // kernels::borrow::operand does.
+    bool contig = true;
+    int64_t expect = 1;
+    for (int d = ndim - 1; d >= 0; --d) {
+      if (shape[d] != 1 && strides[d] != expect) contig = false;
+      expect *= shape[d];
+    }
+    const void* src = x;
+    if (!contig && total > 0) {
+      KeptDims kd{};
+      kd.n = ndim;
+      for (int d = 0; d < ndim; ++d) {
+        kd.size[d] = shape[d];
+        kd.stride[d] = strides[d];
+      }
+      // Reserve the gathered copy past the partials area of the workspace.
+      size_t part_bytes = ((size_t)(total / kChunk + 2) * 16 + 4096 + 255) & ~size_t(255);
+      uint8_t* ws = (uint8_t*)nrs_workspace(h, part_bytes + (size_t)total * es, &st);
+      if (!ws) return st;
+      void* dst = ws + part_bytes;
+      int grid = h->num_sms * 8;
+      if (es == 4)
+        gather_view<uint32_t><<<grid, 256, 0, h->stream>>>((const uint32_t*)x, kd, total, (uint32_t*)dst);
+      else
+        gather_view<uint64_t><<<grid, 256, 0, h->stream>>>((const uint64_t*)x, kd, total, (uint64_t*)dst);
+      if ((st = nrs_after_launch(h, "gather_view"))) return st;
+      src = dst;
+      // The flat kernels must not reuse the gathered region as partials: the
+      // workspace is large enough that their partials (at offset 0) fit below.
+    }
+    switch (dtype) {
+      case NRS_F32: return flat_reduce<float>(h, op, total, ddof, (const float*)src, out);
+      case NRS_F64: return flat_reduce<double>(h, op, total, ddof, (const double*)src, out);
+      case NRS_I64: return flat_reduce_int<int64_t>(h, op, total, (const int64_t*)src, out);
+      default: return flat_reduce_int<int32_t>(h, op, total, (const int32_t*)src, out);
+    }
+  }
+
+  if (ndim == 0) return nrs_fail(h, NRS_ERR_AXIS, "axis given for a 0-d array");
+  int64_t ax = axis < 0 ? axis + ndim : axis;
+  if (ax < 0 || ax >= ndim) {
+    return nrs_fail(h, NRS_ERR_AXIS, "Axis " + std::to_string(axis) +
+                                         " out of bounds for array of dimension " +
+                                         std::to_string(ndim));
+  }
+  if (op == NRS_VAR || op == NRS_STD)
+    return nrs_fail(h, NRS_ERR_UNSUPPORTED, "axis VAR/STD are not provided");
+  if (is_int && op == NRS_MEAN && dtype == NRS_I32)
+    return nrs_fail(h, NRS_ERR_DTYPE, "i32 MEAN is not provided");
+
+  AxisProblem p{};
+  p.dtype = dtype;
+  p.op = op;
+  p.x = x;
+  p.out = out;
+  p.alen = shape[ax];
+  p.astride = strides[ax];
+  // Collapse kept dims (outer to inner), dropping size-1 dims.
+  KeptDims kd{};
+  kd.n = 0;
+  int64_t n_out = 1;
+  for (int d = 0; d < ndim; ++d) {
+    if (d == ax) continue;
+    n_out *= shape[d];
+    if (shape[d] == 1) continue;
+    if (kd.n > 0 && kd.stride[kd.n - 1] == strides[d] * shape[d]) {
+      kd.size[kd.n - 1] *= shape[d];
+      kd.stride[kd.n - 1] = strides[d];
+    } else {
+      kd.size[kd.n] = shape[d];
+      kd.stride[kd.n] = strides[d];
+      kd.n++;
+    }
+  }
+  p.kept = kd;
+  p.n_out = n_out;
+  if (total == 0) {
+    if (n_out == 0 && (op == NRS_SUM || op == NRS_PROD)) return NRS_OK;
+    // Empty array: math::sum gives zeros; max/min/mean error out.
+    if (op == NRS_SUM || op == NRS_PROD) {
+      int grid = h->num_sms * 4;
+      if (dtype == NRS_F32) fill_value<float><<<grid, 256, 0, h->stream>>>((float*)out, n_out, op == NRS_PROD ? 1.f : 0.f);
+      else if (dtype == NRS_F64) fill_value<double><<<grid, 256, 0, h->stream>>>((double*)out, n_out, op == NRS_PROD ? 1.0 : 0.0);
+      else if (dtype == NRS_I64) fill_value<int64_t><<<grid, 256, 0, h->stream>>>((int64_t*)out, n_out, op == NRS_PROD ? 1 : 0);
+      else fill_value<int32_t><<<grid, 256, 0, h->stream>>>((int32_t*)out, n_out, op == NRS_PROD ? 1 : 0);
+      return nrs_after_launch(h, "fill_value");
+    }
+    return nrs_fail(h, NRS_ERR_EMPTY, "Cannot reduce an empty array");
+  }
+  switch (dtype) {
+    case NRS_F32: return dispatch_axis_ops<float>(h, p);
+    case NRS_F64: return dispatch_axis_ops<double>(h, p);
+    case NRS_I64: return dispatch_axis_ops<int64_t>(h, p);
+    default: {
+      if (op == NRS_MEAN) return nrs_fail(h, NRS_ERR_DTYPE, "i32 MEAN is not provided");
+      return dispatch_axis_ops<int32_t>(h, p);
+    }
+  }
+}

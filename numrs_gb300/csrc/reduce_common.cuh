@@ -1,0 +1,120 @@
+// Fold operators and block-level combine shared by the reduction kernels
+// (reduce.cu) and the persistent grouped kernel (grouped.cu), so a row
+// reduced inside a grouped launch is bit-identical to the same row reduced
+// by nrs_reduce.
+#pragma once
+
+#include <climits>
+#include <cmath>
+#include <type_traits>
+
+#include "nrs_internal.cuh"
+
+namespace nrs_red {
+
+// ---------------------------------------------------------------------------
+// Fold operators
+// ---------------------------------------------------------------------------
+template <typename T> struct Lim;
+template <> struct Lim<float> {
+  static __device__ __forceinline__ float lowest() { return -INFINITY; }
+  static __device__ __forceinline__ float highest() { return INFINITY; }
+};
+template <> struct Lim<double> {
+  static __device__ __forceinline__ double lowest() { return -INFINITY; }
+  static __device__ __forceinline__ double highest() { return INFINITY; }
+};
+template <> struct Lim<int64_t> {
+  static __device__ __forceinline__ int64_t lowest() { return LLONG_MIN; }
+  static __device__ __forceinline__ int64_t highest() { return LLONG_MAX; }
+};
+template <> struct Lim<int32_t> {
+  static __device__ __forceinline__ int32_t lowest() { return INT_MIN; }
+  static __device__ __forceinline__ int32_t highest() { return INT_MAX; }
+};
+
+template <typename T> __device__ __forceinline__ bool is_nan(T v) { return v != v; }
+
+// Lane fold step. MAX/MIN: the accumulator starts at -inf/+inf, so the first
+// element always replaces it (or keeps it, bitwise equal, when it is the same
+// infinity); a NaN accumulator is sticky, so the first NaN of the lane is the
+// result -- the reference's short-circuit on `is_unordered(&val)`.
+template <typename T, int OP>
+struct Fold {
+  static __device__ __forceinline__ T init() {
+    if (OP == NRS_MAX) return Lim<T>::lowest();
+    if (OP == NRS_MIN) return Lim<T>::highest();
+    if (OP == NRS_PROD) return T(1);
+    return T(0);
+  }
+  static __device__ __forceinline__ T step(T acc, T v) {
+    if (OP == NRS_MAX) return (!is_nan(acc) && (is_nan(v) || v > acc)) ? v : acc;
+    if (OP == NRS_MIN) return (!is_nan(acc) && (is_nan(v) || v < acc)) ? v : acc;
+    if (OP == NRS_PROD) return mul(acc, v);
+    return add(acc, v);
+  }
+  // Integer sums/products wrap (two's complement), float ones round once.
+  static __device__ __forceinline__ T add(T a, T b) {
+    if constexpr (sizeof(T) == 8 && !std::is_floating_point<T>::value)
+      return (T)((unsigned long long)a + (unsigned long long)b);
+    else if constexpr (sizeof(T) == 4 && !std::is_floating_point<T>::value)
+      return (T)((unsigned)a + (unsigned)b);
+    else
+      return a + b;
+  }
+  static __device__ __forceinline__ T mul(T a, T b) {
+    if constexpr (sizeof(T) == 8 && !std::is_floating_point<T>::value)
+      return (T)((unsigned long long)a * (unsigned long long)b);
+    else if constexpr (sizeof(T) == 4 && !std::is_floating_point<T>::value)
+      return (T)((unsigned)a * (unsigned)b);
+    else
+      return a * b;
+  }
+};
+
+// Output of a lane: MEAN divides by the axis length in T (f64 for integers).
+template <typename T, int OP> struct OutOf { using type = T; };
+template <> struct OutOf<int64_t, NRS_MEAN> { using type = double; };
+template <> struct OutOf<int32_t, NRS_MEAN> { using type = double; };
+
+template <typename T, int OP>
+__device__ __forceinline__ typename OutOf<T, OP>::type finish(T acc, int64_t n) {
+  if constexpr (OP == NRS_MEAN) {
+    if constexpr (std::is_floating_point<T>::value)
+      return acc / (T)n;
+    else
+      return (double)acc / (double)n;
+  } else {
+    return acc;
+  }
+}
+
+// Partial of one chunk: value plus a NaN flag (min/max only).
+template <typename T>
+struct Partial {
+  T v;
+  int nan;
+};
+
+// Block-wide tree combine of per-thread values (fixed shape: warp butterfly,
+// then the 8 warp results in order), result valid in thread 0.
+template <typename T, int OP>
+__device__ __forceinline__ T block_combine(T v, T* sh) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    T o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = Fold<T, OP>::step(v, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  T r = v;
+  if (threadIdx.x == 0) {
+    r = sh[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = Fold<T, OP>::step(r, sh[i]);
+  }
+  __syncthreads();
+  return r;
+}
+
+}  // namespace nrs_red

@@ -1,0 +1,157 @@
+"""Pins the CPU oracle to the reference's own known answers (CPU only).
+
+* Bit patterns pinned by tests/test_reduction_determinism.rs:126-197.
+* NumPy goldens of tests/py/array_operations_reference_data.json (read by
+  tests/test_array_operations_reference.rs, tolerance 1e-15).
+* NaN-placement and empty-input conventions of src/kernels/reduce.rs:843-925,
+  :578-589.
+* GEMM against a double-double oracle on the size grid of
+  src/kernels/gemm.rs:499-513.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+
+
+def _x(dtype):
+    n = GOLD["determinism"]["n"]
+    return (np.arange(n, dtype=dtype) * dtype(0.5) - dtype(12345)).astype(dtype)
+
+
+@pytest.mark.parametrize("name", sorted(GOLD["determinism"]["pins"]))
+def test_determinism_pins(ora, name):
+    pin = GOLD["determinism"]["pins"][name]
+    if name == "sum_f32":
+        got = np.float32(ora.flat("sum", _x(np.float32)))
+    elif name == "sum_f64":
+        got = np.float64(ora.flat("sum", _x(np.float64)))
+    elif name == "mean_f64":
+        got = np.float64(ora.flat("mean", _x(np.float64)))
+    elif name == "var_f64_ddof0":
+        got = np.float64(ora.flat("var", _x(np.float64), 0))
+    else:
+        got = np.sqrt(np.float64(ora.flat("var", _x(np.float64), 0)))
+    width = {32: np.uint32, 64: np.uint64}[pin["width"]]
+    assert int(np.array(got).view(width)) == pin["bits"]
+
+
+def _arr(d):
+    return np.array(d["data"], dtype=np.float64).reshape(d["shape"])
+
+
+@pytest.mark.parametrize("key", sorted(GOLD["statistical_operations"]))
+def test_numpy_stat_goldens(ora, key):
+    case = GOLD["statistical_operations"][key]
+    x = _arr(case["input"])
+    op = case["operation"]
+    axis = case["axis"]
+    if axis is None:
+        if op in ("var", "std"):
+            got = ora.flat("var", x.ravel(), 0)
+            if op == "std":
+                got = np.sqrt(got)
+        else:
+            got = ora.flat(op, x.ravel())
+        np.testing.assert_allclose(got, case["result"], rtol=1e-15, atol=1e-15)
+    else:
+        code = {"sum": O.SUM, "mean": O.MEAN, "max": O.MAX, "min": O.MIN}.get(op)
+        if code is None:  # var/std along an axis: mean-of-squares from two axis folds
+            mu = ora.axis(O.MEAN, x, axis)
+            d = x - np.expand_dims(mu, axis)
+            got = ora.axis(O.MEAN, d * d, axis)
+            if op == "std":
+                got = np.sqrt(got)
+        else:
+            got = ora.axis(code, x, axis)
+        np.testing.assert_allclose(got, _arr(case["result"]).ravel(), rtol=1e-15, atol=1e-15)
+
+
+@pytest.mark.parametrize("key", sorted(GOLD["mathematical_functions"]))
+def test_numpy_exp_goldens(ora, key):
+    case = GOLD["mathematical_functions"][key]
+    x = _arr(case["input"])
+    got = ora.exp_affine(x.ravel(), 1.0, 0.0)
+    np.testing.assert_allclose(got, _arr(case["result"]).ravel(), rtol=1e-15)
+
+
+@pytest.mark.parametrize("key", sorted(GOLD["arithmetic_operations"]))
+def test_numpy_arith_goldens(ora, key):
+    case = GOLD["arithmetic_operations"][key]
+    op = case["operation"].replace("scalar_", "")
+    code = {"add": O.ADD, "subtract": O.SUB, "multiply": O.MUL, "divide": O.DIV}[op]
+    a = _arr(case["input1"] if "input1" in case else case["input"])
+    b = _arr(case["input2"]) if "input2" in case else np.array(case["scalar"], dtype=np.float64)
+    got = ora.binary(code, a, b)
+    np.testing.assert_allclose(got.ravel(), _arr(case["result"]).ravel(), rtol=1e-15)
+
+
+def test_nan_placement(ora):
+    for f in (np.float64, np.float32):
+        assert np.isnan(ora.flat("min", np.array([1, np.nan, 3, -2, np.nan], f)))
+        assert np.isnan(ora.flat("max", np.array([np.nan, 1, 2], f)))
+        assert np.isnan(ora.flat("max", np.array([1, 2, np.nan], f)))
+        assert ora.flat("min", np.array([np.inf, 1.0], f)) == 1.0
+        assert ora.flat("max", np.array([-np.inf, 1.0], f)) == 1.0
+        d = np.ones(64, f)
+        d[0] = 5
+        for pos in (0, 8, 10, 32, 63):
+            e = d.copy()
+            e[pos] = np.nan
+            assert np.isnan(ora.flat("max", e)) and np.isnan(ora.flat("min", e))
+
+
+def test_empty_conventions(ora):
+    e = np.zeros(0, np.float64)
+    assert ora.flat("sum", e) == 0 and ora.flat("mean", e) == 0 and ora.flat("max", e) == 0
+    assert ora.flat("prod", e) == 1 and ora.flat("var", e, 0) == 0
+
+
+def test_ddof(ora):
+    a = np.array([1, 2, 3, 4, 5], np.float64)
+    assert abs(ora.flat("var", a, 0) - 2.0) < 1e-12
+    assert abs(ora.flat("var", a, 1) - 2.5) < 1e-12
+
+
+def test_axis_fold_is_left_to_right(ora):
+    # f32 lane of values whose sum depends on order: the oracle must fold
+    # left to right from 0 (src/math/aggregation.rs:555-561).
+    x = np.array([[1e8], [1.0], [-1e8], [1.0]], np.float32)
+    s = np.float32(0)
+    for v in x[:, 0]:
+        s = np.float32(s + v)
+    assert ora.axis(O.SUM, x, 0)[0] == s
+
+
+SIZE_GRID = [(1, 1, 1), (2, 2, 2), (31, 31, 31), (32, 32, 32), (33, 33, 33), (63, 63, 63),
+             (64, 64, 64), (65, 65, 65), (127, 127, 127), (128, 128, 128), (0, 5, 4), (5, 0, 4),
+             (5, 4, 0)]
+
+
+@pytest.mark.parametrize("mkn", SIZE_GRID)
+def test_gemm_oracle_vs_double_double(ora, mkn):
+    m, k, n = mkn
+    A = ora.gen_uniform_pm1(1, m * k).reshape(m, k)
+    B = ora.gen_uniform_pm1(2, k * n).reshape(k, n)
+    C = ora.gemm(A, B)
+    Cdd, ab = ora.gemm_dd(A, B)
+    if m * n:
+        err = np.abs(C - Cdd) / np.maximum(ab, np.finfo(float).tiny)
+        assert np.all(np.where(ab > 0, err, 0) <= 1e-14)
+        if k == 0:
+            assert np.all(C == 0)
+
+
+def test_generator_twins(ora):
+    # The numpy twin of SplitMix64 used by the host code matches the oracle.
+    from numrs_gb300 import rng
+    for seed in (1, 2, 3, 12825631960650228096):
+        ref = np.array([ora.splitmix64_at(seed, i) for i in range(16)], dtype=np.uint64)
+        assert np.array_equal(rng.splitmix64(seed, 16), ref)
+    assert np.array_equal(rng.uniform_pm1(7, 1000), ora.gen_uniform_pm1(7, 1000))
+    assert np.array_equal(rng.int_range(4, 1000), ora.gen_i64(4, 1000))
