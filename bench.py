@@ -184,6 +184,108 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _time_ms(fn, reps, stream):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def gemm_section(K, L, quick: bool):
+    """Plain f64 GEMM 512^3 (DMMA) and the 8192^3 split-precision GEMM beside
+    the native FP64 DMMA GEMM, errors measured on the GPU against the FP64
+    result as max |C - C_fp64| / (|A||B|)_ij."""
+    import torch
+    stream = torch.cuda.current_stream()
+    out = {}
+    A = torch.empty((512, 512), dtype=torch.float64, device="cuda")
+    B = torch.empty_like(A)
+    K.fill_random(A, L.RNG_UNIFORM, 1, -1.0, 1.0)
+    K.fill_random(B, L.RNG_UNIFORM, 2, -1.0, 1.0)
+    C = torch.empty_like(A)
+    ms = _time_ms(lambda: K.gemm_2d(512, 512, 512, A, B, C, variant=L.GEMM_DMMA), 20, stream)
+    out["f64_512_dmma"] = {"ms": round(ms, 4), "tflops": round(2 * 512 ** 3 / ms / 1e9, 3)}
+    n = 2048 if quick else 8192
+    A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    B = torch.empty_like(A)
+    Cd = torch.empty_like(A)
+    Co = torch.empty_like(A)
+    Aa = torch.empty_like(A)
+    Ba = torch.empty_like(A)
+    AB = torch.empty_like(A)
+    flops = 2.0 * n ** 3
+    res = {}
+    for phi in (0.0, 1.0, 4.0):
+        K.fill_random(A, L.RNG_OZAKI, 5, phi, 0.0)
+        K.fill_random(B, L.RNG_OZAKI, 6, phi, 0.0)
+        ms_d = _time_ms(lambda: K.gemm_2d(n, n, n, A, B, Cd, variant=L.GEMM_DMMA), 1, stream)
+        torch.abs(A, out=Aa)
+        torch.abs(B, out=Ba)
+        K.gemm_2d(n, n, n, Aa, Ba, AB, variant=L.GEMM_DMMA)
+        entry = {"dmma_ms": round(ms_d, 2), "dmma_tflops": round(flops / ms_d / 1e9, 3), "ozaki": []}
+        for s in ((7, 9, 11) if phi == 0.0 else (9, 12, 14, 16)):
+            ms_o = _time_ms(lambda: K.gemm_ozaki(A, B, slices=s, out=Co), 2, stream)
+            err = float(((Co - Cd).abs() / AB.clamp_min(1e-300)).max())
+            entry["ozaki"].append({"slices": s, "ms": round(ms_o, 2), "tflops": round(flops / ms_o / 1e9, 2),
+                                   "max_err_vs_fp64": err})
+        res[f"phi={phi:g}"] = entry
+    out[f"f64_{n}_split_vs_dmma"] = res
+    del A, B, Cd, Co, Aa, Ba, AB
+    torch.cuda.empty_cache()
+    return out
+
+
+def grouped_section(K, L, seed: int = 7):
+    """4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64) and
+    4096 row reductions (length log-uniform in [64, 65536]) in one persistent
+    launch replayed from a CUDA graph, against launching them one by one."""
+    import numpy as np
+    import torch
+    r = np.random.default_rng(seed)
+    lu = lambda lo, hi, n: np.exp(r.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)  # noqa: E731
+    M, N, Kd = lu(16, 512, 4096), lu(16, 512, 4096), lu(16, 512, 4096)
+    gemms = []
+    flops = 0.0
+    for i in range(4096):
+        dt = torch.float32 if i % 2 == 0 else torch.float64
+        a = torch.empty((int(M[i]), int(Kd[i])), dtype=dt, device="cuda").uniform_(-1, 1)
+        b = torch.empty((int(Kd[i]), int(N[i])), dtype=dt, device="cuda").uniform_(-1, 1)
+        c = torch.empty((int(M[i]), int(N[i])), dtype=dt, device="cuda")
+        gemms.append((a, b, c, False))
+        flops += 2.0 * M[i] * N[i] * Kd[i]
+    lens = lu(64, 65536, 4096)
+    reds = []
+    rbytes = 0
+    for i in range(4096):
+        x = torch.randn(int(lens[i]), device="cuda")
+        reds.append((x, L.SUM, torch.empty(1, device="cuda")))
+        rbytes += int(lens[i]) * 4
+    stream = torch.cuda.current_stream()
+    plan = K.Plan(gemms, reds)
+    st = plan.stats()
+    ms_g = _time_ms(lambda: plan.run(use_graph=True), 5, stream)
+
+    def one_by_one():
+        for a, b, c, _ in gemms:
+            K.gemm_2d(a.shape[0], a.shape[1], b.shape[1], a, b, c)
+        for x, op, o in reds:
+            K.reduce(x, op)
+    ms_1 = _time_ms(one_by_one, 1, stream)
+    plan.close()
+    f64_flops = sum(2.0 * M[i] * N[i] * Kd[i] for i in range(1, 4096, 2))
+    return {"gemms": 4096, "row_reductions": 4096, "work_items": st["work_items"],
+            "grouped_graph_ms": round(ms_g, 3), "one_by_one_ms": round(ms_1, 3),
+            "speedup": round(ms_1 / ms_g, 2), "gflops": round(flops / ms_g / 1e6, 1),
+            "f64_share_of_flops": round(f64_flops / flops, 3), "reduce_bytes": rbytes,
+            "tile_choice": "size heuristic (tuner table empty)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,6 +296,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-gemm", action="store_true")
+    ap.add_argument("--quick-gemm", action="store_true", help="2048^3 instead of 8192^3")
+    ap.add_argument("--no-grouped", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -351,6 +456,13 @@ def main():
         out["cpu_baseline"] = {"value": round(nbytes * len(times) / t / 1e9, 2), "unit": "GB/s",
                                "cores": cores, "kind": "port", "sample": sample,
                                "passes": len(times), "seconds": round(t, 2)}
+    if rank == 0 and not args.no_gemm:
+        del x32, x64, y
+        ops = None
+        torch.cuda.empty_cache()
+        out["gemm"] = gemm_section(K, L, quick=args.quick_gemm)
+    if rank == 0 and not args.no_grouped:
+        out["grouped"] = grouped_section(K, L)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:

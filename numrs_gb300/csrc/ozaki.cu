@@ -514,10 +514,10 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
     info->est_rel_error = std::ldexp(2.0, -(6 + OZ_DIGIT_BITS * (S - 1)));
   }
   if (m == 0 || n == 0) return NRS_OK;
+  if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
   if (!A || !B || !C) return nrs_fail(h, NRS_ERR_INVALID, "null operand");
   int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
   if (st) return st;
-  if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
   if (m > (1LL << 31) || n > (1LL << 31) || kpad > (1LL << 31))
     return nrs_fail(h, NRS_ERR_TOO_LARGE, "dimension beyond 2^31");
 

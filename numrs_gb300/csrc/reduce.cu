@@ -123,8 +123,7 @@ __global__ void __launch_bounds__(256 / sizeof(T))
     const int64_t y0 = it * RB;
     const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
     if (cnt == RB) {
-#pragma unroll
-      for (int r = 0; r < RB; ++r) acc = Fold<T, OP>::step(acc, tile[r * LW + t]);
+      acc = RunFold<T, OP>::template run<RB>(acc, [&](int r) { return tile[r * LW + t]; });
     } else {
       for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, tile[r * LW + t]);
     }
@@ -195,20 +194,19 @@ __global__ void __launch_bounds__(64)
     const int64_t x0 = it * XB;
     const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
     if (cnt == XB) {
+      T v[XB];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const T* c = reinterpret_cast<const T*>(row + ((j ^ sw) << 4));
-        T v[PER16];
         if constexpr (sizeof(T) == 4) {
           float4 q = *reinterpret_cast<const float4*>(c);
-          memcpy(v, &q, 16);
+          memcpy(&v[j * PER16], &q, 16);
         } else {
           double2 q = *reinterpret_cast<const double2*>(c);
-          memcpy(v, &q, 16);
+          memcpy(&v[j * PER16], &q, 16);
         }
-#pragma unroll
-        for (int e = 0; e < PER16; ++e) acc = Fold<T, OP>::step(acc, v[e]);
       }
+      acc = RunFold<T, OP>::template run<XB>(acc, [&](int e) { return v[e]; });
     } else {
       for (int e = 0; e < cnt; ++e) {
         const int j = e / PER16;
@@ -587,8 +585,8 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
                           void* out) {
   if (!h) return NRS_ERR_INVALID;
   h->last_error.clear();
-  if (ndim < 0 || ndim > NRS_UFUNC_MAX_DIMS || (ndim > 0 && (!shape || !strides)) || !out)
-    return nrs_fail(h, NRS_ERR_INVALID, "bad ndim/shape/strides/out");
+  if (ndim < 0 || ndim > NRS_UFUNC_MAX_DIMS || (ndim > 0 && (!shape || !strides)))
+    return nrs_fail(h, NRS_ERR_INVALID, "bad ndim/shape/strides");
   if (op < NRS_SUM || op > NRS_STD) return nrs_fail(h, NRS_ERR_INVALID, "unknown reduce op");
   const size_t es = nrs_dtype_size(dtype);
   if (!es) return nrs_fail(h, NRS_ERR_DTYPE, "unknown dtype");
@@ -604,6 +602,7 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
   if (st) return st;
 
   if (axis == NRS_AXIS_NONE) {
+    if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
     if (is_int && (op == NRS_VAR || op == NRS_STD))
       return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
     // Non-contiguous views are gathered into logical order first, as
@@ -687,6 +686,7 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
     if (n_out == 0 && (op == NRS_SUM || op == NRS_PROD)) return NRS_OK;
     // Empty array: math::sum gives zeros; max/min/mean error out.
     if (op == NRS_SUM || op == NRS_PROD) {
+      if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
       int grid = h->num_sms * 4;
       if (dtype == NRS_F32) fill_value<float><<<grid, 256, 0, h->stream>>>((float*)out, n_out, op == NRS_PROD ? 1.f : 0.f);
       else if (dtype == NRS_F64) fill_value<double><<<grid, 256, 0, h->stream>>>((double*)out, n_out, op == NRS_PROD ? 1.0 : 0.0);
@@ -696,6 +696,7 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
     }
     return nrs_fail(h, NRS_ERR_EMPTY, "Cannot reduce an empty array");
   }
+  if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
   switch (dtype) {
     case NRS_F32: return dispatch_axis_ops<float>(h, p);
     case NRS_F64: return dispatch_axis_ops<double>(h, p);

@@ -117,4 +117,54 @@ __device__ __forceinline__ T block_combine(T v, T* sh) {
   return r;
 }
 
+// Folds a run of N values into a lane accumulator with exactly the result of
+// N sequential Fold<T, OP>::step calls, using four independent chains where
+// the order cannot matter:
+//  * integer folds (wrapping sums/products, max, min) are exact in any order;
+//  * float max/min are order-free as long as the run holds no NaN (the first
+//    NaN of a lane is its result) and no zero (a lane keeps the FIRST of -0.0
+//    and +0.0); such runs are detected off the dependency chain and refolded
+//    sequentially from the incoming accumulator;
+//  * float sums/products stay one sequential chain: their rounding depends on
+//    the order, and the reference's order is left to right.
+template <typename T, int OP>
+struct RunFold {
+  static constexpr bool kFloat = std::is_floating_point<T>::value;
+  static constexpr bool kMinMax = (OP == NRS_MAX || OP == NRS_MIN);
+  static constexpr bool kChains = !kFloat || kMinMax;
+
+  static __device__ __forceinline__ T pick(T a, T v) {
+    if constexpr (OP == NRS_MAX) return v > a ? v : a;
+    else return v < a ? v : a;
+  }
+
+  template <int N, typename Get>
+  static __device__ __forceinline__ T run(T acc, Get get) {
+    if constexpr (!kChains) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc = Fold<T, OP>::step(acc, get(i));
+      return acc;
+    } else if constexpr (!kFloat) {
+      T a[4] = {acc, Fold<T, OP>::init(), Fold<T, OP>::init(), Fold<T, OP>::init()};
+#pragma unroll
+      for (int i = 0; i < N; ++i) a[i & 3] = Fold<T, OP>::step(a[i & 3], get(i));
+      return Fold<T, OP>::step(Fold<T, OP>::step(a[0], a[1]), Fold<T, OP>::step(a[2], a[3]));
+    } else {
+      if (acc != acc) return acc;  // the lane already holds its first NaN
+      T a[4] = {acc, Fold<T, OP>::init(), Fold<T, OP>::init(), Fold<T, OP>::init()};
+      bool special = false;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const T v = get(i);
+        special |= (v != v) | (v == T(0));
+        a[i & 3] = pick(a[i & 3], v);
+      }
+      if (!special) return pick(pick(a[0], a[1]), pick(a[2], a[3]));
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc = Fold<T, OP>::step(acc, get(i));
+      return acc;
+    }
+  }
+};
+
 }  // namespace nrs_red
