@@ -128,6 +128,32 @@ typedef enum nrs_reduce_op {
 int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
                const int64_t* strides, int64_t axis, int64_t ddof, const void* x, void* out);
 
+/* Allocation-free flat reduction. This entry point has no counterpart in the
+ * reference; it exists for callers that must not let a library allocate
+ * device memory: code running under another runtime's memory discipline (a
+ * serving stack or framework allocator that owns and budgets all device
+ * memory) and latency-critical loops that cannot afford the device-wide
+ * synchronisation a cudaMalloc may cause. It computes what
+ * nrs_reduce(..., NRS_AXIS_NONE, ...) computes for a contiguous f32/f64
+ * buffer of n elements (op NRS_SUM, NRS_MEAN, NRS_MAX or NRS_MIN; same
+ * kernels, same chunk order, same result) on `cuda_stream` (NULL = default
+ * stream) of the CURRENT device, with no handle and no allocation: the chunk
+ * partials live in a 128 KiB (+256 B) file-scope device array that every GPU
+ * holds from the moment it loads the library until the process exits.
+ *   - Limit: n <= 67,108,864 (8192 chunks of 8192); larger n returns
+ *     NRS_ERR_TOO_LARGE before anything is launched.
+ *   - The first call on a device looks the array's address up (and the SM
+ *     count) with that device current and caches them; make that first call
+ *     before any stream capture.
+ *   - All calls share the one array and it keeps the last call's contents;
+ *     every call rewrites each partial it reads, so nothing has to start at
+ *     zero. Calls whose work overlaps on the GPU (different streams, no
+ *     ordering between them) race on the array: serialise them.
+ *   - Returns NRS_OK, NRS_ERR_INVALID, NRS_ERR_DTYPE, NRS_ERR_TOO_LARGE or
+ *     NRS_ERR_CUDA (there is no handle, hence no message string). */
+int nrs_reduce_flat_noalloc(void* cuda_stream, int dtype, int op, int64_t n, const void* x,
+                            void* out);
+
 /* ---------------------------------------------------------------------- */
 /* Elementwise ufunc programs                                               */
 /* ---------------------------------------------------------------------- */

@@ -72,6 +72,7 @@ SIGNATURES = {
     "nrs_memcpy_d2h": (_i, [_vp, _vp, _vp, _sz]),
     "nrs_fill_random": (_i, [_vp, _i, _i, _u64, _i64, _d, _d, _vp]),
     "nrs_reduce": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _i64, _vp, _vp]),
+    "nrs_reduce_flat_noalloc": (_i, [_vp, _i, _i, _i64, _vp, _vp]),
     "nrs_ufunc": (_i, [_vp, _i, C.POINTER(UfuncOp), _i, _i, _P64, _i, C.POINTER(_vp), _P64, _vp, _P64]),
     "nrs_exp_affine": (_i, [_vp, _i, _i64, _vp, _d, _d, _vp]),
     "nrs_gemm": (_i, [_vp, _i, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u, _i]),

@@ -30,6 +30,7 @@
 #include <type_traits>
 #include <climits>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "reduce_common.cuh"
@@ -706,4 +707,100 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
       return dispatch_axis_ops<int32_t>(h, p);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free flat reduction
+// ---------------------------------------------------------------------------
+// Some callers cannot let this library call cudaMalloc: code that runs under
+// another runtime's memory discipline (a serving stack or framework allocator
+// that owns all device memory and budgets it), or latency-critical loops where
+// the device-wide synchronisation an allocation can cause is not acceptable.
+// nrs_reduce_flat_noalloc serves them: the same chunk-partial kernels as the
+// flat path of nrs_reduce, with the partials in the file-scope array below
+// instead of the handle's cudaMalloc'd workspace. The array is 128 KiB + 256 B
+// and stays resident on every GPU that loads the library until the process
+// exits. Its host-side name is only a stand-in, so the device address is
+// fetched with cudaGetSymbolAddress once per device and cached.
+namespace {
+constexpr int64_t kNoAllocMaxChunks = 8192;  // partials of up to 8192 chunks
+constexpr int64_t kNoAllocMaxElems = kNoAllocMaxChunks * kChunk;  // 67,108,864
+constexpr int kNoAllocMaxDevices = 64;
+static_assert(sizeof(Partial<double>) <= 16, "a chunk partial must fit 16 bytes");
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_partials[kNoAllocMaxChunks * 16 + 256];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+int g_noalloc_sms[kNoAllocMaxDevices] = {0};
+
+template <typename T>
+int noalloc_flat(cudaStream_t s, int op, int64_t n, const T* x, void* out, void* scratch, int sms) {
+  if (n == 0) {
+    write_scalar<T><<<1, 1, 0, s>>>((T*)out, T(0));
+    return cudaGetLastError() == cudaSuccess ? NRS_OK : NRS_ERR_CUDA;
+  }
+  // Same tiering as flat_reduce: SUM/MEAN use one chunk below 10000 elements.
+  const int64_t chunk = ((op == NRS_SUM || op == NRS_MEAN) && n < kParallelMin) ? n : kChunk;
+  const int64_t nchunks = (n + chunk - 1) / chunk;
+  Partial<T>* part = static_cast<Partial<T>*>(scratch);
+  const int grid = (int)(nchunks < (int64_t)sms * 8 ? nchunks : (int64_t)sms * 8);
+  switch (op) {
+    case NRS_SUM:
+    case NRS_MEAN:
+      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_SUM><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    case NRS_MAX:
+      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_MAX><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+    default:
+      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      flat_finish<T, NRS_MIN><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
+      break;
+  }
+  return cudaGetLastError() == cudaSuccess ? NRS_OK : NRS_ERR_CUDA;
+}
+}  // namespace
+
+extern "C" int nrs_reduce_flat_noalloc(void* cuda_stream, int dtype, int op, int64_t n,
+                                       const void* x, void* out) {
+  if (dtype != NRS_F32 && dtype != NRS_F64) return NRS_ERR_DTYPE;
+  if (op != NRS_SUM && op != NRS_MEAN && op != NRS_MAX && op != NRS_MIN) return NRS_ERR_INVALID;
+  if (n < 0 || !out || (n > 0 && !x)) return NRS_ERR_INVALID;
+  if (n > kNoAllocMaxElems) return NRS_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    return NRS_ERR_CUDA;
+  }
+  void* scratch;
+  int sms;
+  {
+    // First call on a device: look up the array's device address with this
+    // device current, and its SM count. Later calls reuse both.
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return NRS_ERR_CUDA;
+      }
+      int count = 0;
+      if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return NRS_ERR_CUDA;
+      }
+      g_noalloc_sms[dev] = count;
+      g_noalloc_ptr[dev] = p;
+    }
+    scratch = g_noalloc_ptr[dev];
+    sms = g_noalloc_sms[dev];
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  if (dtype == NRS_F32) return noalloc_flat<float>(s, op, n, (const float*)x, out, scratch, sms);
+  return noalloc_flat<double>(s, op, n, (const double*)x, out, scratch, sms);
 }
