@@ -19,10 +19,11 @@
 //    cores with FP32 accumulation. |digit products| <= 2^10, so every partial
 //    sum of a K <= 16384 chunk is an integer below 2^24: the FP32
 //    accumulation is EXACT.
-// 4. Cross-slice accumulation: each exact P is added into a per-element
-//    128-bit integer at weight 2^(6(S-1-(s+t))) -- exact, no FP64 op -- and
-//    the last pair of a tile converts it once to f64 and applies
-//    2^(e_a[i] + e_b[j] - 10 - 6(S-1)).
+// 4. Cross-slice accumulation: the exact products of one diagonal
+//    (s + t = d) are summed in int32 registers, then added once per diagonal
+//    into a per-element 128-bit integer at weight 2^(6(S-1-d)) -- exact, no
+//    FP64 op -- and the most significant diagonal converts the total once to
+//    f64 and applies 2^(e_a[i] + e_b[j] - 10 - 6(S-1)).
 //
 // The tensor-core kernel is persistent (one CTA per SM) and warp-specialised:
 //   warp 0      : TMA producer, 4-stage ring of A (128x64) + B (256x64) bf16
@@ -30,8 +31,9 @@
 //   warp 1      : TMEM allocator and single-thread tcgen05.mma issuer,
 //                 M=128 N=256 K=16, accumulators double-buffered in TMEM
 //                 (2 x 256 columns);
-//   warps 2..5  : epilogue, tcgen05.ld of the finished accumulator (one TMEM
-//                 lane = one tile row per thread) into the int128 sums.
+//   warps 2..9  : epilogue, tcgen05.ld of the finished accumulator (one TMEM
+//                 lane = one tile row per thread, two warps per lane quarter
+//                 splitting the 256 columns) into int32 diagonal sums.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
 // word, drains its own copies and MMAs (bounded), frees TMEM and returns.
 #include <cmath>
@@ -48,7 +50,7 @@ constexpr int OZ_STAGES = 4;
 constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;  // 16 KB
 constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 32 KB
 constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
-constexpr int OZ_THREADS = 192;                 // 6 warps
+constexpr int OZ_THREADS = 320;                 // 10 warps: TMA, MMA, 8 epilogue
 constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
 constexpr int OZ_KCHUNK = 16384;                // exact fp32 accumulation bound
 constexpr int OZ_MAX_SLICES = 16;
@@ -105,6 +107,29 @@ NRS_DEV void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+// 32 lanes x 16 consecutive 32-bit columns.
+NRS_DEV void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+NRS_DEV void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+      "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+      : "memory");
+}
+NRS_DEV void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Shared-memory matrix descriptor, K-major operand with 128-byte swizzle:
 // rows of 128 B, 8-row core-matrix groups 1024 B apart (SBO), descriptor
@@ -192,7 +217,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
+      mbar_init(&acce[b], 8);
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -260,11 +285,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const int kb0 = pr.chunk * (OZ_KCHUNK / OZ_BK);
           int kb1 = kb0 + OZ_KCHUNK / OZ_BK;
           if (kb1 > kblocks_full) kb1 = kblocks_full;
-          const int buf = ai & 1;
-          const uint32_t aph = (ai >> 1) & 1;
+          // One accumulator (TMEM columns 0..255); the epilogue frees it as
+          // soon as it has folded it into the diagonal sums (columns 256..511).
+          const int buf = 0;
+          const uint32_t aph = ai & 1;
           if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t d_tmem = tmem_base + buf * OZ_BN;
+          const uint32_t d_tmem = tmem_base;
           for (int kb = kb0; kb < kb1; ++kb, ++it) {
             const int s = it % OZ_STAGES;
             const uint32_t ph = (it / OZ_STAGES) & 1;
@@ -288,42 +315,80 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       mbar_wait_bounded(drain, 0, 1u << 20);
     }
   } else {
-    // ---------------- epilogue (warps 2..5) ----------------
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    // ---------------- epilogue (warps 2..9) ----------------
+    // Warp w reads TMEM lane quarter w % 4 (one tile row per thread) and
+    // column half (w - 2) / 4. The exact pair products of one diagonal
+    // (s + t = d, every K chunk) are summed as int32 in TMEM columns
+    // 256..511 (|sum| < 2^31 by the K limit checked on the host): per unit,
+    // load the accumulator, add it into the diagonal sums, store them back,
+    // and hand the accumulator to the MMA warp. Global memory is touched once
+    // per diagonal: the int128 accumulator gets D_d << 6(S-1-d), and the most
+    // significant diagonal converts the total to f64 into C.
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + half * (OZ_BN / 2);
+    const uint32_t acc_t = lane_base;           // accumulator columns
+    const uint32_t dsum_t = lane_base + OZ_BN;  // diagonal-sum columns
     uint32_t ai = 0;
     bool ok = true;
+    int prev_d = -1;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
       int tm, tn;
       tile_coords(tile, P, tm, tn);
       const int64_t row = (int64_t)tm * OZ_BM + row_in_tile;
       const bool row_ok = row < P.m;
+      const int64_t col0 = (int64_t)tn * OZ_BN + half * (OZ_BN / 2);
+      prev_d = -1;
       for (int u = 0; u < P.n_pairs; ++u, ++ai) {
         const PairOf pr = pair_of(u, P.slices, P.kchunks);
-        const int buf = ai & 1;
-        const uint32_t aph = (ai >> 1) & 1;
-        if (!bounded(&accf[buf], aph, 4)) { ok = false; break; }
+        const int d = pr.s + pr.t;
+        const bool diag_start = (d != prev_d);
+        prev_d = d;
+        const uint32_t aph = ai & 1;
+        if (!bounded(&accf[0], aph, 4)) { ok = false; break; }
         tc_fence_after();
-        const bool first = (u == 0), last = (u == P.n_pairs - 1);
-        const int shift = OZ_DIGIT_BITS * (P.slices - 1 - (pr.s + pr.t));
-        const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + buf * OZ_BN;
+#pragma unroll 2
         for (int c = 0; c < OZ_BN / 32; ++c) {
-          uint32_t v[32];
-          tmem_ld32(taddr + c * 32, v);
-          if (!row_ok) continue;
-          const int64_t col0 = (int64_t)tn * OZ_BN + c * 32;
-          __int128* accp = P.acc + row * P.n + col0;
-          int ecol_base = 0;
-          if (last) ecol_base = P.ea[row] + P.final_shift;
+          uint32_t v[16], w[16];
+          tmem_ld16(acc_t + c * 16, v);
+          if (!diag_start) {
+            tmem_ld16(dsum_t + c * 16, w);
 #pragma unroll
-          for (int e = 0; e < 32; ++e) {
-            const int64_t col = col0 + e;
+            for (int e = 0; e < 16; ++e)
+              w[e] = (uint32_t)((int32_t)w[e] + __float2int_rn(__uint_as_float(v[e])));
+          } else {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) w[e] = (uint32_t)__float2int_rn(__uint_as_float(v[e]));
+          }
+          tmem_st16(dsum_t + c * 16, w);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[0]);
+        // Is this the last unit of its diagonal?
+        const bool diag_end = (u == P.n_pairs - 1) || (pair_of(u + 1, P.slices, P.kchunks).s +
+                                                      pair_of(u + 1, P.slices, P.kchunks).t) != d;
+        if (!diag_end) continue;
+        const bool first = (d == P.slices - 1), last = (d == 0);
+        const int shift = OZ_DIGIT_BITS * (P.slices - 1 - d);
+        const int ecol_base = (last && row_ok) ? P.ea[row] + P.final_shift : 0;
+        __int128* accp = P.acc + (row_ok ? row : 0) * P.n + col0;
+#pragma unroll 1
+        for (int c = 0; c < OZ_BN / 32; ++c) {
+          uint32_t w[16];
+          tmem_ld16(dsum_t + c * 16, w);
+          if (!row_ok) continue;
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int j = c * 16 + e;
+            const int64_t col = col0 + j;
             if (col >= P.n) continue;
-            const float f = __uint_as_float(v[e]);
-            const __int128 contrib = ((__int128)__float2int_rn(f)) << shift;
-            const __int128 sum = first ? contrib : (accp[e] + contrib);
+            const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
+            const __int128 sum = first ? contrib : (accp[j] + contrib);
             if (!last) {
-              accp[e] = sum;
+              accp[j] = sum;
             } else {
               // |sum| < 2^127: keep its top 64 significant bits, convert once.
               const bool neg = sum < 0;
@@ -338,9 +403,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&acce[buf]);
       }
     }
   }
@@ -505,6 +567,10 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   const int64_t kpad = ((k + 7) / 8) * 8;
   const int kchunks = (int)((kpad + OZ_KCHUNK - 1) / OZ_KCHUNK);
   const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
+  // A diagonal's int32 register sum holds at most kchunks * S products of
+  // magnitude <= 2^24 each: keep it below 2^31.
+  if ((int64_t)kchunks * S >= 128)
+    return nrs_fail(h, NRS_ERR_TOO_LARGE, "k too large for this slice count (k * S < 128 * 16384)");
   if (info) {
     info->slices = S;
     info->products = n_pairs;

@@ -81,13 +81,18 @@ struct PipeSmem {
 
 // Lanes adjacent (stride 1), axis strided. Tensor map dims (lanes, axis,
 // batch), box (LW, RB, 1), no swizzle: tile row r holds lanes [l0, l0+LW) of
-// axis position y0 + r.
+// axis position y0 + r. 64 lanes per CTA for every dtype, so a 16384-lane
+// problem is 256 CTAs: one wave at the three 66 KB CTAs an SM holds.
+constexpr int kColLanes = 64;
+template <typename T>
+constexpr int col_rows() { return 8192 / (kColLanes * (int)sizeof(T)); }
+
 template <typename T, int OP, int STAGES>
-__global__ void __launch_bounds__(256 / sizeof(T))
+__global__ void __launch_bounds__(kColLanes)
     fold_cols_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
                   typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err) {
-  constexpr int LW = 256 / sizeof(T);  // lanes per tile (= threads)
-  constexpr int RB = 32;               // axis positions per tile
+  constexpr int LW = kColLanes;        // lanes per tile (= threads)
+  constexpr int RB = col_rows<T>();    // axis positions per tile (8 KB tiles)
   constexpr int TILE = LW * RB * sizeof(T);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -429,13 +434,13 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
     const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
     uint64_t sb = (uint64_t)(batch > 1 ? bstride : p.astride * p.alen) * es;
     const uint64_t strides[2] = {(uint64_t)p.astride * es, sb};
-    const uint32_t box[3] = {(uint32_t)(256 / es), 32, 1};
+    const uint32_t box[3] = {(uint32_t)kColLanes, (uint32_t)col_rows<T>(), 1};
     if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
       return NRS_ERR_UNSUPPORTED;
     auto kern = fold_cols_tma<T, OP, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((lanes + 256 / es - 1) / (256 / es)), (unsigned)batch);
-    kern<<<grid, 256 / es, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
+    dim3 grid((unsigned)((lanes + kColLanes - 1) / kColLanes), (unsigned)batch);
+    kern<<<grid, kColLanes, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
     return nrs_after_launch(h, "fold_cols_tma");
   }
   if (p.astride == 1 && lstride > 1) {

@@ -1,0 +1,87 @@
+"""Small, self-contained launch cases for profiling one kernel at a time.
+
+    python -m numrs_gb300.profile_cases --case fold_cols_f32_max [--n 8192] [--launches 3]
+
+Each case allocates inputs larger than the 129 MB L2 but only a few GB in
+total, runs one warm-up launch and then `--launches` launches of the kernel
+under study, so a profiler can capture them with -k/-c.
+"""
+from __future__ import annotations
+
+import argparse
+
+import torch
+
+from . import _lib as L
+from . import kernels as K
+
+CASES = {
+    "fold_cols_f32_sum": ("f32", L.SUM, 0),
+    "fold_cols_f32_max": ("f32", L.MAX, 0),
+    "fold_rows_f32_sum": ("f32", L.SUM, 1),
+    "fold_rows_f32_max": ("f32", L.MAX, 1),
+    "fold_cols_i64_sum": ("i64", L.SUM, 0),
+    "fold_cols_i64_max": ("i64", L.MAX, 0),
+    "fold_rows_i64_sum": ("i64", L.SUM, 1),
+    "exp_affine_f32": ("f32", None, None),
+    "ozaki_f64": ("f64", None, None),
+    "dmma_f64": ("f64", None, None),
+    "grouped": (None, None, None),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", required=True, choices=sorted(CASES))
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--slices", type=int, default=9)
+    a = ap.parse_args()
+    dt, op, axis = CASES[a.case]
+    n = a.n
+    if a.case.startswith("fold"):
+        if dt == "f32":
+            x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+            K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        else:
+            x = torch.empty((n, n), dtype=torch.int64, device="cuda")
+            K.fill_random(x, L.RNG_INT, 4, -(1 << 20), float(1 << 21))
+        fn = lambda: K.reduce(x, op, axis)  # noqa: E731
+    elif a.case == "exp_affine_f32":
+        x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        y = torch.empty_like(x)
+        fn = lambda: K.exp_affine(x, 0.5, -0.25, out=y)  # noqa: E731
+    elif a.case in ("ozaki_f64", "dmma_f64"):
+        A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        B = torch.empty_like(A)
+        C = torch.empty_like(A)
+        K.fill_random(A, L.RNG_UNIFORM, 5, -0.5, 0.5)
+        K.fill_random(B, L.RNG_UNIFORM, 6, -0.5, 0.5)
+        if a.case == "ozaki_f64":
+            fn = lambda: K.gemm_ozaki(A, B, slices=a.slices, out=C)  # noqa: E731
+        else:
+            fn = lambda: K.gemm_2d(n, n, n, A, B, C, variant=L.GEMM_DMMA)  # noqa: E731
+    else:
+        import numpy as np
+        r = np.random.default_rng(7)
+        lu = lambda lo, hi, k: np.exp(r.uniform(np.log(lo), np.log(hi), k)).astype(np.int64)  # noqa: E731
+        M, N, Kd = lu(16, 512, 512), lu(16, 512, 512), lu(16, 512, 512)
+        gemms = []
+        for i in range(512):
+            t = torch.float32 if i % 2 == 0 else torch.float64
+            gemms.append((torch.randn(int(M[i]), int(Kd[i]), dtype=t, device="cuda"),
+                          torch.randn(int(Kd[i]), int(N[i]), dtype=t, device="cuda"),
+                          torch.empty(int(M[i]), int(N[i]), dtype=t, device="cuda"), False))
+        plan = K.Plan(gemms)
+        fn = lambda: plan.run(use_graph=False)  # noqa: E731
+    fn()
+    torch.cuda.synchronize()
+    for _ in range(a.launches):
+        fn()
+    torch.cuda.synchronize()
+    print("ok", a.case)
+
+
+if __name__ == "__main__":
+    main()

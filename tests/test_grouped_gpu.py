@@ -182,3 +182,16 @@ def test_selector_training_reduces_loss(K):
     y = sel.predict(xd)
     assert float(((y - td) ** 2).mean()) < 0.2 * float(((td - td.mean(0)) ** 2).mean())
     sel.close()
+
+
+def test_learned_selector_vs_heuristic_on_held_out_shapes(K):
+    """Trains the selector on autotuner timings and compares, on held-out
+    shapes, its picks and the size heuristic's against exhaustive tuning."""
+    from numrs_gb300 import tune_selector as TS
+    res, sel, rows, _ = TS.run(360, 120, seed=11, reps=1, epochs=200, hi=1024,
+                               f64_max_flops=2e10, f32_max_flops=2e11)
+    print("selector", res["selector"], "heuristic", res["heuristic"])
+    assert res["selector"]["throughput_vs_exhaustive"] >= 0.85
+    assert res["selector"]["mean_regret"] <= res["heuristic"]["mean_regret"] + 0.02
+    assert res["tuning_time_saved_x"] > 10
+    sel.close()
