@@ -37,6 +37,27 @@ F32_SEED, I64_SEED = 3, 4
 A_SCALE, B_SHIFT = 0.5, -0.25
 
 
+CONFIG = {"workload": "16384x16384 f32 N(0,1) + i64 U[-2^20,2^20): axis-0/1 sum/mean/max (f32), "
+                      "sum/max (i64), row-major and transposed-stride views, + fused exp(0.5x-0.25); "
+                      "one step = 21 launches",
+          "l2": "no flush: inputs (1 GiB, 2 GiB) > 129 MB L2"}
+
+
+def max_over_ranks(value: float, dist, device) -> float:
+    """The slowest rank's time (replicas: the job ends with the last one)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(step_bytes: int, world: int, ms_per_step: float) -> float:
+    """Whole-job throughput: every rank processes its own replica of the step."""
+    return step_bytes * world / (ms_per_step / 1e3) / 1e9
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -174,9 +195,8 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": {"workload": f"axis-0/1 sum/mean/max f32 + sum/max i64 (row-major and transposed) "
-                                   f"+ fused exp(0.5x-0.25), {rows}x16384 slab per step",
-                       "l2": "inputs larger than L2"},
+            "config": dict(CONFIG, sample=f"each step: the same 21 operations on a {rows}x16384 "
+                                          "row slab of both arrays (CPU)"),
             "cpu_baseline": {"value": round(val, 2), "unit": "GB/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(val, 2), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -267,9 +287,29 @@ def grouped_section(K, L, seed: int = 7):
         reds.append((x, L.SUM, torch.empty(1, device="cuda")))
         rbytes += int(lens[i]) * 4
     stream = torch.cuda.current_stream()
+    # Tile choice without tuning (the size heuristic) for comparison.
+    K.tuner_clear()
+    plan_h = K.Plan(gemms, reds)
+    ms_h = _time_ms(lambda: plan_h.run(use_graph=True), 5, stream)
+    plan_h.close()
+    # Exhaustive autotuning per shape bucket (log2-rounded m, k, n and dtype),
+    # each bucket timed as a grouped launch of as many copies as it has
+    # problems in this batch (capped at 64).
+    buckets = {}
+    for a, b, c, _ in gemms:
+        key = (L.F32 if a.dtype == torch.float32 else L.F64,
+               *(int(round(np.log2(v))) for v in (a.shape[0], a.shape[1], b.shape[1])))
+        buckets.setdefault(key, []).append((a.shape[0], a.shape[1], b.shape[1]))
+    t_tune = time.perf_counter()
+    for (dt, *_), shapes in buckets.items():
+        m, k, n = shapes[len(shapes) // 2]
+        _, best = K.tune_gemm(dt, m, k, n, batch=min(len(shapes), 64), reps=2)
+        K.tuner_set(dt, m, k, n, best)
+    tune_s = time.perf_counter() - t_tune
     plan = K.Plan(gemms, reds)
     st = plan.stats()
     ms_g = _time_ms(lambda: plan.run(use_graph=True), 5, stream)
+    K.tuner_clear()
 
     def one_by_one():
         for a, b, c, _ in gemms:
@@ -283,7 +323,8 @@ def grouped_section(K, L, seed: int = 7):
             "grouped_graph_ms": round(ms_g, 3), "one_by_one_ms": round(ms_1, 3),
             "speedup": round(ms_1 / ms_g, 2), "gflops": round(flops / ms_g / 1e6, 1),
             "f64_share_of_flops": round(f64_flops / flops, 3), "reduce_bytes": rbytes,
-            "tile_choice": "size heuristic (tuner table empty)"}
+            "tile_choice": f"autotuner: {len(buckets)} shape buckets tuned in {tune_s:.2f} s",
+            "heuristic_tiles_graph_ms": round(ms_h, 3)}
 
 
 def main():
@@ -357,13 +398,9 @@ def main():
         for i, (cls, _, _) in enumerate(ops):
             per_class.setdefault(cls, []).append(ev[s_i][i][0].elapsed_time(ev[s_i][i][1]))
     clk = clocks.stop()
-    ms_total = t_start.elapsed_time(t_end)
-    if dist is not None:
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(t_start.elapsed_time(t_end), dist, "cuda")
     ms_per_step = ms_total / args.steps
-    value = step_bytes * world / (ms_per_step / 1e3) / 1e9
+    value = whole_job_gbs(step_bytes, world, ms_per_step)
 
     peak, peak_kind = _peaks()
     # per kernel class: algorithmic bytes per launch / mean launch time
@@ -388,11 +425,7 @@ def main():
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
            "data": "synthetic (SplitMix64, seeds 3/4)",
-           "config": {"workload": "16384x16384 f32 N(0,1) + i64 U[-2^20,2^20): axis-0/1 sum/mean/max (f32), "
-                                  "sum/max (i64), row-major and transposed-stride views, + fused "
-                                  "exp(0.5x-0.25); one step = 21 launches",
-                      "bytes_per_step": step_bytes, "l2": "no flush: inputs (1 GiB, 2 GiB) > 129 MB L2",
-                      "parallelism": f"replicas x{world}"},
+           "config": dict(CONFIG, bytes_per_step=step_bytes, parallelism=f"replicas x{world}"),
            "gpu_launches": launches,
            "roofline": {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_gbs"],
                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -410,22 +443,47 @@ def main():
         L.check(lib.nrs_memcpy_d2h(h, hp32, C.c_void_p(x32.data_ptr()), nb32), h)
         L.check(lib.nrs_memcpy_d2h(h, hp64, C.c_void_p(x64.data_ptr()), nb64), h)
         L.check(lib.nrs_synchronize(h), h)
-        outs = []
-        red_outs = []
+        # Two extra handles on their own non-blocking streams carry the bulk
+        # copies (H2D and D2H use separate copy engines); CUDA events order
+        # them against the compute on the current stream, so the i64 upload
+        # and the ufunc download overlap the f32 reductions.
+        h_in, h_out = C.c_void_p(), C.c_void_p()
+        L.check(lib.nrs_create(local, C.byref(h_in)))
+        L.check(lib.nrs_create(local, C.byref(h_out)))
+        s_in = torch.cuda.ExternalStream(lib.nrs_get_stream(h_in))
+        s_out = torch.cuda.ExternalStream(lib.nrs_get_stream(h_out))
+        ev32, ev64, evy = (torch.cuda.Event() for _ in range(3))
+        cur = torch.cuda.current_stream()
+        f32_ops = [fn for cls, _, fn in ops if cls.endswith("/f32") and not cls.startswith("exp")]
+        i64_ops = [fn for cls, _, fn in ops if cls.endswith("/i64")]
+        res_host = {}
+
+        def d2h_small(r, key):
+            nbytes = r.numel() * r.element_size()
+            if key not in res_host:
+                res_host[key] = torch.empty(r.shape, dtype=r.dtype, pin_memory=True)
+            L.check(lib.nrs_memcpy_d2h(h, C.c_void_p(res_host[key].data_ptr()), C.c_void_p(r.data_ptr()),
+                                       nbytes), h)
+            return nbytes
 
         def e2e_step():
-            L.check(lib.nrs_memcpy_h2d(h, C.c_void_p(x32.data_ptr()), hp32, nb32), h)
-            L.check(lib.nrs_memcpy_h2d(h, C.c_void_p(x64.data_ptr()), hp64, nb64), h)
-            res = [fn() for _, _, fn in ops]
-            d2h = 0
-            for r in res[:-1]:
-                host = torch.empty(r.shape, dtype=r.dtype, pin_memory=True)
-                L.check(lib.nrs_memcpy_d2h(h, C.c_void_p(host.data_ptr()), C.c_void_p(r.data_ptr()),
-                                           r.numel() * r.element_size()), h)
-                d2h += r.numel() * r.element_size()
-            L.check(lib.nrs_memcpy_d2h(h, hy, C.c_void_p(y.data_ptr()), nb32), h)
-            d2h += nb32
-            L.check(lib.nrs_synchronize(h), h)
+            L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x32.data_ptr()), hp32, nb32), h_in)
+            ev32.record(s_in)
+            L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x64.data_ptr()), hp64, nb64), h_in)
+            ev64.record(s_in)
+            cur.wait_event(ev32)
+            K.exp_affine(x32, A_SCALE, B_SHIFT, out=y)
+            evy.record(cur)
+            s_out.wait_event(evy)
+            L.check(lib.nrs_memcpy_d2h(h_out, hy, C.c_void_p(y.data_ptr()), nb32), h_out)
+            d2h = nb32
+            for i, fn in enumerate(f32_ops):
+                d2h += d2h_small(fn(), ("f32", i))
+            cur.wait_event(ev64)
+            for i, fn in enumerate(i64_ops):
+                d2h += d2h_small(fn(), ("i64", i))
+            for hh in (h_in, h_out, h):
+                L.check(lib.nrs_synchronize(hh), hh)
             return d2h
 
         e2e_step()
@@ -435,16 +493,14 @@ def main():
         for _ in range(e_steps):
             d2h = e2e_step()
         barrier()
-        dt = (time.perf_counter() - t0) / e_steps
-        if dist is not None:
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-        out["e2e"] = {"value": round(step_bytes * world / dt / 1e9, 1), "unit": "GB/s",
+        dt = max_over_ranks((time.perf_counter() - t0) / e_steps, dist, "cuda")
+        out["e2e"] = {"value": round(whole_job_gbs(step_bytes, world, dt * 1e3), 1), "unit": "GB/s",
                       "h2d_bytes_per_step": nb32 + nb64, "d2h_bytes_per_step": d2h,
                       "ms_per_step": round(dt * 1e3, 3)}
         for p in (hp32, hp64, hy):
             lib.nrs_host_free(h, p)
+        lib.nrs_destroy(h_in)
+        lib.nrs_destroy(h_out)
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
