@@ -99,7 +99,8 @@ int nrs_fill_random(nrs_handle* h, int dtype, int dist, uint64_t seed, int64_t n
 /* Reductions                                                               */
 /* ---------------------------------------------------------------------- */
 typedef enum nrs_reduce_op {
-  NRS_SUM = 0, NRS_MEAN = 1, NRS_MAX = 2, NRS_MIN = 3, NRS_PROD = 4, NRS_VAR = 5, NRS_STD = 6
+  NRS_SUM = 0, NRS_MEAN = 1, NRS_MAX = 2, NRS_MIN = 3, NRS_PROD = 4, NRS_VAR = 5, NRS_STD = 6,
+  NRS_ARGMAX = 7, NRS_ARGMIN = 8 /* output: int64 indices */
 } nrs_reduce_op;
 #define NRS_AXIS_NONE INT64_MIN
 
@@ -123,8 +124,16 @@ typedef enum nrs_reduce_op {
  *   lane sums match the reference's fold order exactly.
  *   MAX/MIN/MEAN over an empty axis return NRS_ERR_EMPTY (the reference's
  *   "Cannot find max of empty array"); SUM gives zeros.
- * dtypes: F32, F64, I64 (I32 for SUM/MAX/MIN/PROD). For I64, MEAN writes f64
- *   (no reference counterpart: math::mean requires T: Float). */
+ *   VAR/STD along an axis follow math::statistics::var/std(axis, ddof)
+ *   (src/math/statistics/mod.rs:1334-1500, :1308): per-lane mean, then the
+ *   left-to-right sum of (x - mean)^2, / (axis length - ddof), sqrt for STD;
+ *   axis length <= ddof returns NRS_ERR_EMPTY ("Degrees of freedom ...").
+ *   ARGMAX/ARGMIN follow math::statistics::argmax/argmin
+ *   (src/math/statistics/mod.rs:79, :218): first index of the strictly
+ *   greatest (smallest) value, NaN never chosen unless it is element 0 of
+ *   its lane; `out` is int64.
+ * dtypes: F32, F64, I64 (I32 for SUM/MAX/MIN/PROD/ARG*). For I64, MEAN writes
+ *   f64 (no reference counterpart: math::mean requires T: Float). */
 int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
                const int64_t* strides, int64_t axis, int64_t ddof, const void* x, void* out);
 

@@ -17,7 +17,7 @@ F32, F64, I32, I64 = 0, 1, 2, 3
 OK = 0
 ERR_INVALID, ERR_SHAPE, ERR_DTYPE, ERR_AXIS, ERR_EMPTY, ERR_STRIDE = -1, -2, -3, -4, -5, -6
 ERR_CUDA, ERR_TIMEOUT, ERR_ALLOC, ERR_UNSUPPORTED, ERR_TOO_LARGE = -7, -8, -9, -10, -11
-SUM, MEAN, MAX, MIN, PROD, VAR, STD = 0, 1, 2, 3, 4, 5, 6
+SUM, MEAN, MAX, MIN, PROD, VAR, STD, ARGMAX, ARGMIN = 0, 1, 2, 3, 4, 5, 6, 7, 8
 AXIS_NONE = -(2 ** 63)
 OP_INPUT, OP_SCALAR, OP_ADD, OP_SUB, OP_MUL, OP_DIV = 0, 1, 2, 3, 4, 5
 OP_NEG, OP_ABS, OP_SQRT, OP_EXP, OP_LN, OP_MAX, OP_MIN = 6, 7, 8, 9, 10, 11, 12

@@ -54,7 +54,8 @@ struct KeptDims {
 
 template <typename T, int OP>
 __global__ void fold_generic(const T* __restrict__ x, KeptDims kd, int64_t n_out, int64_t alen,
-                             int64_t astride, typename OutOf<T, OP>::type* __restrict__ out) {
+                             int64_t astride, typename OutOf<T, OP>::type* __restrict__ out,
+                             const T* __restrict__ lane_mean, T div) {
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
        o += (int64_t)gridDim.x * blockDim.x) {
     int64_t rem = o, base = 0;
@@ -64,10 +65,115 @@ __global__ void fold_generic(const T* __restrict__ x, KeptDims kd, int64_t n_out
       base += c * kd.stride[d];
     }
     const T* p = x + base;
+    const T m = lane_mean ? lane_mean[o] : T(0);
     T acc = Fold<T, OP>::init();
-    for (int64_t j = 0; j < alen; ++j) acc = Fold<T, OP>::step(acc, p[j * astride]);
-    out[o] = finish<T, OP>(acc, alen);
+    for (int64_t j = 0; j < alen; ++j) acc = Fold<T, OP>::step(acc, lane_xform<T, OP>(p[j * astride], m));
+    out[o] = finish<T, OP>(acc, alen, div);
   }
+}
+
+// argmax / argmin along an axis (math::statistics::argmax/argmin,
+// src/math/statistics/mod.rs:79, :218): the first element starts the lane,
+// a later one replaces it only if strictly greater (smaller), so ties keep
+// the first index and a NaN is never chosen unless it is element 0.
+template <typename T, bool MAX>
+__global__ void arg_generic(const T* __restrict__ x, KeptDims kd, int64_t n_out, int64_t alen,
+                            int64_t astride, int64_t* __restrict__ out) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
+       o += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = o, base = 0;
+    for (int d = kd.n - 1; d >= 0; --d) {
+      int64_t c = rem % kd.size[d];
+      rem /= kd.size[d];
+      base += c * kd.stride[d];
+    }
+    const T* p = x + base;
+    T best = p[0];
+    int64_t bi = 0;
+    for (int64_t j = 1; j < alen; ++j) {
+      const T v = p[j * astride];
+      if (MAX ? (v > best) : (v < best)) {
+        best = v;
+        bi = j;
+      }
+    }
+    out[o] = bi;
+  }
+}
+
+// Flat argmax / argmin (axis = None): the reference scans left to right from
+// element 0 keeping the first strictly greater (smaller) value. The same
+// answer in parallel: a candidate (v, i) beats (w, j) if v is strictly
+// better, or equal with i < j; NaNs never win; and if element 0 is NaN the
+// answer is 0 (nothing compares greater than it). Chunk candidates go to
+// workspace and one thread combines them.
+template <typename T>
+struct ArgCand {
+  T v;  // unused when idx < 0
+  int64_t idx;
+};
+
+template <typename T, bool MAX>
+__device__ __forceinline__ bool arg_better(T v, int64_t i, T w, int64_t j) {
+  if (v != v) return false;
+  if (j < 0 || w != w) return true;
+  if (MAX ? (v > w) : (v < w)) return true;
+  return v == w && i < j;
+}
+
+template <typename T, bool MAX>
+__global__ void __launch_bounds__(256)
+    arg_partials(const T* __restrict__ x, int64_t n, ArgCand<T>* __restrict__ part) {
+  __shared__ T sv[256];
+  __shared__ int64_t si[256];
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const int64_t lo = c * kChunk, hi = (lo + kChunk < n) ? lo + kChunk : n;
+    T bv = T(0);
+    int64_t bi = -1;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += 256) {
+      const T v = x[i];
+      if (arg_better<T, MAX>(v, i, bv, bi)) {
+        bv = v;
+        bi = i;
+      }
+    }
+    sv[threadIdx.x] = bv;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+      if (threadIdx.x < s && si[threadIdx.x + s] >= 0 &&
+          arg_better<T, MAX>(sv[threadIdx.x + s], si[threadIdx.x + s], sv[threadIdx.x], si[threadIdx.x])) {
+        sv[threadIdx.x] = sv[threadIdx.x + s];
+        si[threadIdx.x] = si[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[c] = ArgCand<T>{sv[0], si[0]};
+    __syncthreads();
+  }
+}
+
+template <typename T, bool MAX>
+__global__ void arg_finish(const T* __restrict__ x, const ArgCand<T>* __restrict__ part,
+                           int64_t nchunks, int64_t* out) {
+  if (threadIdx.x != 0) return;
+  const T x0 = x[0];
+  if (x0 != x0) {  // a NaN first element is never replaced
+    out[0] = 0;
+    return;
+  }
+  T bv = T(0);
+  int64_t bi = -1;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    if (part[c].idx < 0) continue;
+    const T v = part[c].v;
+    if (arg_better<T, MAX>(v, part[c].idx, bv, bi)) {
+      bv = v;
+      bi = part[c].idx;
+    }
+  }
+  out[0] = bi < 0 ? 0 : bi;  // all NaN (after element 0 checked): index 0
 }
 
 // ---------------------------------------------------------------------------
@@ -90,7 +196,8 @@ constexpr int col_rows() { return 8192 / (kColLanes * (int)sizeof(T)); }
 template <typename T, int OP, int STAGES>
 __global__ void __launch_bounds__(kColLanes)
     fold_cols_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
-                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err) {
+                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err,
+                  const T* __restrict__ lane_mean, T div) {
   constexpr int LW = kColLanes;        // lanes per tile (= threads)
   constexpr int RB = col_rows<T>();    // axis positions per tile (8 KB tiles)
   constexpr int TILE = LW * RB * sizeof(T);
@@ -117,6 +224,7 @@ __global__ void __launch_bounds__(kColLanes)
       tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
     }
   }
+  const T m = (lane_mean && l0 + t < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + t] : T(0);
   T acc = Fold<T, OP>::init();
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
@@ -129,9 +237,10 @@ __global__ void __launch_bounds__(kColLanes)
     const int64_t y0 = it * RB;
     const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
     if (cnt == RB) {
-      acc = RunFold<T, OP>::template run<RB>(acc, [&](int r) { return tile[r * LW + t]; });
+      acc = RunFold<T, OP>::template run<RB>(
+          acc, [&](int r) { return lane_xform<T, OP>(tile[r * LW + t], m); });
     } else {
-      for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, tile[r * LW + t]);
+      for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, lane_xform<T, OP>(tile[r * LW + t], m));
     }
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + STAGES < n_tiles) {
@@ -150,7 +259,7 @@ __global__ void __launch_bounds__(kColLanes)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen);
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
 // Lanes contiguous along the axis. Tensor map dims (axis, lanes, batch), box
@@ -159,7 +268,8 @@ __global__ void __launch_bounds__(kColLanes)
 template <typename T, int OP, int STAGES>
 __global__ void __launch_bounds__(64)
     fold_rows_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
-                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err) {
+                  typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err,
+                  const T* __restrict__ lane_mean, T div) {
   constexpr int LN = 64;                  // lanes per tile (= threads)
   constexpr int XB = 128 / sizeof(T);     // axis elements per tile row
   constexpr int PER16 = 16 / sizeof(T);   // elements per 16-byte chunk
@@ -187,6 +297,7 @@ __global__ void __launch_bounds__(64)
       tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
     }
   }
+  const T m = (lane_mean && l0 + t < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + t] : T(0);
   T acc = Fold<T, OP>::init();
   const int sw = t & 7;
   int64_t it = 0;
@@ -212,12 +323,12 @@ __global__ void __launch_bounds__(64)
           memcpy(&v[j * PER16], &q, 16);
         }
       }
-      acc = RunFold<T, OP>::template run<XB>(acc, [&](int e) { return v[e]; });
+      acc = RunFold<T, OP>::template run<XB>(acc, [&](int e) { return lane_xform<T, OP>(v[e], m); });
     } else {
       for (int e = 0; e < cnt; ++e) {
         const int j = e / PER16;
         const T* c = reinterpret_cast<const T*>(row + ((j ^ sw) << 4));
-        acc = Fold<T, OP>::step(acc, c[e % PER16]);
+        acc = Fold<T, OP>::step(acc, lane_xform<T, OP>(c[e % PER16], m));
       }
     }
     __syncthreads();
@@ -236,7 +347,7 @@ __global__ void __launch_bounds__(64)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen);
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
 constexpr int kStages = 8;
@@ -383,6 +494,8 @@ struct AxisProblem {
   int64_t alen, astride;
   KeptDims kept;  // collapsed kept dims, outer to inner
   int64_t n_out;
+  const void* lane_mean;  // VAR/STD second pass: per-lane means (else null)
+  double div;             // VAR/STD divisor: axis length - ddof
 };
 
 template <typename T, int OP>
@@ -391,8 +504,19 @@ int launch_generic(nrs_handle* h, const AxisProblem& p) {
   int grid = (int)(blocks < (int64_t)h->num_sms * 16 ? blocks : (int64_t)h->num_sms * 16);
   if (grid < 1) grid = 1;
   fold_generic<T, OP><<<grid, 256, 0, h->stream>>>(
-      (const T*)p.x, p.kept, p.n_out, p.alen, p.astride, (typename OutOf<T, OP>::type*)p.out);
+      (const T*)p.x, p.kept, p.n_out, p.alen, p.astride, (typename OutOf<T, OP>::type*)p.out,
+      (const T*)p.lane_mean, (T)p.div);
   return nrs_after_launch(h, "fold_generic");
+}
+
+template <typename T, bool MAX>
+int launch_arg(nrs_handle* h, const AxisProblem& p) {
+  int64_t blocks = (p.n_out + 255) / 256;
+  int grid = (int)(blocks < (int64_t)h->num_sms * 16 ? blocks : (int64_t)h->num_sms * 16);
+  if (grid < 1) grid = 1;
+  arg_generic<T, MAX><<<grid, 256, 0, h->stream>>>((const T*)p.x, p.kept, p.n_out, p.alen,
+                                                   p.astride, (int64_t*)p.out);
+  return nrs_after_launch(h, "arg_generic");
 }
 
 // Builds a 3-D tensor map (dim0 contiguous). Returns false if TMA rules are
@@ -440,7 +564,8 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
     auto kern = fold_cols_tma<T, OP, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((unsigned)((lanes + kColLanes - 1) / kColLanes), (unsigned)batch);
-    kern<<<grid, kColLanes, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
+    kern<<<grid, kColLanes, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error,
+                                               (const T*)p.lane_mean, (T)p.div);
     return nrs_after_launch(h, "fold_cols_tma");
   }
   if (p.astride == 1 && lstride > 1) {
@@ -454,7 +579,8 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
     auto kern = fold_rows_tma<T, OP, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch);
-    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error,
+                                        (const T*)p.lane_mean, (T)p.div);
     return nrs_after_launch(h, "fold_rows_tma");
   }
   (void)tile_bytes;
@@ -479,7 +605,27 @@ int dispatch_axis_ops(nrs_handle* h, const AxisProblem& p) {
     case NRS_MAX: return dispatch_axis_t<T, NRS_MAX>(h, p);
     case NRS_MIN: return dispatch_axis_t<T, NRS_MIN>(h, p);
     case NRS_PROD: return dispatch_axis_t<T, NRS_PROD>(h, p);
-    default: return nrs_fail(h, NRS_ERR_UNSUPPORTED, "axis VAR/STD are not provided");
+    case NRS_ARGMAX: return launch_arg<T, true>(h, p);
+    case NRS_ARGMIN: return launch_arg<T, false>(h, p);
+    default: {
+      if constexpr (!std::is_floating_point<T>::value) {
+        return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
+      } else {
+        // math::statistics::var(axis): per-lane mean first (the MEAN fold),
+        // then the sum of squared deviations from it, / (axis length - ddof).
+        int st;
+        T* means = (T*)nrs_workspace(h, (size_t)p.n_out * sizeof(T) + 256, &st);
+        if (!means) return st;
+        AxisProblem pm = p;
+        pm.out = means;
+        pm.lane_mean = nullptr;
+        if ((st = dispatch_axis_t<T, NRS_MEAN>(h, pm))) return st;
+        AxisProblem pv = p;
+        pv.lane_mean = means;
+        return p.op == NRS_VAR ? dispatch_axis_t<T, NRS_VAR>(h, pv)
+                               : dispatch_axis_t<T, NRS_STD>(h, pv);
+      }
+    }
   }
 }
 
@@ -541,6 +687,18 @@ int flat_reduce(nrs_handle* h, int op, int64_t n, int64_t ddof, const T* x, void
   return nrs_after_launch(h, "flat reduction");
 }
 
+template <typename T, bool MAX>
+int flat_arg(nrs_handle* h, int64_t n, const void* x, void* out) {
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  int st;
+  ArgCand<T>* part = (ArgCand<T>*)nrs_workspace(h, (size_t)(nchunks + 1) * sizeof(ArgCand<T>), &st);
+  if (!part) return st;
+  const int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
+  arg_partials<T, MAX><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
+  arg_finish<T, MAX><<<1, 32, 0, h->stream>>>((const T*)x, part, nchunks, (int64_t*)out);
+  return nrs_after_launch(h, "flat argmax/argmin");
+}
+
 // Integer flat reductions: any order is exact. MEAN writes f64.
 template <typename T>
 int flat_reduce_int(nrs_handle* h, int op, int64_t n, const T* x, void* out) {
@@ -593,7 +751,8 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
   h->last_error.clear();
   if (ndim < 0 || ndim > NRS_UFUNC_MAX_DIMS || (ndim > 0 && (!shape || !strides)))
     return nrs_fail(h, NRS_ERR_INVALID, "bad ndim/shape/strides");
-  if (op < NRS_SUM || op > NRS_STD) return nrs_fail(h, NRS_ERR_INVALID, "unknown reduce op");
+  if (op < NRS_SUM || op > NRS_ARGMIN) return nrs_fail(h, NRS_ERR_INVALID, "unknown reduce op");
+  const bool is_arg = (op == NRS_ARGMAX || op == NRS_ARGMIN);
   const size_t es = nrs_dtype_size(dtype);
   if (!es) return nrs_fail(h, NRS_ERR_DTYPE, "unknown dtype");
   const bool is_int = (dtype == NRS_I32 || dtype == NRS_I64);
@@ -611,6 +770,9 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
     if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
     if (is_int && (op == NRS_VAR || op == NRS_STD))
       return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
+    if (is_arg && total == 0)
+      return nrs_fail(h, NRS_ERR_EMPTY, op == NRS_ARGMAX ? "Cannot find argmax of empty array"
+                                                         : "Cannot find argmin of empty array");
     // Non-contiguous views are gathered into logical order first, as
     // kernels::borrow::operand does.
     bool contig = true;
@@ -642,6 +804,14 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
       // The flat kernels must not reuse the gathered region as partials: the
       // workspace is large enough that their partials (at offset 0) fit below.
     }
+    if (is_arg) {
+      switch (dtype) {
+        case NRS_F32: return op == NRS_ARGMAX ? flat_arg<float, true>(h, total, src, out) : flat_arg<float, false>(h, total, src, out);
+        case NRS_F64: return op == NRS_ARGMAX ? flat_arg<double, true>(h, total, src, out) : flat_arg<double, false>(h, total, src, out);
+        case NRS_I64: return op == NRS_ARGMAX ? flat_arg<int64_t, true>(h, total, src, out) : flat_arg<int64_t, false>(h, total, src, out);
+        default: return op == NRS_ARGMAX ? flat_arg<int32_t, true>(h, total, src, out) : flat_arg<int32_t, false>(h, total, src, out);
+      }
+    }
     switch (dtype) {
       case NRS_F32: return flat_reduce<float>(h, op, total, ddof, (const float*)src, out);
       case NRS_F64: return flat_reduce<double>(h, op, total, ddof, (const double*)src, out);
@@ -657,10 +827,15 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
                                          " out of bounds for array of dimension " +
                                          std::to_string(ndim));
   }
-  if (op == NRS_VAR || op == NRS_STD)
-    return nrs_fail(h, NRS_ERR_UNSUPPORTED, "axis VAR/STD are not provided");
+  if (is_int && (op == NRS_VAR || op == NRS_STD))
+    return nrs_fail(h, NRS_ERR_DTYPE, "VAR/STD need a float dtype");
   if (is_int && op == NRS_MEAN && dtype == NRS_I32)
     return nrs_fail(h, NRS_ERR_DTYPE, "i32 MEAN is not provided");
+  if (total == 0 && (op == NRS_VAR || op == NRS_STD || is_arg))
+    return nrs_fail(h, NRS_ERR_EMPTY, "Cannot reduce an empty array");
+  if ((op == NRS_VAR || op == NRS_STD) && (ddof < 0 || shape[ax] <= ddof))
+    return nrs_fail(h, NRS_ERR_EMPTY, "Degrees of freedom " + std::to_string(ddof) +
+                                          " >= axis size " + std::to_string(shape[ax]));
 
   AxisProblem p{};
   p.dtype = dtype;
@@ -669,6 +844,8 @@ extern "C" int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int6
   p.out = out;
   p.alen = shape[ax];
   p.astride = strides[ax];
+  p.lane_mean = nullptr;
+  p.div = (double)(shape[ax] - ddof);
   // Collapse kept dims (outer to inner), dropping size-1 dims.
   KeptDims kd{};
   kd.n = 0;

@@ -77,15 +77,39 @@ template <typename T, int OP> struct OutOf { using type = T; };
 template <> struct OutOf<int64_t, NRS_MEAN> { using type = double; };
 template <> struct OutOf<int32_t, NRS_MEAN> { using type = double; };
 
+// `div` is the variance divisor (axis length - ddof) for VAR/STD.
 template <typename T, int OP>
-__device__ __forceinline__ typename OutOf<T, OP>::type finish(T acc, int64_t n) {
+__device__ __forceinline__ typename OutOf<T, OP>::type finish(T acc, int64_t n, T div = T(1)) {
   if constexpr (OP == NRS_MEAN) {
     if constexpr (std::is_floating_point<T>::value)
       return acc / (T)n;
     else
       return (double)acc / (double)n;
+  } else if constexpr (OP == NRS_VAR || OP == NRS_STD) {
+    if constexpr (std::is_floating_point<T>::value) {
+      const T v = acc / div;
+      return OP == NRS_STD ? sqrt(v) : v;
+    } else {
+      return acc;
+    }
   } else {
     return acc;
+  }
+}
+
+// Per-element transform of a lane fold: VAR/STD fold (x - mean)^2 of the
+// lane (math::statistics::var(axis), src/math/statistics/mod.rs:1483-1488:
+// `diff = val - mean; sum_sq + diff * diff`, each op rounded once).
+template <typename T, int OP>
+__device__ __forceinline__ T lane_xform(T v, T m) {
+  if constexpr ((OP == NRS_VAR || OP == NRS_STD) && std::is_same<T, float>::value) {
+    const float d = __fsub_rn(v, m);
+    return __fmul_rn(d, d);
+  } else if constexpr ((OP == NRS_VAR || OP == NRS_STD) && std::is_same<T, double>::value) {
+    const double d = __dsub_rn(v, m);
+    return __dmul_rn(d, d);
+  } else {
+    return v;
   }
 }
 

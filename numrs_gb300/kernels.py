@@ -98,7 +98,10 @@ def reduce(a: torch.Tensor, op: int, axis: int | None = None, keepdims: bool = F
                 out_shape = [1]
         else:
             out_shape = [1]
-    out_dtype = torch.float64 if (op == L.MEAN and code in (L.I32, L.I64)) else a.dtype
+    if op in (L.ARGMAX, L.ARGMIN):
+        out_dtype = torch.int64
+    else:
+        out_dtype = torch.float64 if (op == L.MEAN and code in (L.I32, L.I64)) else a.dtype
     out = torch.empty(out_shape, dtype=out_dtype, device=a.device)
     shape = L.i64_array(a.shape)
     strides = L.i64_array(a.stride())
@@ -133,6 +136,15 @@ def var(a, axis=None, ddof=0, keepdims=False):
 
 def std(a, axis=None, ddof=0, keepdims=False):
     return reduce(a, L.STD, axis, keepdims, ddof)
+
+
+def argmax(a, axis=None, keepdims=False):
+    """math::statistics::argmax: int64 indices (first index of the maximum)."""
+    return reduce(a, L.ARGMAX, axis, keepdims)
+
+
+def argmin(a, axis=None, keepdims=False):
+    return reduce(a, L.ARGMIN, axis, keepdims)
 
 
 def sum_axis(a, axis: int):

@@ -312,6 +312,71 @@ static void lane_bases(int ndim, const int64_t* shape, const int64_t* strides, i
 DEFINE_AXIS_FLOAT(float, f32)
 DEFINE_AXIS_FLOAT(double, f64)
 
+/* math::statistics::var(axis, ddof) (src/math/statistics/mod.rs:1404-1500):
+ * the lane mean from mean(axis) (zero-seeded left-to-right sum / n), then a
+ * zero-seeded left-to-right sum of diff*diff (diff = val - mean), divided by
+ * (axis_size - ddof); std = sqrt(var) (:1308). */
+#define DEFINE_AXIS_VAR(T, SUF, SQRT)                                                      \
+  void orc_axis_var_##SUF(int ndim, const int64_t* shape, const int64_t* strides,          \
+                          int axis, int64_t ddof, int want_std, const T* x, T* out) {      \
+    int64_t n_out = 1;                                                                     \
+    for (int d = 0; d < ndim; ++d) if (d != axis) n_out *= shape[d];                       \
+    const int64_t alen = shape[axis], ast = strides[axis];                                 \
+    const T divisor = (T)(alen - ddof);                                                    \
+    _Pragma("omp parallel for schedule(static)")                                           \
+    for (int64_t o = 0; o < n_out; ++o) {                                                  \
+      int64_t b;                                                                           \
+      lane_bases(ndim, shape, strides, axis, o, &b);                                       \
+      const T* p = x + b;                                                                  \
+      T s = (T)0;                                                                          \
+      for (int64_t j = 0; j < alen; ++j) s = s + p[j * ast];                               \
+      const T mean = s / (T)alen;                                                          \
+      T sq = (T)0;                                                                         \
+      for (int64_t j = 0; j < alen; ++j) {                                                 \
+        T diff = p[j * ast] - mean;                                                        \
+        sq = sq + diff * diff;                                                             \
+      }                                                                                    \
+      T v = sq / divisor;                                                                  \
+      out[o] = want_std ? SQRT(v) : v;                                                     \
+    }                                                                                      \
+  }
+DEFINE_AXIS_VAR(float, f32, sqrtf)
+DEFINE_AXIS_VAR(double, f64, sqrt)
+
+/* math::statistics::argmax/argmin (src/math/statistics/mod.rs:79-198,
+ * :218-330): axis = Some -> per lane, the first element starts, a later one
+ * wins only if strictly greater (smaller); axis = None -> the same scan over
+ * the flattened array. Written for any dtype through a comparison macro. */
+#define DEFINE_ARG(T, SUF)                                                                 \
+  void orc_axis_arg_##SUF(int want_max, int ndim, const int64_t* shape,                    \
+                          const int64_t* strides, int axis, const T* x, int64_t* out) {    \
+    int64_t n_out = 1;                                                                     \
+    for (int d = 0; d < ndim; ++d) if (d != axis) n_out *= shape[d];                       \
+    const int64_t alen = shape[axis], ast = strides[axis];                                 \
+    for (int64_t o = 0; o < n_out; ++o) {                                                  \
+      int64_t b;                                                                           \
+      lane_bases(ndim, shape, strides, axis, o, &b);                                       \
+      const T* p = x + b;                                                                  \
+      T best = p[0];                                                                       \
+      int64_t bi = 0;                                                                      \
+      for (int64_t j = 1; j < alen; ++j) {                                                 \
+        T v = p[j * ast];                                                                  \
+        if (want_max ? (v > best) : (v < best)) { best = v; bi = j; }                      \
+      }                                                                                    \
+      out[o] = bi;                                                                         \
+    }                                                                                      \
+  }                                                                                        \
+  int64_t orc_flat_arg_##SUF(int want_max, const T* x, int64_t n) {                        \
+    T best = x[0];                                                                         \
+    int64_t bi = 0;                                                                        \
+    for (int64_t i = 1; i < n; ++i)                                                        \
+      if (want_max ? (x[i] > best) : (x[i] < best)) { best = x[i]; bi = i; }               \
+    return bi;                                                                             \
+  }
+DEFINE_ARG(float, f32)
+DEFINE_ARG(double, f64)
+DEFINE_ARG(int64_t, i64)
+
 /* Integer axis folds: Array::sum_axis (src/array/operations.rs:75-156),
  * math::max/min(axis) for T: PartialOrd. There is no integer mean in the
  * reference (math::mean needs T: Float); MEAN here is the f64 lane sum / n

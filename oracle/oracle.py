@@ -88,6 +88,14 @@ def _declare(L):
     L.orc_set_threads.argtypes, L.orc_set_threads.restype = [i32], None
     L.orc_mlp_forward_backward.argtypes = [i64, i64, i64, i64] + [vp] * 16
     L.orc_mlp_forward_backward.restype = f32
+    for suf in ("f32", "f64"):
+        fn = getattr(L, f"orc_axis_var_{suf}")
+        fn.argtypes, fn.restype = [i32, vp, vp, i32, i64, i32, vp, vp], None
+    for suf in ("f32", "f64", "i64"):
+        fn = getattr(L, f"orc_axis_arg_{suf}")
+        fn.argtypes, fn.restype = [i32, i32, vp, vp, i32, vp, vp], None
+        fn = getattr(L, f"orc_flat_arg_{suf}")
+        fn.argtypes, fn.restype = [i32, vp, i64], i64
 
 
 _SUF = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.int64): "i64"}
@@ -137,6 +145,37 @@ class Oracle:
         ptr = C.c_void_p(x.__array_interface__["data"][0])
         fn = getattr(self.L, f"orc_axis_{suf}")
         fn(op, x.ndim, _p(shape), _p(strides), axis, ptr, _p(out))
+        return out
+
+    def _view_args(self, x, axis):
+        if axis < 0:
+            axis += x.ndim
+        item = x.dtype.itemsize
+        shape = np.array(x.shape, dtype=np.int64)
+        strides = np.array([s // item for s in x.strides], dtype=np.int64)
+        out_shape = [d for i, d in enumerate(x.shape) if i != axis]
+        return axis, shape, strides, (out_shape if out_shape else [1])
+
+    def axis_var(self, x: np.ndarray, axis: int, ddof: int = 0, std: bool = False) -> np.ndarray:
+        """math::statistics::var/std(axis, ddof) restated (two passes per lane)."""
+        axis, shape, strides, out_shape = self._view_args(x, axis)
+        out = np.empty(out_shape, dtype=x.dtype)
+        getattr(self.L, f"orc_axis_var_{_SUF[x.dtype]}")(
+            x.ndim, _p(shape), _p(strides), axis, ddof, int(std),
+            C.c_void_p(x.__array_interface__["data"][0]), _p(out))
+        return out
+
+    def axis_arg(self, x: np.ndarray, axis, want_max: bool) -> np.ndarray:
+        """math::statistics::argmax/argmin restated (axis=None: flattened)."""
+        if axis is None:
+            flat = np.ascontiguousarray(x).ravel()
+            return np.array([getattr(self.L, f"orc_flat_arg_{_SUF[x.dtype]}")(int(want_max), _p(flat), flat.size)],
+                            dtype=np.int64)
+        axis, shape, strides, out_shape = self._view_args(x, axis)
+        out = np.empty(out_shape, dtype=np.int64)
+        getattr(self.L, f"orc_axis_arg_{_SUF[x.dtype]}")(
+            int(want_max), x.ndim, _p(shape), _p(strides), axis,
+            C.c_void_p(x.__array_interface__["data"][0]), _p(out))
         return out
 
     # -- elementwise ------------------------------------------------------

@@ -61,12 +61,8 @@ def test_numpy_stat_goldens(ora, key):
         np.testing.assert_allclose(got, case["result"], rtol=1e-15, atol=1e-15)
     else:
         code = {"sum": O.SUM, "mean": O.MEAN, "max": O.MAX, "min": O.MIN}.get(op)
-        if code is None:  # var/std along an axis: mean-of-squares from two axis folds
-            mu = ora.axis(O.MEAN, x, axis)
-            d = x - np.expand_dims(mu, axis)
-            got = ora.axis(O.MEAN, d * d, axis)
-            if op == "std":
-                got = np.sqrt(got)
+        if code is None:  # var/std(axis, ddof=0): math::statistics::var restated
+            got = ora.axis_var(x, axis, ddof=0, std=(op == "std"))
         else:
             got = ora.axis(code, x, axis)
         np.testing.assert_allclose(got, _arr(case["result"]).ravel(), rtol=1e-15, atol=1e-15)
@@ -155,3 +151,20 @@ def test_generator_twins(ora):
         assert np.array_equal(rng.splitmix64(seed, 16), ref)
     assert np.array_equal(rng.uniform_pm1(7, 1000), ora.gen_uniform_pm1(7, 1000))
     assert np.array_equal(rng.int_range(4, 1000), ora.gen_i64(4, 1000))
+
+
+def test_argmax_argmin_reference_examples(ora):
+    # The reference's own doc examples (src/math/statistics/mod.rs:64-77, :203-216).
+    a = np.array([1.0, 3.0, 2.0, 4.0, 5.0, 1.0]).reshape(2, 3)
+    assert list(ora.axis_arg(a, 1, True)) == [1, 1]
+    assert list(ora.axis_arg(a, -1, True)) == [1, 1]
+    assert list(ora.axis_arg(a, None, True)) == [4]
+    b = np.array([5.0, 3.0, 2.0, 4.0, 1.0, 6.0]).reshape(2, 3)
+    assert list(ora.axis_arg(b, 1, False)) == [2, 1]
+    assert list(ora.axis_arg(b, None, False)) == [4]
+
+
+def test_axis_var_ddof(ora):
+    x = np.arange(12, dtype=np.float64).reshape(3, 4)
+    np.testing.assert_allclose(ora.axis_var(x, 0, ddof=1), np.var(x, axis=0, ddof=1), rtol=1e-15)
+    np.testing.assert_allclose(ora.axis_var(x, 1, ddof=0, std=True), np.std(x, axis=1), rtol=1e-15)
