@@ -58,6 +58,20 @@ def whole_job_gbs(step_bytes: int, world: int, ms_per_step: float) -> float:
     return step_bytes * world / (ms_per_step / 1e3) / 1e9
 
 
+def profiled_traffic(kernel_class: str):
+    """DRAM bytes per full-size launch of `kernel_class` recorded from an ncu
+    capture in profiles/*.md as a line `traffic_per_launch_bytes[<class>] = N`."""
+    import glob
+    import re
+    pat = re.compile(r"traffic_per_launch_bytes\[([^\]]+)\]\s*=\s*([0-9]+)")
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(path):
+            m = pat.search(line)
+            if m and m.group(1) == kernel_class:
+                return int(m.group(2))
+    return None
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -261,6 +275,33 @@ def gemm_section(K, L, quick: bool):
     return out
 
 
+def elementwise_section(K, L):
+    """Operators on 16384x16384 f32 (binary_serial / *_broadcast): same-shape
+    add (12 B/elem), add of a broadcast row (8 B/elem), and an ExprNode tree
+    (a*b + c, 16 B/elem), each one launch."""
+    import torch
+    n = R * C_
+    stream = torch.cuda.current_stream()
+    a = torch.empty((R, C_), device="cuda")
+    b = torch.empty_like(a)
+    c = torch.empty_like(a)
+    K.fill_random(a, L.RNG_NORMAL, 11, 0.0, 1.0)
+    K.fill_random(b, L.RNG_NORMAL, 12, 0.0, 1.0)
+    K.fill_random(c, L.RNG_NORMAL, 13, 0.0, 1.0)
+    row = b[0].clone()
+    E = K.Expr.leaf
+    cases = {"add_same_shape": (lambda: K.add(a, b), 12 * n),
+             "add_broadcast_row": (lambda: K.add(a, row), 8 * n + 4 * C_),
+             "expr_a_mul_b_add_c": (lambda: ((E(a) * E(b)) + E(c)).eval(), 16 * n)}
+    out = {}
+    for name, (fn, nbytes) in cases.items():
+        ms = _time_ms(fn, 5, stream)
+        out[name] = {"ms": round(ms, 4), "gbs": round(nbytes / ms / 1e6, 1)}
+    del a, b, c
+    torch.cuda.empty_cache()
+    return out
+
+
 def grouped_section(K, L, seed: int = 7):
     """4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64) and
     4096 row reductions (length log-uniform in [64, 65536]) in one persistent
@@ -340,6 +381,7 @@ def main():
     ap.add_argument("--no-gemm", action="store_true")
     ap.add_argument("--quick-gemm", action="store_true", help="2048^3 instead of 8192^3")
     ap.add_argument("--no-grouped", action="store_true")
+    ap.add_argument("--no-elementwise", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -416,10 +458,7 @@ def main():
                         "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
                         "share": round(sum(ts) / sum(sum(v) for v in per_class.values()), 4)}
     dom = max(kernels, key=lambda c: kernels[c]["share"])
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(dom)
+    traffic = profiled_traffic(dom)
 
     out = {"metric": "reduce GB/s", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
@@ -517,6 +556,8 @@ def main():
         ops = None
         torch.cuda.empty_cache()
         out["gemm"] = gemm_section(K, L, quick=args.quick_gemm)
+    if rank == 0 and not args.no_elementwise:
+        out["elementwise"] = elementwise_section(K, L)
     if rank == 0 and not args.no_grouped:
         out["grouped"] = grouped_section(K, L)
     if rank == 0:

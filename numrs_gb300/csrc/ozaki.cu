@@ -439,19 +439,32 @@ __global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k
   }
 }
 
-// Column exponents of B (k x n row-major): thread per column.
-__global__ void col_exponents(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
-                              int* __restrict__ eb) {
+// Column maxima of |B| (k x n row-major) as IEEE bit patterns (ordered like
+// the magnitudes): a 2-D grid of 256-row strips, coalesced across columns,
+// combined with atomicMax on the bit pattern into a zeroed array.
+constexpr int kColStrip = 256;
+__global__ void col_max_bits(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
+                             unsigned long long* __restrict__ colmax) {
   const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= n) return;
-  uint64_t mx = 0;
-  for (int64_t i = 0; i < k; ++i) {
-    uint64_t b = (uint64_t)__double_as_longlong(B[i * ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
+  const int64_t r0 = (int64_t)blockIdx.y * kColStrip;
+  const int64_t r1 = (r0 + kColStrip) < k ? (r0 + kColStrip) : k;
+  unsigned long long mx = 0;
+  for (int64_t i = r0; i < r1; ++i) {
+    const unsigned long long b =
+        (unsigned long long)__double_as_longlong(B[i * ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
     mx = b > mx ? b : mx;
   }
-  int e = (int)(mx >> 52) - 1022;
-  if ((mx >> 52) == 0) e = -1021;
-  eb[col] = e;
+  atomicMax(&colmax[col], mx);
+}
+
+// frexp-style exponent from a max-magnitude bit pattern.
+__global__ void exponents_from_bits(const unsigned long long* __restrict__ mx, int64_t n,
+                                    int* __restrict__ e) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long b = mx[i];
+  e[i] = ((b >> 52) == 0) ? -1021 : (int)(b >> 52) - 1022;
 }
 
 // Signed 6-bit digits of x * 2^-e (|x| < 2^e): see the file header.
@@ -602,7 +615,13 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   cudaStream_t s = h->stream;
 
   row_exponents<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(A, m, k, lda, ea);
-  col_exponents<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, k, n, ldb, eb);
+  // Column maxima go through the (not yet used) accumulator region.
+  unsigned long long* colmax = reinterpret_cast<unsigned long long*>(acc);
+  if ((st = nrs_cuda_check(h, cudaMemsetAsync(colmax, 0, (size_t)n * 8, s), "cudaMemsetAsync")))
+    return st;
+  col_max_bits<<<dim3((unsigned)((n + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip)), 256, 0,
+                 s>>>(B, k, n, ldb, colmax);
+  exponents_from_bits<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(colmax, n, eb);
   int grid = h->num_sms * 8;
   slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
   dim3 g2((unsigned)((n + 31) / 32), (unsigned)((kpad + 31) / 32));

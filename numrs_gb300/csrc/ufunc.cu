@@ -88,6 +88,161 @@ __device__ __forceinline__ T binop(int code, T a, T b) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Evaluators. Everything stays in registers: inputs and the value stack are
+// fixed-size arrays read and written only at compile-time indices (a select
+// loop over the slots instead of a dynamic index, which would spill them to
+// local memory).
+// ---------------------------------------------------------------------------
+constexpr int kMaxIn = 4;  // inputs the register evaluators handle
+
+template <typename T, int N>
+__device__ __forceinline__ T sel(const T (&r)[N], int i) {
+  T v = r[0];
+#pragma unroll
+  for (int q = 1; q < N; ++q)
+    if (q == i) v = r[q];
+  return v;
+}
+template <typename T, int N>
+__device__ __forceinline__ void put(T (&r)[N], int i, T v) {
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    if (q == i) r[q] = v;
+}
+
+// The general program, interpreted per element.
+template <typename T>
+struct ProgEval {
+  Prog prog;
+  __device__ __forceinline__ T operator()(const T (&in)[kMaxIn]) const {
+    T st[kStack];
+#pragma unroll
+    for (int q = 0; q < kStack; ++q) st[q] = T(0);
+    int sp = 0;
+    for (int pc = 0; pc < prog.len; ++pc) {
+      const int code = prog.code[pc];
+      if (code == NRS_OP_INPUT) {
+        put(st, sp++, sel(in, prog.arg[pc]));
+      } else if (code == NRS_OP_SCALAR) {
+        put(st, sp++, (T)prog.scalar[pc]);
+      } else if (code >= NRS_OP_NEG && code <= NRS_OP_LN) {
+        put(st, sp - 1, unary<T>(code, sel(st, sp - 1)));
+      } else {
+        const T b = sel(st, --sp);
+        put(st, sp - 1, binop<T>(code, sel(st, sp - 1), b));
+      }
+    }
+    return st[0];
+  }
+};
+
+// `inputs[0] op inputs[1]`: the operators and binary closures.
+template <typename T, int OP>
+struct BinEval {
+  __device__ __forceinline__ T operator()(const T (&in)[kMaxIn]) const {
+    return binop<T>(OP, in[0], in[1]);
+  }
+};
+
+// Any strides, one element per thread, full index decode (small inner dims).
+template <typename T, typename Eval>
+__global__ void __launch_bounds__(256)
+    ufunc_decode(Eval ev, Geometry g, int64_t n, T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t off[kMaxIn] = {0, 0, 0, 0};
+    int64_t ooff = 0;
+    int64_t rem = i;
+    for (int d = g.ndim - 1; d >= 0; --d) {
+      const int64_t c = rem % g.shape[d];
+      rem /= g.shape[d];
+      ooff += c * g.out_stride[d];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k) off[k] += c * g.in_stride[k][d];
+    }
+    T v[kMaxIn];
+#pragma unroll
+    for (int k = 0; k < kMaxIn; ++k)
+      v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k]] : T(0);
+    out[ooff] = ev(v);
+  }
+}
+
+// Broadcast / strided views with a long last dimension: a CTA takes one
+// row (all dims but the last) at a time, decodes its offsets once and walks
+// the row with plain strided increments.
+template <typename T, typename Eval>
+__global__ void __launch_bounds__(256)
+    ufunc_rows(Eval ev, Geometry g, int64_t rows, T* __restrict__ out) {
+  const int last = g.ndim - 1;
+  const int64_t inner = g.shape[last];
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t off[kMaxIn] = {0, 0, 0, 0};
+    int64_t ooff = 0;
+    int64_t rem = r;
+    for (int d = last - 1; d >= 0; --d) {
+      const int64_t c = rem % g.shape[d];
+      rem /= g.shape[d];
+      ooff += c * g.out_stride[d];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k) off[k] += c * g.in_stride[k][d];
+    }
+    for (int64_t j = threadIdx.x; j < inner; j += blockDim.x) {
+      T v[kMaxIn];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k)
+        v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k] + j * g.in_stride[k][last]] : T(0);
+      out[ooff + j * g.out_stride[last]] = ev(v);
+    }
+  }
+}
+
+// Same-shape contiguous, 16-byte aligned inputs and output (the common
+// `&a + &b` of binary_serial): 16 bytes of every input per thread step.
+template <typename T, typename Eval>
+__global__ void __launch_bounds__(256)
+    ufunc_flat_vec(Eval ev, Geometry g, int64_t n, T* __restrict__ out) {
+  using V = typename std::conditional<sizeof(T) == 4, int4, longlong2>::type;
+  constexpr int PER = 16 / sizeof(T);
+  const int64_t nv = n / PER;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv; i += stride) {
+    T x[kMaxIn][PER];
+#pragma unroll
+    for (int k = 0; k < kMaxIn; ++k) {
+      if (k < g.n_inputs) {
+        const V q = __ldcs(reinterpret_cast<const V*>(g.in[k]) + i);
+        memcpy(x[k], &q, 16);
+      } else {
+#pragma unroll
+        for (int e = 0; e < PER; ++e) x[k][e] = T(0);
+      }
+    }
+    T res[PER];
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      T v[kMaxIn];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k) v[k] = x[k][e];
+      res[e] = ev(v);
+    }
+    V q;
+    memcpy(&q, res, 16);
+    __stcs(reinterpret_cast<V*>(out) + i, q);
+  }
+  // scalar tail (< PER elements)
+  const int64_t t = nv * PER + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n) {
+    T v[kMaxIn];
+#pragma unroll
+    for (int k = 0; k < kMaxIn; ++k) v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[t] : T(0);
+    out[t] = ev(v);
+  }
+}
+
+// Programs with more than kMaxIn inputs: the stack interpreter over up to 8
+// inputs with a full index decode per element.
 template <typename T>
 __global__ void __launch_bounds__(256)
     ufunc_generic(Prog prog, Geometry g, int64_t n, T* __restrict__ out) {
@@ -190,13 +345,49 @@ int launch_exp_affine(nrs_handle* h, int64_t n, const T* x, T a, T b, T* y) {
   return nrs_after_launch(h, "exp_affine");
 }
 
-template <typename T>
-int launch_generic(nrs_handle* h, const Prog& p, const Geometry& g, int64_t n, void* out) {
+// Picks the access pattern: flat vectors, row walks, or a full decode.
+template <typename T, typename Eval>
+int launch_eval(nrs_handle* h, const Eval& ev, const Geometry& g, int64_t n, bool flat, void* out) {
   if (n == 0) return NRS_OK;
-  int64_t need = (n + 255) / 256;
-  int grid = (int)(need < (int64_t)h->num_sms * 16 ? need : (int64_t)h->num_sms * 16);
-  ufunc_generic<T><<<grid, 256, 0, h->stream>>>(p, g, n, (T*)out);
-  return nrs_after_launch(h, "ufunc_generic");
+  const int cap = h->num_sms * 8;
+  if (flat) {
+    const int64_t need = (n / (16 / (int64_t)sizeof(T)) + 255) / 256 + 1;
+    const int grid = (int)(need < cap ? need : cap);
+    ufunc_flat_vec<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, n, (T*)out);
+    return nrs_after_launch(h, "ufunc_flat_vec");
+  }
+  if (g.ndim >= 1 && g.shape[g.ndim - 1] >= 256) {
+    const int64_t rows = n / g.shape[g.ndim - 1];
+    const int grid = (int)(rows < (int64_t)h->num_sms * 16 ? rows : (int64_t)h->num_sms * 16);
+    ufunc_rows<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, rows, (T*)out);
+    return nrs_after_launch(h, "ufunc_rows");
+  }
+  const int64_t need = (n + 255) / 256;
+  const int grid = (int)(need < (int64_t)h->num_sms * 16 ? need : (int64_t)h->num_sms * 16);
+  ufunc_decode<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, n, (T*)out);
+  return nrs_after_launch(h, "ufunc_decode");
+}
+
+// Dispatch on the program's shape: a lone binary op gets its own functor.
+template <typename T>
+int launch_program(nrs_handle* h, const Prog& p, const Geometry& g, int64_t n, bool flat, void* out) {
+  if (g.n_inputs > kMaxIn) {
+    const int64_t need = (n + 255) / 256;
+    const int grid = (int)(need < (int64_t)h->num_sms * 16 ? need : (int64_t)h->num_sms * 16);
+    ufunc_generic<T><<<grid, 256, 0, h->stream>>>(p, g, n, (T*)out);
+    return nrs_after_launch(h, "ufunc_generic");
+  }
+  if (p.len == 3 && p.code[0] == NRS_OP_INPUT && p.arg[0] == 0 && p.code[1] == NRS_OP_INPUT &&
+      p.arg[1] == 1) {
+    switch (p.code[2]) {
+      case NRS_OP_ADD: return launch_eval<T>(h, BinEval<T, NRS_OP_ADD>{}, g, n, flat, out);
+      case NRS_OP_SUB: return launch_eval<T>(h, BinEval<T, NRS_OP_SUB>{}, g, n, flat, out);
+      case NRS_OP_MUL: return launch_eval<T>(h, BinEval<T, NRS_OP_MUL>{}, g, n, flat, out);
+      case NRS_OP_DIV: return launch_eval<T>(h, BinEval<T, NRS_OP_DIV>{}, g, n, flat, out);
+      default: break;
+    }
+  }
+  return launch_eval<T>(h, ProgEval<T>{p}, g, n, flat, out);
 }
 
 }  // namespace
@@ -295,10 +486,17 @@ extern "C" int nrs_ufunc(nrs_handle* h, int dtype, const nrs_ufunc_op* prog, int
     // (x * a) rounds the same as (a * x): IEEE multiplication is commutative.
     return nrs_exp_affine(h, dtype, n, inputs[0], prog[1].scalar, prog[3].scalar, out);
   }
+  // Same-shape contiguous operands, all 16-byte aligned: flat vector path.
+  bool flat = false;
+  if (all_contig) {
+    uintptr_t align = reinterpret_cast<uintptr_t>(out);
+    for (int k = 0; k < n_inputs; ++k) align |= reinterpret_cast<uintptr_t>(inputs[k]);
+    flat = (align & 15) == 0;
+  }
   switch (dtype) {
-    case NRS_F32: return launch_generic<float>(h, p, g, n, out);
-    case NRS_F64: return launch_generic<double>(h, p, g, n, out);
-    case NRS_I64: return launch_generic<int64_t>(h, p, g, n, out);
-    default: return launch_generic<int32_t>(h, p, g, n, out);
+    case NRS_F32: return launch_program<float>(h, p, g, n, flat, out);
+    case NRS_F64: return launch_program<double>(h, p, g, n, flat, out);
+    case NRS_I64: return launch_program<int64_t>(h, p, g, n, flat, out);
+    default: return launch_program<int32_t>(h, p, g, n, flat, out);
   }
 }

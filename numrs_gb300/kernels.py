@@ -226,10 +226,22 @@ def matmul(a: torch.Tensor, b: torch.Tensor, variant: int = L.GEMM_AUTO) -> torc
     if len(batch) == 0:
         _gemm_views(ab, bb, out, False, variant)
     else:
+        # batched_gemm (src/array/linalg.rs:56-136): every batch panel of the
+        # broadcast operands; f32/f64 panels run as one grouped launch.
+        panels = []
         for idx in range(out[..., 0, 0].numel()):
             bi = torch.unravel_index(torch.tensor(idx), batch)
             bi = tuple(int(x) for x in bi)
-            _gemm_views(ab[bi], bb[bi], out[bi], False, variant)
+            panels.append((ab[bi], bb[bi], out[bi]))
+        grouped_ok = a.dtype in (torch.float32, torch.float64) and variant == L.GEMM_AUTO and all(
+            _mat_strides(p[0]) is not None and _mat_strides(p[1]) is not None for p in panels)
+        if grouped_ok and m > 0 and n > 0:
+            plan = Plan([(pa, pb, pc, False) for pa, pb, pc in panels])
+            plan.run(use_graph=False)
+            plan.close()
+        else:
+            for pa, pb, pc in panels:
+                _gemm_views(pa, pb, pc, False, variant)
     if squeeze_a:
         out = out.squeeze(-2)
     if squeeze_b:
