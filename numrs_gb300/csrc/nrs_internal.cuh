@@ -132,6 +132,26 @@ NRS_DEV void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int32
       : "memory");
 }
 
+// Tiled TMA store (shared -> global) of one box at (x, y, z); elements
+// outside the tensor are not written. Tracked by the issuing thread's bulk
+// async-groups: commit, then wait (reads of shared memory done / complete).
+NRS_DEV void tma_store_3d(const CUtensorMap* map, const void* src, int32_t x, int32_t y, int32_t z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+NRS_DEV void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+NRS_DEV void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+template <int N>
+NRS_DEV void bulk_wait() {
+  asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+
 NRS_DEV void prefetch_tensormap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }

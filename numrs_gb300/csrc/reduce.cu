@@ -12,8 +12,9 @@
 //
 //  * fold_cols_tma : lanes are adjacent in memory (stride 1), the axis is
 //                    strided -- e.g. axis 0 of a row-major matrix, or axis 1
-//                    of its transposed view. Tile = 256 B of lanes x 32 rows;
-//                    thread t folds column t of every tile.
+//                    of its transposed view. Tile = 64 lanes x
+//                    (8 KB / (64 * sizeof(T))) rows; thread t folds column t
+//                    of every tile.
 //  * fold_rows_tma : each lane is contiguous along the axis -- axis 1 of a
 //                    row-major matrix, axis 0 of its transposed view. Tile =
 //                    128 B along the axis x 64 lanes with the 128-byte

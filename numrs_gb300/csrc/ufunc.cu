@@ -89,59 +89,122 @@ __device__ __forceinline__ T binop(int code, T a, T b) {
 }
 
 // ---------------------------------------------------------------------------
-// Evaluators. Everything stays in registers: inputs and the value stack are
-// fixed-size arrays read and written only at compile-time indices (a select
-// loop over the slots instead of a dynamic index, which would spill them to
-// local memory).
+// Evaluators. An evaluator maps W elements of every input to W results:
+// run<W>(in[kMaxIn][W], res[W]). Everything stays in registers. The program
+// is the same for every thread, so its op codes, input numbers and stack
+// depth are warp-uniform: each step is decoded once per W elements and
+// dispatched with a uniform switch whose cases touch the register arrays at
+// compile-time indices only (a dynamic index would move them to local
+// memory, a per-element select chain would cost ~8 instructions per slot).
+// The top of the stack lives in `acc`; slots below it in `st`.
 // ---------------------------------------------------------------------------
 constexpr int kMaxIn = 4;  // inputs the register evaluators handle
 
-template <typename T, int N>
-__device__ __forceinline__ T sel(const T (&r)[N], int i) {
-  T v = r[0];
-#pragma unroll
-  for (int q = 1; q < N; ++q)
-    if (q == i) v = r[q];
-  return v;
+#define NRS_SLOT_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6)
+static_assert(kStack - 1 == 7, "NRS_SLOT_CASES lists the kStack - 1 slots below the top");
+
+// st has SL slots (the program's depth - 1, rounded up to 1, 3 or 7).
+template <typename T, int SL, int W>
+__device__ __forceinline__ void slot_store(T (&st)[SL][W], int slot, const T (&v)[W]) {
+  switch (slot) {
+#define NRS_STORE(S)                                                            \
+  case S:                                                                       \
+    if constexpr (S < SL) {                                                     \
+      _Pragma("unroll") for (int e = 0; e < W; ++e) st[S < SL ? S : 0][e] = v[e]; \
+    }                                                                           \
+    break;
+    NRS_SLOT_CASES(NRS_STORE)
+#undef NRS_STORE
+  }
 }
-template <typename T, int N>
-__device__ __forceinline__ void put(T (&r)[N], int i, T v) {
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-    if (q == i) r[q] = v;
+template <typename T, int SL, int W>
+__device__ __forceinline__ void slot_load(const T (&st)[SL][W], int slot, T (&v)[W]) {
+  switch (slot) {
+#define NRS_LOAD(S)                                                             \
+  case S:                                                                       \
+    if constexpr (S < SL) {                                                     \
+      _Pragma("unroll") for (int e = 0; e < W; ++e) v[e] = st[S < SL ? S : 0][e]; \
+    }                                                                           \
+    break;
+    NRS_SLOT_CASES(NRS_LOAD)
+#undef NRS_LOAD
+  }
+}
+template <typename T, int W>
+__device__ __forceinline__ void input_load(const T (&in)[kMaxIn][W], int k, T (&v)[W]) {
+  switch (k) {
+#define NRS_IN(S) \
+  case S:         \
+    _Pragma("unroll") for (int e = 0; e < W; ++e) v[e] = in[S][e]; break;
+    NRS_IN(0) NRS_IN(1) NRS_IN(2) NRS_IN(3)
+#undef NRS_IN
+  }
+}
+template <typename T, int W>
+__device__ __forceinline__ void unary_vec(int code, T (&acc)[W]) {
+  switch (code) {
+#define NRS_UN(C) \
+  case C:         \
+    _Pragma("unroll") for (int e = 0; e < W; ++e) acc[e] = unary<T>(C, acc[e]); break;
+    NRS_UN(NRS_OP_NEG) NRS_UN(NRS_OP_ABS) NRS_UN(NRS_OP_SQRT) NRS_UN(NRS_OP_EXP) NRS_UN(NRS_OP_LN)
+#undef NRS_UN
+  }
+}
+// acc = lhs (op) acc
+template <typename T, int W>
+__device__ __forceinline__ void binary_vec(int code, const T (&lhs)[W], T (&acc)[W]) {
+  switch (code) {
+#define NRS_BIN(C) \
+  case C:          \
+    _Pragma("unroll") for (int e = 0; e < W; ++e) acc[e] = binop<T>(C, lhs[e], acc[e]); break;
+    NRS_BIN(NRS_OP_ADD) NRS_BIN(NRS_OP_SUB) NRS_BIN(NRS_OP_MUL) NRS_BIN(NRS_OP_DIV)
+    NRS_BIN(NRS_OP_MAX) NRS_BIN(NRS_OP_MIN)
+#undef NRS_BIN
+  }
 }
 
-// The general program, interpreted per element.
-template <typename T>
+// The general program (validated on the host: depth 1..D, inputs
+// < n_inputs, ends with one value). D (2, 4 or 8) bounds the stack the
+// program reaches, so a shallow program holds only D - 1 slots in registers.
+template <typename T, int D>
 struct ProgEval {
   Prog prog;
-  __device__ __forceinline__ T operator()(const T (&in)[kMaxIn]) const {
-    T st[kStack];
-#pragma unroll
-    for (int q = 0; q < kStack; ++q) st[q] = T(0);
-    int sp = 0;
+  template <int W>
+  __device__ __forceinline__ void run(const T (&in)[kMaxIn][W], T (&res)[W]) const {
+    T acc[W], lhs[W], st[D - 1][W];
+    int depth = 0;  // values on the stack, acc included
     for (int pc = 0; pc < prog.len; ++pc) {
       const int code = prog.code[pc];
-      if (code == NRS_OP_INPUT) {
-        put(st, sp++, sel(in, prog.arg[pc]));
-      } else if (code == NRS_OP_SCALAR) {
-        put(st, sp++, (T)prog.scalar[pc]);
+      if (code == NRS_OP_INPUT || code == NRS_OP_SCALAR) {
+        if (depth > 0) slot_store(st, depth - 1, acc);
+        ++depth;
+        if (code == NRS_OP_INPUT) {
+          input_load(in, prog.arg[pc], acc);
+        } else {
+          const T s = (T)prog.scalar[pc];
+#pragma unroll
+          for (int e = 0; e < W; ++e) acc[e] = s;
+        }
       } else if (code >= NRS_OP_NEG && code <= NRS_OP_LN) {
-        put(st, sp - 1, unary<T>(code, sel(st, sp - 1)));
+        unary_vec(code, acc);
       } else {
-        const T b = sel(st, --sp);
-        put(st, sp - 1, binop<T>(code, sel(st, sp - 1), b));
+        --depth;
+        slot_load(st, depth - 1, lhs);
+        binary_vec(code, lhs, acc);
       }
     }
-    return st[0];
+#pragma unroll
+    for (int e = 0; e < W; ++e) res[e] = acc[e];
   }
 };
 
 // `inputs[0] op inputs[1]`: the operators and binary closures.
 template <typename T, int OP>
 struct BinEval {
-  __device__ __forceinline__ T operator()(const T (&in)[kMaxIn]) const {
-    return binop<T>(OP, in[0], in[1]);
+  template <int W>
+  __device__ __forceinline__ void run(const T (&in)[kMaxIn][W], T (&res)[W]) const {
+#pragma unroll
+    for (int e = 0; e < W; ++e) res[e] = binop<T>(OP, in[0][e], in[1][e]);
   }
 };
 
@@ -161,11 +224,12 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int k = 0; k < kMaxIn; ++k) off[k] += c * g.in_stride[k][d];
     }
-    T v[kMaxIn];
+    T v[kMaxIn][1], r[1];
 #pragma unroll
     for (int k = 0; k < kMaxIn; ++k)
-      v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k]] : T(0);
-    out[ooff] = ev(v);
+      v[k][0] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k]] : T(0);
+    ev.template run<1>(v, r);
+    out[ooff] = r[0];
   }
 }
 
@@ -189,11 +253,60 @@ __global__ void __launch_bounds__(256)
       for (int k = 0; k < kMaxIn; ++k) off[k] += c * g.in_stride[k][d];
     }
     for (int64_t j = threadIdx.x; j < inner; j += blockDim.x) {
-      T v[kMaxIn];
+      T v[kMaxIn][1], res[1];
 #pragma unroll
       for (int k = 0; k < kMaxIn; ++k)
-        v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k] + j * g.in_stride[k][last]] : T(0);
-      out[ooff + j * g.out_stride[last]] = ev(v);
+        v[k][0] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[off[k] + j * g.in_stride[k][last]] : T(0);
+      ev.template run<1>(v, res);
+      out[ooff + j * g.out_stride[last]] = res[0];
+    }
+  }
+}
+
+// Broadcast rows with 16-byte vectors: the last dimension has stride 1 in
+// the output and stride 1 or 0 in every input (a broadcast row or column),
+// every row starts 16-byte aligned and the row length is a multiple of the
+// vector width (the host checks all three). A stride-0 input is one value
+// per row, loaded once.
+template <typename T, typename Eval>
+__global__ void __launch_bounds__(256)
+    ufunc_rows_vec(Eval ev, Geometry g, int64_t rows, T* __restrict__ out) {
+  using V = typename std::conditional<sizeof(T) == 4, int4, longlong2>::type;
+  constexpr int PER = 16 / sizeof(T);
+  const int last = g.ndim - 1;
+  const int64_t nv = g.shape[last] / PER;
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t off[kMaxIn] = {0, 0, 0, 0};
+    int64_t ooff = 0;
+    int64_t rem = r;
+    for (int d = last - 1; d >= 0; --d) {
+      const int64_t c = rem % g.shape[d];
+      rem /= g.shape[d];
+      ooff += c * g.out_stride[d];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k) off[k] += c * g.in_stride[k][d];
+    }
+    T bcast[kMaxIn];
+#pragma unroll
+    for (int k = 0; k < kMaxIn; ++k)
+      bcast[k] = (k < g.n_inputs && g.in_stride[k][last] == 0) ? static_cast<const T*>(g.in[k])[off[k]] : T(0);
+    for (int64_t j = threadIdx.x; j < nv; j += blockDim.x) {
+      T x[kMaxIn][PER];
+#pragma unroll
+      for (int k = 0; k < kMaxIn; ++k) {
+        if (k < g.n_inputs && g.in_stride[k][last] != 0) {
+          const V q = __ldcs(reinterpret_cast<const V*>(static_cast<const T*>(g.in[k]) + off[k]) + j);
+          memcpy(x[k], &q, 16);
+        } else {
+#pragma unroll
+          for (int e = 0; e < PER; ++e) x[k][e] = bcast[k];
+        }
+      }
+      T res[PER];
+      ev.template run<PER>(x, res);
+      V q;
+      memcpy(&q, res, 16);
+      __stcs(reinterpret_cast<V*>(out + ooff) + j, q);
     }
   }
 }
@@ -220,13 +333,7 @@ __global__ void __launch_bounds__(256)
       }
     }
     T res[PER];
-#pragma unroll
-    for (int e = 0; e < PER; ++e) {
-      T v[kMaxIn];
-#pragma unroll
-      for (int k = 0; k < kMaxIn; ++k) v[k] = x[k][e];
-      res[e] = ev(v);
-    }
+    ev.template run<PER>(x, res);
     V q;
     memcpy(&q, res, 16);
     __stcs(reinterpret_cast<V*>(out) + i, q);
@@ -234,10 +341,11 @@ __global__ void __launch_bounds__(256)
   // scalar tail (< PER elements)
   const int64_t t = nv * PER + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < n) {
-    T v[kMaxIn];
+    T v[kMaxIn][1], r[1];
 #pragma unroll
-    for (int k = 0; k < kMaxIn; ++k) v[k] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[t] : T(0);
-    out[t] = ev(v);
+    for (int k = 0; k < kMaxIn; ++k) v[k][0] = k < g.n_inputs ? static_cast<const T*>(g.in[k])[t] : T(0);
+    ev.template run<1>(v, r);
+    out[t] = r[0];
   }
 }
 
@@ -345,16 +453,25 @@ int launch_exp_affine(nrs_handle* h, int64_t n, const T* x, T a, T b, T* y) {
   return nrs_after_launch(h, "exp_affine");
 }
 
-// Picks the access pattern: flat vectors, row walks, or a full decode.
+enum class Access { kFlat, kRowsVec, kStrided };
+
+// Picks the access pattern: flat vectors, vector row walks, scalar row walks,
+// or a full decode.
 template <typename T, typename Eval>
-int launch_eval(nrs_handle* h, const Eval& ev, const Geometry& g, int64_t n, bool flat, void* out) {
+int launch_eval(nrs_handle* h, const Eval& ev, const Geometry& g, int64_t n, Access acc, void* out) {
   if (n == 0) return NRS_OK;
   const int cap = h->num_sms * 8;
-  if (flat) {
+  if (acc == Access::kFlat) {
     const int64_t need = (n / (16 / (int64_t)sizeof(T)) + 255) / 256 + 1;
     const int grid = (int)(need < cap ? need : cap);
     ufunc_flat_vec<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, n, (T*)out);
     return nrs_after_launch(h, "ufunc_flat_vec");
+  }
+  if (acc == Access::kRowsVec) {
+    const int64_t rows = n / g.shape[g.ndim - 1];
+    const int grid = (int)(rows < (int64_t)h->num_sms * 16 ? rows : (int64_t)h->num_sms * 16);
+    ufunc_rows_vec<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, rows, (T*)out);
+    return nrs_after_launch(h, "ufunc_rows_vec");
   }
   if (g.ndim >= 1 && g.shape[g.ndim - 1] >= 256) {
     const int64_t rows = n / g.shape[g.ndim - 1];
@@ -370,7 +487,8 @@ int launch_eval(nrs_handle* h, const Eval& ev, const Geometry& g, int64_t n, boo
 
 // Dispatch on the program's shape: a lone binary op gets its own functor.
 template <typename T>
-int launch_program(nrs_handle* h, const Prog& p, const Geometry& g, int64_t n, bool flat, void* out) {
+int launch_program(nrs_handle* h, const Prog& p, int depth, const Geometry& g, int64_t n, Access flat,
+                   void* out) {
   if (g.n_inputs > kMaxIn) {
     const int64_t need = (n + 255) / 256;
     const int grid = (int)(need < (int64_t)h->num_sms * 16 ? need : (int64_t)h->num_sms * 16);
@@ -387,7 +505,9 @@ int launch_program(nrs_handle* h, const Prog& p, const Geometry& g, int64_t n, b
       default: break;
     }
   }
-  return launch_eval<T>(h, ProgEval<T>{p}, g, n, flat, out);
+  if (depth <= 2) return launch_eval<T>(h, ProgEval<T, 2>{p}, g, n, flat, out);
+  if (depth <= 4) return launch_eval<T>(h, ProgEval<T, 4>{p}, g, n, flat, out);
+  return launch_eval<T>(h, ProgEval<T, kStack>{p}, g, n, flat, out);
 }
 
 }  // namespace
@@ -422,7 +542,7 @@ extern "C" int nrs_ufunc(nrs_handle* h, int dtype, const nrs_ufunc_op* prog, int
   // Validate the program: stack discipline, input indices, dtype support.
   Prog p{};
   p.len = prog_len;
-  int depth = 0;
+  int depth = 0, max_depth = 0;
   for (int i = 0; i < prog_len; ++i) {
     const int c = prog[i].code;
     p.code[i] = c;
@@ -444,6 +564,7 @@ extern "C" int nrs_ufunc(nrs_handle* h, int dtype, const nrs_ufunc_op* prog, int
       return nrs_fail(h, NRS_ERR_INVALID, "unknown op code");
     }
     if (depth > kStack) return nrs_fail(h, NRS_ERR_INVALID, "stack deeper than 8");
+    if (depth > max_depth) max_depth = depth;
   }
   if (depth != 1) return nrs_fail(h, NRS_ERR_INVALID, "program must leave exactly one value");
   int64_t n = 1;
@@ -487,16 +608,30 @@ extern "C" int nrs_ufunc(nrs_handle* h, int dtype, const nrs_ufunc_op* prog, int
     return nrs_exp_affine(h, dtype, n, inputs[0], prog[1].scalar, prog[3].scalar, out);
   }
   // Same-shape contiguous operands, all 16-byte aligned: flat vector path.
-  bool flat = false;
-  if (all_contig) {
-    uintptr_t align = reinterpret_cast<uintptr_t>(out);
-    for (int k = 0; k < n_inputs; ++k) align |= reinterpret_cast<uintptr_t>(inputs[k]);
-    flat = (align & 15) == 0;
+  // Otherwise rows of 16-byte vectors when the last dimension is unit-stride
+  // (or broadcast) everywhere and every row starts 16-byte aligned.
+  Access flat = Access::kStrided;
+  uintptr_t align = reinterpret_cast<uintptr_t>(out);
+  for (int k = 0; k < n_inputs; ++k) align |= reinterpret_cast<uintptr_t>(inputs[k]);
+  if (all_contig && (align & 15) == 0) {
+    flat = Access::kFlat;
+  } else if (ndim >= 1 && (align & 15) == 0 && g.shape[ndim - 1] >= 64 &&
+             (g.shape[ndim - 1] * (int64_t)es) % 16 == 0 && g.out_stride[ndim - 1] == 1) {
+    bool ok = true;
+    for (int d = 0; d < ndim - 1; ++d)
+      if (g.shape[d] > 1 && (g.out_stride[d] * (int64_t)es) % 16 != 0) ok = false;
+    for (int k = 0; k < n_inputs && ok; ++k) {
+      const int64_t ls = g.in_stride[k][ndim - 1];
+      if (ls > 1) ok = false;
+      for (int d = 0; d < ndim - 1 && ok; ++d)
+        if (ls == 1 && g.shape[d] > 1 && (g.in_stride[k][d] * (int64_t)es) % 16 != 0) ok = false;
+    }
+    if (ok) flat = Access::kRowsVec;
   }
   switch (dtype) {
-    case NRS_F32: return launch_program<float>(h, p, g, n, flat, out);
-    case NRS_F64: return launch_program<double>(h, p, g, n, flat, out);
-    case NRS_I64: return launch_program<int64_t>(h, p, g, n, flat, out);
-    default: return launch_program<int32_t>(h, p, g, n, flat, out);
+    case NRS_F32: return launch_program<float>(h, p, max_depth, g, n, flat, out);
+    case NRS_F64: return launch_program<double>(h, p, max_depth, g, n, flat, out);
+    case NRS_I64: return launch_program<int64_t>(h, p, max_depth, g, n, flat, out);
+    default: return launch_program<int32_t>(h, p, max_depth, g, n, flat, out);
   }
 }

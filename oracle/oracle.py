@@ -192,6 +192,54 @@ class Oracle:
         self.L.orc_exp_affine_eager_f32(_p(x), x.size, a, b, _p(tmp), _p(y))
         return y
 
+    def program(self, prog, inputs):
+        """Postfix ufunc program over broadcast numpy inputs, one IEEE
+        rounding per op (numpy's elementwise float ops never contract), as
+        ExprNode's eager evaluation does (src/expr/owned.rs:557; two
+        roundings for a*b+c, src/expr/fused_eval.rs:17-21). Codes follow
+        nrs_ufunc: INPUT 0, SCALAR 1, ADD 2, SUB 3, MUL 4, DIV 5, NEG 6,
+        ABS 7, SQRT 8, EXP 9, LN 10, MAX 11, MIN 12. MAX/MIN keep the left
+        operand if it is NaN or strictly greater (smaller). Integer division
+        truncates toward zero and gives 0 for a zero divisor or MIN / -1."""
+        dt = inputs[0].dtype
+        shape = np.broadcast_shapes(*[x.shape for x in inputs])
+        ins = [np.broadcast_to(x, shape) for x in inputs]
+        st = []
+        with np.errstate(all="ignore"):
+            for code, arg, scal in prog:
+                if code == 0:
+                    st.append(np.array(ins[arg], dtype=dt))
+                elif code == 1:
+                    st.append(np.full(shape, scal, dtype=dt))
+                elif code in (6, 7, 8, 9, 10):
+                    v = st.pop()
+                    f = {6: np.negative, 7: np.abs, 8: np.sqrt, 9: np.exp, 10: np.log}[code]
+                    st.append(f(v).astype(dt))
+                else:
+                    b = st.pop()
+                    a = st.pop()
+                    if code == 2:
+                        r = a + b
+                    elif code == 3:
+                        r = a - b
+                    elif code == 4:
+                        r = a * b
+                    elif code == 5 and dt.kind == "f":
+                        r = a / b
+                    elif code == 5:
+                        bad = (b == 0) | ((b == -1) & (a == np.iinfo(dt).min))
+                        bs = np.where(bad, 1, b)
+                        # C division: the remainder takes the dividend's sign,
+                        # so (a - rem) / b is exact and truncates toward zero.
+                        r = np.where(bad, 0, (a - np.fmod(a, bs)) // bs)
+                    elif code == 11:
+                        r = np.where((a != a) | (a > b), a, b)
+                    else:
+                        r = np.where((a != a) | (a < b), a, b)
+                    st.append(np.asarray(r).astype(dt))
+        assert len(st) == 1
+        return st[0]
+
     def binary(self, op: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:
         shape = np.broadcast_shapes(a.shape, b.shape)
         ab = np.broadcast_to(a, shape)

@@ -168,3 +168,20 @@ def test_axis_var_ddof(ora):
     x = np.arange(12, dtype=np.float64).reshape(3, 4)
     np.testing.assert_allclose(ora.axis_var(x, 0, ddof=1), np.var(x, axis=0, ddof=1), rtol=1e-15)
     np.testing.assert_allclose(ora.axis_var(x, 1, ddof=0, std=True), np.std(x, axis=1), rtol=1e-15)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int64])
+def test_program_evaluator_matches_binary(ora, dtype):
+    """The oracle's postfix-program evaluator agrees with its C binary ops
+    (broadcast row, negative integers, zero divisors)."""
+    r = np.random.default_rng(11)
+    if dtype == np.int64:
+        a = r.integers(-1000, 1000, (40, 30)).astype(dtype)
+        b = r.integers(-7, 8, (30,)).astype(dtype)
+    else:
+        a = r.standard_normal((40, 30)).astype(dtype)
+        b = r.standard_normal((30,)).astype(dtype)
+    for code, op in ((2, O.ADD), (3, O.SUB), (4, O.MUL), (5, O.DIV)):
+        p = ora.program([(0, 0, 0.0), (0, 1, 0.0), (code, 0, 0.0)], [a, b])
+        c = ora.binary(op, a, b)
+        np.testing.assert_array_equal(p.view(np.uint8), c.view(np.uint8))

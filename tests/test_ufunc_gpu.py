@@ -130,3 +130,87 @@ def test_arith_goldens(K, key):
         b = np.array(case["scalar"], np.float64)
     got = to_np(getattr(K, op)(_dev(a), _dev(b)))
     np.testing.assert_allclose(got.ravel(), case["result"]["data"], rtol=1e-15)
+
+
+def _random_program(r, n_inputs, n_leaves, dt_kind):
+    """A random expression tree in postfix form. Trees lean right half the
+    time so the stack reaches the number of leaves (up to 8)."""
+    ops = [2, 3, 4, 5, 11, 12]
+
+    def leaf():
+        if r.random() < 0.2:
+            s = float(r.integers(-5, 6)) if dt_kind != "f" else float(r.standard_normal())
+            return [(1, 0, s)]
+        return [(0, int(r.integers(0, n_inputs)), 0.0)]
+
+    def tree(nl, right_deep):
+        if nl == 1:
+            t = leaf()
+        else:
+            k = 1 if right_deep else int(r.integers(1, nl))
+            t = tree(k, right_deep) + tree(nl - k, right_deep) + [(int(r.choice(ops)), 0, 0.0)]
+        if r.random() < 0.15:
+            t = t + [(int(r.choice([6, 7])), 0, 0.0)]
+        return t
+
+    return tree(n_leaves, bool(r.random() < 0.5))
+
+
+def _depth(prog):
+    d = m = 0
+    for code, _, _ in prog:
+        d += 1 if code in (0, 1) else (0 if code in (6, 7, 8, 9, 10) else -1)
+        m = max(m, d)
+    return m
+
+
+def _same_or_both_nan(got, ref):
+    got, ref = np.ascontiguousarray(got), np.ascontiguousarray(ref)
+    if got.dtype.kind == "f":
+        nan = np.isnan(ref)
+        np.testing.assert_array_equal(np.isnan(got), nan)
+        np.testing.assert_array_equal(bits(got[~nan]), bits(ref[~nan]))
+    else:
+        np.testing.assert_array_equal(got, ref)
+
+
+# (input shapes, view): same-shape contiguous -> flat vectors; an aligned
+# broadcast row / column -> vector rows; odd widths and transposed views ->
+# scalar rows or the full decode.
+PROGRAM_CASES = [
+    ([(300, 256)] * 4, None),
+    ([(300, 256), (256,), (300, 1), (1, 256)], None),
+    ([(64, 8, 128), (8, 1), (64, 1, 128), (128,)], None),
+    ([(37, 65), (65,), (37, 1), (37, 65)], None),
+    ([(33, 70)] * 4, "t"),
+    ([(5000,)] * 4, None),
+]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int64])
+@pytest.mark.parametrize("case", range(len(PROGRAM_CASES)))
+def test_random_programs_bit_exact(K, ora, dtype, case):
+    """Random postfix programs of stack depth 1..8 over 1..4 broadcast inputs
+    through every access path, bit-exact against the oracle's evaluation."""
+    shapes, view = PROGRAM_CASES[case]
+    r = np.random.default_rng(100 + case)
+    kind = np.dtype(dtype).kind
+    if kind == "f":
+        arrs = [r.standard_normal(s).astype(dtype) for s in shapes]
+    else:
+        arrs = [r.integers(-1000, 1000, s).astype(dtype) for s in shapes]
+    devs = [_dev(a) for a in arrs]
+    if view == "t":  # transposed views of (70, 33) buffers
+        arrs = [np.ascontiguousarray(a.T).T for a in arrs]
+        devs = [_dev(np.ascontiguousarray(a.T)).t() for a in arrs]
+    seen = set()
+    for trial in range(24):
+        n_in = int(r.integers(1, 5))
+        prog = _random_program(r, n_in, int(r.integers(1, 9)), kind)
+        if _depth(prog) > 8:
+            continue
+        seen.add(_depth(prog))
+        got = to_np(K.run_program(prog, devs[:n_in]))
+        ref = ora.program(prog, arrs[:n_in])
+        _same_or_both_nan(got, ref)
+    assert max(seen) >= 5 and min(seen) <= 2  # shallow and deep stacks both ran
