@@ -302,6 +302,29 @@ def elementwise_section(K, L):
     return out
 
 
+def scan_section(K, L):
+    """Running folds on 16384x16384 f32 N(0,1) (seed 3): cumsum along axis 0
+    (column pipeline), axis 1 (row pipeline) and over the flattened array
+    (chunked parallel scan), each one call; algorithmic bytes = read + write
+    of the array (8 B/elem)."""
+    import torch
+    n = R * C_
+    stream = torch.cuda.current_stream()
+    x = torch.empty((R, C_), device="cuda")
+    K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+    cases = {"cumsum_axis0": lambda: K.cumsum(x, 0),
+             "cumsum_axis1": lambda: K.cumsum(x, 1),
+             "cumsum_flat": lambda: K.cumsum(x),
+             "maximum_accumulate_axis1": lambda: K.ufunc_accumulate("maximum", x, 1)}
+    out = {}
+    for name, fn in cases.items():
+        ms = _time_ms(fn, 5, stream)
+        out[name] = {"ms": round(ms, 4), "gbs": round(8 * n / ms / 1e6, 1)}
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 def grouped_section(K, L, seed: int = 7):
     """4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64) and
     4096 row reductions (length log-uniform in [64, 65536]) in one persistent
@@ -382,6 +405,7 @@ def main():
     ap.add_argument("--quick-gemm", action="store_true", help="2048^3 instead of 8192^3")
     ap.add_argument("--no-grouped", action="store_true")
     ap.add_argument("--no-elementwise", action="store_true")
+    ap.add_argument("--no-scan", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -558,6 +582,8 @@ def main():
         out["gemm"] = gemm_section(K, L, quick=args.quick_gemm)
     if rank == 0 and not args.no_elementwise:
         out["elementwise"] = elementwise_section(K, L)
+    if rank == 0 and not args.no_scan:
+        out["scan"] = scan_section(K, L)
     if rank == 0 and not args.no_grouped:
         out["grouped"] = grouped_section(K, L)
     if rank == 0:

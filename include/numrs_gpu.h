@@ -212,6 +212,55 @@ int nrs_exp_affine(nrs_handle* h, int dtype, int64_t n, const void* x, double a,
                    void* y);
 
 /* ---------------------------------------------------------------------- */
+/* Ufunc reduce / accumulate                                                */
+/* ---------------------------------------------------------------------- */
+/* `op` is one of the binary op codes of nrs_ufunc_op: NRS_OP_ADD, _SUB,
+ * _MUL, _DIV, _MAX, _MIN (UfuncOp::{Add, Subtract, Multiply, Divide,
+ * Maximum, Minimum}, src/ufunc_ops.rs:106). The op is UfuncOp::apply
+ * (:153-181): one rounding; maximum/minimum give NaN if either side is NaN,
+ * else the left operand only if strictly greater (smaller). Integer dtypes
+ * wrap; integer DIV returns NRS_ERR_DTYPE. */
+
+/* op.reduce(x, axis, initial): replaces ufunc_ops::ufunc_reduce
+ * (src/ufunc_ops.rs:417). `initial` points to one host value of `dtype`, or
+ * is NULL for none.
+ * axis == NRS_AXIS_NONE (reduce_full, :265): add / multiply are
+ *   initial-or-0 + the flat sum and initial-or-1 * the flat product (the
+ *   tiered flat kernels of nrs_reduce); maximum / minimum / subtract /
+ *   divide fold the flattened array from `initial` or from its first
+ *   element. out = 1 element.
+ * axis given (reduce_along_axis, :317): every lane folds left to right from
+ *   `initial` or from its first element (reduce_lane, :230); out = the kept
+ *   dimensions in row-major order. Negative axes count from the end.
+ * Empty input or empty lanes without `initial`: add gives 0, multiply 1,
+ * the rest NRS_ERR_EMPTY ("zero-size array to reduction operation maximum
+ * which has no identity"). */
+int nrs_ufunc_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+                     const int64_t* strides, int64_t axis, const void* initial, const void* x,
+                     void* out);
+
+/* op.accumulate(x, axis): replaces ufunc_ops::ufunc_accumulate
+ * (src/ufunc_ops.rs:523) and math::cumsum / cumprod
+ * (src/math/statistics/mod.rs:584, :795). add is cumsum (every lane, or the
+ * flattened array, a running sum from 0), multiply is cumprod (from 1), the
+ * other ops start from the first element (accumulate_flat :452,
+ * accumulate_along_axis :470).
+ * axis given: out has x's shape; out_strides (NULL = row-major contiguous)
+ *   are its element strides. Lanes are folded left to right, bit-identical
+ *   to the reference's loops.
+ * axis == NRS_AXIS_NONE: out is the prod(shape) values of the flattened array
+ *   in logical order, contiguous (out_strides ignored). Maximum / minimum and
+ *   integer add / multiply are exact; f32/f64 add / multiply of 64 or more
+ *   elements reassociate the running sum / product (a chunked parallel
+ *   scan), like the reference's f32/f64 cumsum at that size (scirs2-core's
+ *   simd_cumsum); subtract / divide (and float add / multiply below 64
+ *   elements) run the strict left-to-right chain.
+ * Empty input: nothing is written. */
+int nrs_accumulate(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+                   const int64_t* strides, int64_t axis, const void* x, void* out,
+                   const int64_t* out_strides);
+
+/* ---------------------------------------------------------------------- */
 /* GEMM                                                                     */
 /* ---------------------------------------------------------------------- */
 #define NRS_GEMM_ACCUMULATE 1u /* C += A*B (Array::matmul_to, src/array/operations_optimized.rs:385) */

@@ -75,6 +75,8 @@ SIGNATURES = {
     "nrs_reduce_flat_noalloc": (_i, [_vp, _i, _i, _i64, _vp, _vp]),
     "nrs_ufunc": (_i, [_vp, _i, C.POINTER(UfuncOp), _i, _i, _P64, _i, C.POINTER(_vp), _P64, _vp, _P64]),
     "nrs_exp_affine": (_i, [_vp, _i, _i64, _vp, _d, _d, _vp]),
+    "nrs_ufunc_reduce": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _vp]),
+    "nrs_accumulate": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _P64]),
     "nrs_gemm": (_i, [_vp, _i, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u, _i]),
     "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i,
                             C.POINTER(OzakiInfo)]),

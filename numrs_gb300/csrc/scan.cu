@@ -1,0 +1,990 @@
+// Seeded and running folds: ufunc reduce with `initial`, ufunc accumulate,
+// cumsum and cumprod.
+//
+//   ufunc_ops::ufunc_reduce      src/ufunc_ops.rs:417 (reduce_full :265,
+//                                reduce_along_axis :317, reduce_lane :230)
+//   ufunc_ops::ufunc_accumulate  src/ufunc_ops.rs:523 (accumulate_flat :452,
+//                                accumulate_along_axis :470)
+//   math::cumsum / cumprod       src/math/statistics/mod.rs:584, :795
+//
+// Along an axis every lane is one sequential chain, exactly the reference's
+// left-to-right fold, so results are bit-identical; lanes run in parallel
+// through the same TMA pipelines as the axis reductions. A running fold
+// (accumulate) rewrites each staged tile in shared memory with its prefix
+// values and stores it back with a TMA store: HBM traffic is one read and one
+// write of the array.
+//
+// Over the flattened array (axis = None) the order-free cases use a
+// reduce-then-scan over 8192-element chunks whose combine always keeps the
+// earlier operand on the left. maximum/minimum are associative under the
+// reference's apply (NaN absorbs, ties take the right operand), so the
+// parallel scan is exact; integer add/multiply wrap and are exact in any
+// order; float add/multiply reassociate (tolerance-based, as the flat
+// product is). subtract/divide are inherently serial and run as one lane.
+#include <limits>
+#include <string>
+#include <type_traits>
+
+#include "nrs_internal.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// UfuncOp::apply (src/ufunc_ops.rs:153-181)
+// ---------------------------------------------------------------------------
+template <typename T> NRS_DEV T qnan();
+template <> NRS_DEV float qnan<float>() { return __int_as_float(0x7fc00000); }
+template <> NRS_DEV double qnan<double>() { return __longlong_as_double(0x7ff8000000000000LL); }
+
+// One rounding per op; maximum/minimum: NaN (Rust's quiet-NaN bits) if
+// either side is NaN, else the left operand only if strictly greater
+// (smaller). Integers wrap; integer division is rejected on the host.
+template <typename T, int OP>
+NRS_DEV T apply(T a, T b) {
+  if constexpr (std::is_same<T, float>::value) {
+    if constexpr (OP == NRS_OP_ADD) return __fadd_rn(a, b);
+    else if constexpr (OP == NRS_OP_SUB) return __fsub_rn(a, b);
+    else if constexpr (OP == NRS_OP_MUL) return __fmul_rn(a, b);
+    else if constexpr (OP == NRS_OP_DIV) return __fdiv_rn(a, b);
+    else if constexpr (OP == NRS_OP_MAX) return (a != a || b != b) ? qnan<float>() : (a > b ? a : b);
+    else return (a != a || b != b) ? qnan<float>() : (a < b ? a : b);
+  } else if constexpr (std::is_same<T, double>::value) {
+    if constexpr (OP == NRS_OP_ADD) return __dadd_rn(a, b);
+    else if constexpr (OP == NRS_OP_SUB) return __dsub_rn(a, b);
+    else if constexpr (OP == NRS_OP_MUL) return __dmul_rn(a, b);
+    else if constexpr (OP == NRS_OP_DIV) return __ddiv_rn(a, b);
+    else if constexpr (OP == NRS_OP_MAX) return (a != a || b != b) ? qnan<double>() : (a > b ? a : b);
+    else return (a != a || b != b) ? qnan<double>() : (a < b ? a : b);
+  } else {
+    using U = typename std::make_unsigned<T>::type;
+    if constexpr (OP == NRS_OP_ADD) return (T)((U)a + (U)b);
+    else if constexpr (OP == NRS_OP_SUB) return (T)((U)a - (U)b);
+    else if constexpr (OP == NRS_OP_MUL) return (T)((U)a * (U)b);
+    else if constexpr (OP == NRS_OP_MAX) return a > b ? a : b;
+    else if constexpr (OP == NRS_OP_MIN) return a < b ? a : b;
+    else return b == 0 ? T(0) : a / b;
+  }
+}
+
+// A value e with apply(e, x) == x and apply(x, e) == x bit for bit, for the
+// order-free ops: -0.0 for float add (-0 + -0 = -0, -0 + +0 = +0), 1 for
+// multiply, -inf / +inf (integer extremes) for maximum / minimum.
+template <typename T, int OP>
+NRS_DEV T identity() {
+  if constexpr (OP == NRS_OP_ADD) {
+    if constexpr (std::is_floating_point<T>::value) return -T(0);
+    else return T(0);
+  } else if constexpr (OP == NRS_OP_MUL) {
+    return T(1);
+  } else if constexpr (OP == NRS_OP_MAX) {
+    if constexpr (std::is_floating_point<T>::value) return -INFINITY;
+    else return std::numeric_limits<T>::lowest();
+  } else {
+    if constexpr (std::is_floating_point<T>::value) return INFINITY;
+    else return std::numeric_limits<T>::max();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Lanes
+// ---------------------------------------------------------------------------
+constexpr int kMaxDims = NRS_UFUNC_MAX_DIMS;
+
+// Kept (non-axis) dimensions, outer to inner, with the input's strides and,
+// for a running fold, the output's.
+struct Lanes {
+  int n;
+  int64_t size[kMaxDims];
+  int64_t xstride[kMaxDims];
+  int64_t ostride[kMaxDims];
+};
+
+// How a lane starts: from `seed` folding every element, or from its first
+// element (seed ignored).
+struct Seed {
+  int first;
+  double fseed;   // f32/f64 seeds
+  int64_t iseed;  // integer seeds
+  template <typename T>
+  __host__ __device__ T get() const {
+    if constexpr (std::is_floating_point<T>::value) return (T)fseed;
+    else return (T)iseed;
+  }
+};
+
+// One thread per lane, any strides. RUNNING writes every prefix to
+// out[obase + j * oastride]; otherwise the lane's result to out[o].
+template <typename T, int OP, bool RUNNING>
+__global__ void __launch_bounds__(256)
+    lane_scan_generic(const T* __restrict__ x, Lanes g, int64_t n_lanes, int64_t alen,
+                      int64_t xastride, T* __restrict__ out, int64_t oastride, Seed seed) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_lanes;
+       o += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = o, xb = 0, ob = 0;
+    for (int d = g.n - 1; d >= 0; --d) {
+      const int64_t c = rem % g.size[d];
+      rem /= g.size[d];
+      xb += c * g.xstride[d];
+      ob += c * g.ostride[d];
+    }
+    T acc = seed.get<T>();
+    int64_t j = 0;
+    if (seed.first) {
+      acc = x[xb];
+      if (RUNNING) out[ob] = acc;
+      j = 1;
+    }
+    for (; j < alen; ++j) {
+      acc = apply<T, OP>(acc, x[xb + j * xastride]);
+      if (RUNNING) out[ob + j * oastride] = acc;
+    }
+    if (!RUNNING) out[o] = acc;
+  }
+}
+
+// Lanes adjacent in memory (stride 1), axis strided: tiles of 64 lanes x
+// (8 KB / 64 / sizeof(T)) axis positions through an 8-stage TMA ring (the
+// geometry of the column reductions). Thread t owns lane l0 + t.
+//
+// RUNNING: thread t overwrites column t of the staged tile with its prefix
+// values; after a proxy fence and a CTA barrier one thread TMA-stores the
+// tile into the output (same dims and strides, positions outside the array
+// are clipped by the store) and re-arms the buffer only once that store has
+// finished reading it (bulk async-group wait), one iteration later.
+constexpr int kLanesPerCta = 64;
+constexpr int kScanStages = 8;
+constexpr int kTileBytes = 8192;
+
+template <typename T>
+constexpr int col_rows() { return kTileBytes / (kLanesPerCta * (int)sizeof(T)); }
+
+template <typename T, int OP, bool RUNNING>
+__global__ void __launch_bounds__(kLanesPerCta)
+    lane_scan_cols_tma(const __grid_constant__ CUtensorMap xmap,
+                       const __grid_constant__ CUtensorMap omap, int64_t alen, int64_t lanes,
+                       T* __restrict__ out, uint32_t* err, Seed seed) {
+  constexpr int LW = kLanesPerCta;
+  constexpr int RB = col_rows<T>();
+  constexpr int S = kScanStages;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTileBytes * S);
+  __shared__ int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * LW;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + RB - 1) / RB;
+
+  if (t == 0) {
+    prefetch_tensormap(&xmap);
+    if (RUNNING) prefetch_tensormap(&omap);
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int s = 0; s < S && s < n_tiles; ++s) {
+      mbar_arrive_expect_tx(&full[s], kTileBytes);
+      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
+    }
+  }
+  T acc = seed.get<T>();
+  int64_t it = 0;
+  for (; it < n_tiles; ++it) {
+    const int s = (int)(it % S);
+    if (!mbar_wait_bounded(&full[s], (uint32_t)((it / S) & 1), NRS_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) break;
+    T* tile = reinterpret_cast<T*>(smem + s * kTileBytes);
+    const int64_t y0 = it * RB;
+    const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
+    int r = 0;
+    if (it == 0 && seed.first) {
+      acc = tile[t];
+      r = 1;
+    }
+    for (; r < cnt; ++r) {
+      acc = apply<T, OP>(acc, tile[r * LW + t]);
+      if (RUNNING) tile[r * LW + t] = acc;
+    }
+    if (RUNNING) fence_proxy_async_smem();
+    __syncthreads();
+    if (t == 0) {
+      if (RUNNING) {
+        tma_store_3d(&omap, tile, (int32_t)l0, (int32_t)y0, batch);
+        bulk_commit();
+        const int64_t nt = it - 1 + S;  // refill the previous iteration's buffer
+        if (it >= 1 && nt < n_tiles) {
+          bulk_wait_read<1>();
+          const int ps = (int)((it - 1) % S);
+          mbar_arrive_expect_tx(&full[ps], kTileBytes);
+          tma_load_3d(smem + ps * kTileBytes, &xmap, &full[ps], (int32_t)l0, (int32_t)(nt * RB), batch);
+        }
+      } else if (it + S < n_tiles) {
+        mbar_arrive_expect_tx(&full[s], kTileBytes);
+        tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)l0, (int32_t)((it + S) * RB), batch);
+      }
+    }
+  }
+  if (abort_flag) {
+    if (t == 0) {
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (3u << 8));
+      // Loads issued and not consumed: tiles it .. it + S - 1 at most.
+      for (int64_t j = it; j < n_tiles && j < it + S; ++j)
+        mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
+      if (RUNNING) bulk_wait<0>();
+    }
+    return;
+  }
+  if (RUNNING) {
+    if (t == 0) bulk_wait<0>();
+  } else {
+    const int64_t lane = l0 + t;
+    if (lane < lanes) out[(int64_t)batch * lanes + lane] = acc;
+  }
+}
+
+// Lanes contiguous along the axis: tiles of 64 lanes x 128 bytes of axis with
+// the 128-byte swizzle (16-byte chunk j of tile row r at r*128 +
+// ((j ^ (r & 7)) * 16)); thread t owns row t. RUNNING rewrites the row in
+// place (same swizzled positions) and TMA-stores it like the column kernel.
+template <typename T, int OP, bool RUNNING>
+__global__ void __launch_bounds__(kLanesPerCta)
+    lane_scan_rows_tma(const __grid_constant__ CUtensorMap xmap,
+                       const __grid_constant__ CUtensorMap omap, int64_t alen, int64_t lanes,
+                       T* __restrict__ out, uint32_t* err, Seed seed) {
+  constexpr int XB = 128 / sizeof(T);
+  constexpr int PER16 = 16 / sizeof(T);
+  constexpr int S = kScanStages;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTileBytes * S);
+  __shared__ int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * kLanesPerCta;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + XB - 1) / XB;
+
+  if (t == 0) {
+    prefetch_tensormap(&xmap);
+    if (RUNNING) prefetch_tensormap(&omap);
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int s = 0; s < S && s < n_tiles; ++s) {
+      mbar_arrive_expect_tx(&full[s], kTileBytes);
+      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
+    }
+  }
+  T acc = seed.get<T>();
+  const int sw = t & 7;
+  int64_t it = 0;
+  for (; it < n_tiles; ++it) {
+    const int s = (int)(it % S);
+    if (!mbar_wait_bounded(&full[s], (uint32_t)((it / S) & 1), NRS_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) break;
+    uint8_t* row = smem + s * kTileBytes + t * 128;
+    const int64_t x0 = it * XB;
+    const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
+    T v[XB];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], row + ((j ^ sw) << 4), 16);
+    int e0 = 0;
+    if (it == 0 && seed.first) {
+      acc = v[0];
+      e0 = 1;
+    }
+    if (cnt == XB) {
+#pragma unroll
+      for (int e = 0; e < XB; ++e) {
+        if (e >= e0) {
+          acc = apply<T, OP>(acc, v[e]);
+          v[e] = acc;
+        }
+      }
+    } else {
+      for (int e = e0; e < cnt; ++e) {
+        acc = apply<T, OP>(acc, v[e]);
+        v[e] = acc;
+      }
+    }
+    if (RUNNING) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) memcpy(row + ((j ^ sw) << 4), &v[j * PER16], 16);
+      fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (t == 0) {
+      if (RUNNING) {
+        tma_store_3d(&omap, smem + s * kTileBytes, (int32_t)x0, (int32_t)l0, batch);
+        bulk_commit();
+        const int64_t nt = it - 1 + S;
+        if (it >= 1 && nt < n_tiles) {
+          bulk_wait_read<1>();
+          const int ps = (int)((it - 1) % S);
+          mbar_arrive_expect_tx(&full[ps], kTileBytes);
+          tma_load_3d(smem + ps * kTileBytes, &xmap, &full[ps], (int32_t)(nt * XB), (int32_t)l0, batch);
+        }
+      } else if (it + S < n_tiles) {
+        mbar_arrive_expect_tx(&full[s], kTileBytes);
+        tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)((it + S) * XB), (int32_t)l0, batch);
+      }
+    }
+  }
+  if (abort_flag) {
+    if (t == 0) {
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (4u << 8));
+      for (int64_t j = it; j < n_tiles && j < it + S; ++j)
+        mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
+      if (RUNNING) bulk_wait<0>();
+    }
+    return;
+  }
+  if (RUNNING) {
+    if (t == 0) bulk_wait<0>();
+  } else {
+    const int64_t lane = l0 + t;
+    if (lane < lanes) out[(int64_t)batch * lanes + lane] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Flat scans (order-free ops)
+// ---------------------------------------------------------------------------
+// A block takes one chunk; warp w takes its sub-chunk as R rounds of 32
+// consecutive elements (coalesced), held in registers: R = 32 for 4-byte
+// types (8192-element chunks), 16 for 8-byte ones (4096). Every combine
+// keeps the earlier operand on the left.
+constexpr int kScanWarps = 8;
+template <typename T>
+constexpr int rounds_of() { return sizeof(T) == 4 ? 32 : 16; }
+template <typename T>
+constexpr int64_t flat_chunk() { return 32 * rounds_of<T>() * kScanWarps; }
+
+template <typename T, int OP>
+NRS_DEV T warp_inclusive(T v, int lane) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const T o = __shfl_up_sync(0xffffffffu, v, off);
+    if (lane >= off) v = apply<T, OP>(o, v);
+  }
+  return v;
+}
+
+// Loads the warp's rounds (identity past n), scans each round in place, and
+// returns the warp total (the rounds' totals folded in order).
+template <typename T, int OP>
+NRS_DEV T warp_rounds(const T* __restrict__ x, int64_t wbase, int64_t n, int lane,
+                      T (&v)[rounds_of<T>()]) {
+  constexpr int kRounds = rounds_of<T>();
+#pragma unroll
+  for (int k = 0; k < kRounds; ++k) {
+    const int64_t i = wbase + k * 32 + lane;
+    v[k] = i < n ? x[i] : identity<T, OP>();
+  }
+#pragma unroll
+  for (int k = 0; k < kRounds; ++k) v[k] = warp_inclusive<T, OP>(v[k], lane);
+  T run = identity<T, OP>();
+#pragma unroll
+  for (int k = 0; k < kRounds; ++k) run = apply<T, OP>(run, __shfl_sync(0xffffffffu, v[k], 31));
+  return run;
+}
+
+// Phase 1: the ordered total of every chunk.
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    flat_chunk_totals(const T* __restrict__ x, int64_t n, T* __restrict__ totals) {
+  constexpr int kRounds = rounds_of<T>();
+  constexpr int64_t kChunk = flat_chunk<T>();
+  __shared__ T wt[kScanWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    T v[kRounds];
+    const T tot = warp_rounds<T, OP>(x, c * kChunk + (int64_t)w * 32 * kRounds, n, lane, v);
+    if (lane == 0) wt[w] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T r = wt[0];
+      for (int i = 1; i < kScanWarps; ++i) r = apply<T, OP>(r, wt[i]);
+      totals[c] = r;
+    }
+    __syncthreads();
+  }
+}
+
+// Phase 2 (one block of 1024): carries[c] = seed (op) totals[0] (op) ...
+// (op) totals[c - 1] in order (identity in place of an absent seed); with
+// `final_out` set, writes seed (op) all totals there instead.
+template <typename T, int OP>
+__global__ void __launch_bounds__(1024)
+    flat_chunk_carries(const T* __restrict__ totals, int64_t nchunks, int has_seed, Seed seed,
+                       T* __restrict__ carries, T* __restrict__ final_out) {
+  __shared__ T runs[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (nchunks + 1023) / 1024;
+  const int64_t lo = t * per, hi = (lo + per < nchunks) ? lo + per : nchunks;
+  T r = identity<T, OP>();
+  for (int64_t i = lo; i < hi; ++i) r = apply<T, OP>(r, totals[i]);
+  runs[t] = r;
+  __syncthreads();
+  if (t == 0) {
+    T c = has_seed ? seed.get<T>() : identity<T, OP>();
+    for (int i = 0; i < 1024; ++i) {
+      const T ri = runs[i];
+      runs[i] = c;  // exclusive prefix of run i
+      c = apply<T, OP>(c, ri);
+    }
+    if (final_out) *final_out = c;
+  }
+  __syncthreads();
+  if (final_out) return;
+  T c = runs[t];
+  for (int64_t i = lo; i < hi; ++i) {
+    carries[i] = c;
+    c = apply<T, OP>(c, totals[i]);
+  }
+}
+
+// Phase 3: every element's prefix: the warp's carry, then the earlier
+// rounds' totals, then the element's own round prefix.
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    flat_chunk_scan(const T* __restrict__ x, int64_t n, const T* __restrict__ carries,
+                    T* __restrict__ out) {
+  constexpr int kRounds = rounds_of<T>();
+  constexpr int64_t kChunk = flat_chunk<T>();
+  __shared__ T wt[kScanWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const int64_t wbase = c * kChunk + (int64_t)w * 32 * kRounds;
+    T v[kRounds];
+    const T tot = warp_rounds<T, OP>(x, wbase, n, lane, v);
+    if (lane == 0) wt[w] = tot;
+    __syncthreads();
+    T run = carries[c];
+    for (int i = 0; i < w; ++i) run = apply<T, OP>(run, wt[i]);
+#pragma unroll
+    for (int k = 0; k < kRounds; ++k) {
+      const int64_t i = wbase + k * 32 + lane;
+      if (i < n) out[i] = apply<T, OP>(run, v[k]);
+      run = apply<T, OP>(run, __shfl_sync(0xffffffffu, v[k], 31));
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int OP>
+__global__ void seed_combine(T* out, Seed seed) {
+  out[0] = apply<T, OP>(seed.get<T>(), out[0]);
+}
+
+template <typename T>
+__global__ void fill_seed(T* out, int64_t n, Seed seed) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = seed.get<T>();
+}
+
+template <typename T>
+__global__ void gather_logical(const T* __restrict__ x, Lanes g, int64_t n, T* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = i, off = 0;
+    for (int d = g.n - 1; d >= 0; --d) {
+      off += (rem % g.size[d]) * g.xstride[d];
+      rem /= g.size[d];
+    }
+    y[i] = x[off];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+CUtensorMapDataType map_dtype(int dtype) {
+  switch (dtype) {
+    case NRS_F32: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    case NRS_F64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    case NRS_I32: return CU_TENSOR_MAP_DATA_TYPE_INT32;
+    default: return CU_TENSOR_MAP_DATA_TYPE_INT64;
+  }
+}
+
+bool encode_map(CUtensorMap* map, int dtype, const void* base, const uint64_t dims[3],
+                const uint64_t strides_bytes[2], const uint32_t box[3], CUtensorMapSwizzle sw) {
+  auto enc = nrs_get_encode_tiled();
+  if (!enc) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+  for (int i = 0; i < 2; ++i)
+    if ((strides_bytes[i] & 15) != 0 || strides_bytes[i] >= (1ull << 40) || strides_bytes[i] == 0)
+      return false;
+  for (int i = 0; i < 3; ++i)
+    if (dims[i] == 0 || dims[i] > (1ull << 32)) return false;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, map_dtype(dtype), 3, const_cast<void*>(base), dims, strides_bytes, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct LaneProblem {
+  int dtype;
+  const void* x;
+  void* out;
+  int64_t alen, xastride, oastride;
+  Lanes lanes;
+  int64_t n_lanes;
+  bool running;
+  bool same_layout;  // running fold: output strides equal the input's
+  Seed seed;
+};
+
+int grid_for(nrs_handle* h, int64_t items, int per_block) {
+  const int64_t blocks = (items + per_block - 1) / per_block;
+  const int64_t cap = (int64_t)h->num_sms * 16;
+  return (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+}
+
+// TMA lane kernels for (batch, lanes) x axis views; NRS_ERR_UNSUPPORTED when
+// the view does not qualify (nothing launched).
+template <typename T, int OP, bool RUNNING>
+int launch_lane_tma(nrs_handle* h, const LaneProblem& p) {
+  const Lanes& k = p.lanes;
+  if (k.n < 1 || k.n > 2 || p.alen < 1) return NRS_ERR_UNSUPPORTED;
+  if (RUNNING && !p.same_layout) return NRS_ERR_UNSUPPORTED;
+  const int es = sizeof(T);
+  const int64_t lanes = k.size[k.n - 1], lstride = k.xstride[k.n - 1];
+  const int64_t batch = (k.n == 2) ? k.size[0] : 1;
+  const int64_t bstride = (k.n == 2) ? k.xstride[0] : 0;
+  if (batch > 65535) return NRS_ERR_UNSUPPORTED;
+  const size_t smem = (size_t)kTileBytes * kScanStages + 8 * kScanStages + 1024;
+  CUtensorMap xmap, omap;
+  if (lstride == 1 && p.xastride > 1) {
+    const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
+    const uint64_t sb = (uint64_t)(batch > 1 ? bstride : p.xastride * p.alen) * es;
+    const uint64_t strides[2] = {(uint64_t)p.xastride * es, sb};
+    const uint32_t box[3] = {(uint32_t)kLanesPerCta, (uint32_t)col_rows<T>(), 1};
+    if (!encode_map(&xmap, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
+      return NRS_ERR_UNSUPPORTED;
+    if (RUNNING && !encode_map(&omap, p.dtype, p.out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
+      return NRS_ERR_UNSUPPORTED;
+    if (!RUNNING) omap = xmap;
+    auto kern = lane_scan_cols_tma<T, OP, RUNNING>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((unsigned)((lanes + kLanesPerCta - 1) / kLanesPerCta), (unsigned)batch);
+    kern<<<grid, kLanesPerCta, smem, h->stream>>>(xmap, omap, p.alen, lanes, (T*)p.out, h->dev_error,
+                                                   p.seed);
+    return nrs_after_launch(h, "lane_scan_cols_tma");
+  }
+  if (p.xastride == 1 && lstride > 1) {
+    const uint64_t dims[3] = {(uint64_t)p.alen, (uint64_t)lanes, (uint64_t)batch};
+    const uint64_t sb = (uint64_t)(batch > 1 ? bstride : lstride * lanes) * es;
+    const uint64_t strides[2] = {(uint64_t)lstride * es, sb};
+    const uint32_t box[3] = {(uint32_t)(128 / es), (uint32_t)kLanesPerCta, 1};
+    if (!encode_map(&xmap, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+      return NRS_ERR_UNSUPPORTED;
+    if (RUNNING && !encode_map(&omap, p.dtype, p.out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+      return NRS_ERR_UNSUPPORTED;
+    if (!RUNNING) omap = xmap;
+    auto kern = lane_scan_rows_tma<T, OP, RUNNING>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((unsigned)((lanes + kLanesPerCta - 1) / kLanesPerCta), (unsigned)batch);
+    kern<<<grid, kLanesPerCta, smem, h->stream>>>(xmap, omap, p.alen, lanes, (T*)p.out, h->dev_error,
+                                                   p.seed);
+    return nrs_after_launch(h, "lane_scan_rows_tma");
+  }
+  return NRS_ERR_UNSUPPORTED;
+}
+
+template <typename T, int OP, bool RUNNING>
+int launch_lanes(nrs_handle* h, const LaneProblem& p) {
+  if (p.alen >= 256 && p.n_lanes >= 64) {
+    const int st = launch_lane_tma<T, OP, RUNNING>(h, p);
+    if (st != NRS_ERR_UNSUPPORTED) return st;
+  }
+  lane_scan_generic<T, OP, RUNNING><<<grid_for(h, p.n_lanes, 256), 256, 0, h->stream>>>(
+      (const T*)p.x, p.lanes, p.n_lanes, p.alen, p.xastride, (T*)p.out, p.oastride, p.seed);
+  return nrs_after_launch(h, "lane_scan_generic");
+}
+
+template <typename T>
+int lanes_by_op(nrs_handle* h, int op, const LaneProblem& p) {
+#define NRS_LANE_CASE(OPC)                                                          \
+  case OPC:                                                                         \
+    return p.running ? launch_lanes<T, OPC, true>(h, p) : launch_lanes<T, OPC, false>(h, p);
+  switch (op) {
+    NRS_LANE_CASE(NRS_OP_ADD)
+    NRS_LANE_CASE(NRS_OP_SUB)
+    NRS_LANE_CASE(NRS_OP_MUL)
+    NRS_LANE_CASE(NRS_OP_MAX)
+    NRS_LANE_CASE(NRS_OP_MIN)
+    default:
+      if constexpr (std::is_floating_point<T>::value) {
+        return p.running ? launch_lanes<T, NRS_OP_DIV, true>(h, p) : launch_lanes<T, NRS_OP_DIV, false>(h, p);
+      } else {
+        return nrs_fail(h, NRS_ERR_DTYPE, "integer divide has no ufunc reduce/accumulate");
+      }
+  }
+#undef NRS_LANE_CASE
+}
+
+int run_lanes(nrs_handle* h, int op, const LaneProblem& p) {
+  switch (p.dtype) {
+    case NRS_F32: return lanes_by_op<float>(h, op, p);
+    case NRS_F64: return lanes_by_op<double>(h, op, p);
+    case NRS_I64: return lanes_by_op<int64_t>(h, op, p);
+    default: return lanes_by_op<int32_t>(h, op, p);
+  }
+}
+
+// Flat reduce-then-scan over a contiguous buffer. `final_out` set: only the
+// seeded total is written there (reduce); otherwise out[0..n) gets every
+// prefix (accumulate).
+template <typename T, int OP>
+int flat_scan_t(nrs_handle* h, const T* x, int64_t n, int has_seed, Seed seed, T* out,
+                T* final_out) {
+  const int64_t nchunks = (n + flat_chunk<T>() - 1) / flat_chunk<T>();
+  int st;
+  T* ws = (T*)nrs_workspace(h, (size_t)(2 * nchunks + 2) * sizeof(T) + 256, &st);
+  if (!ws) return st;
+  T* totals = ws;
+  T* carries = ws + nchunks + 1;
+  const int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
+  flat_chunk_totals<T, OP><<<grid, 256, 0, h->stream>>>(x, n, totals);
+  flat_chunk_carries<T, OP><<<1, 1024, 0, h->stream>>>(totals, nchunks, has_seed, seed, carries, final_out);
+  if (!final_out) flat_chunk_scan<T, OP><<<grid, 256, 0, h->stream>>>(x, n, carries, out);
+  return nrs_after_launch(h, "flat scan");
+}
+
+template <typename T>
+int flat_scan(nrs_handle* h, int op, const T* x, int64_t n, int has_seed, Seed seed, T* out,
+              T* final_out) {
+  switch (op) {
+    case NRS_OP_ADD: return flat_scan_t<T, NRS_OP_ADD>(h, x, n, has_seed, seed, out, final_out);
+    case NRS_OP_MUL: return flat_scan_t<T, NRS_OP_MUL>(h, x, n, has_seed, seed, out, final_out);
+    case NRS_OP_MAX: return flat_scan_t<T, NRS_OP_MAX>(h, x, n, has_seed, seed, out, final_out);
+    default: return flat_scan_t<T, NRS_OP_MIN>(h, x, n, has_seed, seed, out, final_out);
+  }
+}
+
+int flat_scan_dtype(nrs_handle* h, int dtype, int op, const void* x, int64_t n, int has_seed, Seed seed,
+                    void* out, void* final_out) {
+  switch (dtype) {
+    case NRS_F32: return flat_scan<float>(h, op, (const float*)x, n, has_seed, seed, (float*)out, (float*)final_out);
+    case NRS_F64: return flat_scan<double>(h, op, (const double*)x, n, has_seed, seed, (double*)out, (double*)final_out);
+    case NRS_I64: return flat_scan<int64_t>(h, op, (const int64_t*)x, n, has_seed, seed, (int64_t*)out, (int64_t*)final_out);
+    default: return flat_scan<int32_t>(h, op, (const int32_t*)x, n, has_seed, seed, (int32_t*)out, (int32_t*)final_out);
+  }
+}
+
+bool valid_op(int op) {
+  return op == NRS_OP_ADD || op == NRS_OP_SUB || op == NRS_OP_MUL || op == NRS_OP_DIV ||
+         op == NRS_OP_MAX || op == NRS_OP_MIN;
+}
+
+const char* op_name(int op) {
+  switch (op) {
+    case NRS_OP_ADD: return "add";
+    case NRS_OP_SUB: return "subtract";
+    case NRS_OP_MUL: return "multiply";
+    case NRS_OP_DIV: return "divide";
+    case NRS_OP_MAX: return "maximum";
+    default: return "minimum";
+  }
+}
+
+Seed seed_from(int dtype, const void* value) {
+  Seed s{};
+  s.first = 0;
+  switch (dtype) {
+    case NRS_F32: s.fseed = *(const float*)value; break;
+    case NRS_F64: s.fseed = *(const double*)value; break;
+    case NRS_I64: s.iseed = *(const int64_t*)value; break;
+    default: s.iseed = *(const int32_t*)value; break;
+  }
+  return s;
+}
+
+Seed seed_const(double v) {
+  Seed s{};
+  s.first = 0;
+  s.fseed = v;
+  s.iseed = (int64_t)v;
+  return s;
+}
+
+Seed seed_first() {
+  Seed s{};
+  s.first = 1;
+  return s;
+}
+
+// Shared validation and the gather of a non-contiguous view into logical
+// order (kernels::borrow::operand, src/kernels/borrow.rs:59).
+struct View {
+  int64_t total = 1;
+  bool contig = true;
+  Lanes all{};
+};
+
+int check_view(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+               const int64_t* strides, View* v) {
+  if (ndim < 0 || ndim > kMaxDims || (ndim > 0 && (!shape || !strides)))
+    return nrs_fail(h, NRS_ERR_INVALID, "bad ndim/shape/strides");
+  if (!valid_op(op)) return nrs_fail(h, NRS_ERR_INVALID, "unknown ufunc op");
+  if (!nrs_dtype_size(dtype)) return nrs_fail(h, NRS_ERR_DTYPE, "unknown dtype");
+  if (op == NRS_OP_DIV && (dtype == NRS_I32 || dtype == NRS_I64))
+    return nrs_fail(h, NRS_ERR_DTYPE, "integer divide has no ufunc reduce/accumulate");
+  int64_t expect = 1;
+  v->all.n = ndim;
+  for (int d = ndim - 1; d >= 0; --d) {
+    if (shape[d] < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative dimension");
+    if (strides[d] < 0) return nrs_fail(h, NRS_ERR_STRIDE, "negative stride");
+    if (shape[d] != 1 && strides[d] != expect) v->contig = false;
+    expect *= shape[d];
+    v->total *= shape[d];
+    v->all.size[d] = shape[d];
+    v->all.xstride[d] = strides[d];
+  }
+  return NRS_OK;
+}
+
+// Contiguous logical-order copy of a view in workspace, past `reserve` bytes.
+int gathered(nrs_handle* h, int dtype, const void* x, const View& v, size_t reserve, const void** src) {
+  if (v.contig || v.total == 0) {
+    *src = x;
+    return NRS_OK;
+  }
+  const size_t es = nrs_dtype_size(dtype);
+  int st;
+  uint8_t* ws = (uint8_t*)nrs_workspace(h, reserve + (size_t)v.total * es, &st);
+  if (!ws) return st;
+  void* dst = ws + reserve;
+  const int grid = h->num_sms * 8;
+  if (es == 4) gather_logical<uint32_t><<<grid, 256, 0, h->stream>>>((const uint32_t*)x, v.all, v.total, (uint32_t*)dst);
+  else gather_logical<uint64_t><<<grid, 256, 0, h->stream>>>((const uint64_t*)x, v.all, v.total, (uint64_t*)dst);
+  if ((st = nrs_after_launch(h, "gather_logical"))) return st;
+  *src = dst;
+  return NRS_OK;
+}
+
+int fill(nrs_handle* h, int dtype, void* out, int64_t n, Seed s) {
+  const int grid = grid_for(h, n, 256);
+  switch (dtype) {
+    case NRS_F32: fill_seed<float><<<grid, 256, 0, h->stream>>>((float*)out, n, s); break;
+    case NRS_F64: fill_seed<double><<<grid, 256, 0, h->stream>>>((double*)out, n, s); break;
+    case NRS_I64: fill_seed<int64_t><<<grid, 256, 0, h->stream>>>((int64_t*)out, n, s); break;
+    default: fill_seed<int32_t><<<grid, 256, 0, h->stream>>>((int32_t*)out, n, s); break;
+  }
+  return nrs_after_launch(h, "fill_seed");
+}
+
+template <int OP>
+int seed_combine_dtype(nrs_handle* h, int dtype, void* out, Seed s) {
+  switch (dtype) {
+    case NRS_F32: seed_combine<float, OP><<<1, 1, 0, h->stream>>>((float*)out, s); break;
+    case NRS_F64: seed_combine<double, OP><<<1, 1, 0, h->stream>>>((double*)out, s); break;
+    case NRS_I64: seed_combine<int64_t, OP><<<1, 1, 0, h->stream>>>((int64_t*)out, s); break;
+    default: seed_combine<int32_t, OP><<<1, 1, 0, h->stream>>>((int32_t*)out, s); break;
+  }
+  return nrs_after_launch(h, "seed_combine");
+}
+
+// Normalises `axis` and builds the lane problem: kept dims collapsed outer
+// to inner where both the input's and the output's strides allow.
+int lane_problem(nrs_handle* h, int ndim, const int64_t* shape, const int64_t* strides, int64_t axis,
+                 const int64_t* out_strides, LaneProblem* p, int* ax_out) {
+  if (ndim == 0) return nrs_fail(h, NRS_ERR_AXIS, "axis given for a 0-d array");
+  const int64_t ax = axis < 0 ? axis + ndim : axis;
+  if (ax < 0 || ax >= ndim)
+    return nrs_fail(h, NRS_ERR_AXIS, "axis " + std::to_string(axis) +
+                                         " out of bounds for array of dimension " +
+                                         std::to_string(ndim));
+  *ax_out = (int)ax;
+  p->alen = shape[ax];
+  p->xastride = strides[ax];
+  p->oastride = out_strides ? out_strides[ax] : 0;
+  Lanes& k = p->lanes;
+  k.n = 0;
+  p->n_lanes = 1;
+  p->same_layout = true;
+  for (int d = 0; d < ndim; ++d) {
+    const int64_t os = out_strides ? out_strides[d] : 0;
+    if (out_strides && shape[d] != 1 && os != strides[d]) p->same_layout = false;
+    if (d == ax) continue;
+    p->n_lanes *= shape[d];
+    if (shape[d] == 1) continue;
+    if (k.n > 0 && k.xstride[k.n - 1] == strides[d] * shape[d] &&
+        k.ostride[k.n - 1] == os * shape[d]) {
+      k.size[k.n - 1] *= shape[d];
+      k.xstride[k.n - 1] = strides[d];
+      k.ostride[k.n - 1] = os;
+    } else {
+      k.size[k.n] = shape[d];
+      k.xstride[k.n] = strides[d];
+      k.ostride[k.n] = os;
+      k.n++;
+    }
+  }
+  // A reduction writes lane o at out[o]: row-major kept dims.
+  if (!out_strides) {
+    int64_t c = 1;
+    for (int d = k.n - 1; d >= 0; --d) {
+      k.ostride[d] = c;
+      c *= k.size[d];
+    }
+  }
+  return NRS_OK;
+}
+
+}  // namespace
+
+extern "C" int nrs_ufunc_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+                                const int64_t* strides, int64_t axis, const void* initial,
+                                const void* x, void* out) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  View v;
+  int st = check_view(h, dtype, op, ndim, shape, strides, &v);
+  if (st) return st;
+  if (v.total > 0 && !x) return nrs_fail(h, NRS_ERR_INVALID, "null input");
+  if ((st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice"))) return st;
+  const bool has_init = initial != nullptr;
+  const std::string no_identity =
+      std::string("zero-size array to reduction operation ") + op_name(op) + " which has no identity";
+
+  if (axis == NRS_AXIS_NONE) {
+    if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
+    // reduce_full: add / multiply are seed (op) the tiered flat sum / product.
+    if (op == NRS_OP_ADD || op == NRS_OP_MUL) {
+      const int64_t one = 1;
+      const int64_t* shp = ndim ? shape : &one;
+      const int64_t* strd = ndim ? strides : &one;
+      if ((st = nrs_reduce(h, dtype, op == NRS_OP_ADD ? NRS_SUM : NRS_PROD, ndim ? ndim : 1, shp, strd,
+                           NRS_AXIS_NONE, 0, x, out)))
+        return st;
+      const Seed s = has_init ? seed_from(dtype, initial) : seed_const(op == NRS_OP_ADD ? 0.0 : 1.0);
+      return op == NRS_OP_ADD ? seed_combine_dtype<NRS_OP_ADD>(h, dtype, out, s)
+                              : seed_combine_dtype<NRS_OP_MUL>(h, dtype, out, s);
+    }
+    if (v.total == 0) {
+      if (!has_init) return nrs_fail(h, NRS_ERR_EMPTY, no_identity);
+      return fill(h, dtype, out, 1, seed_from(dtype, initial));
+    }
+    const size_t reserve = (size_t)(2 * (v.total / 4096 + 2)) * 8 + 4096;
+    const void* src;
+    if ((st = gathered(h, dtype, x, v, reserve, &src))) return st;
+    if (op == NRS_OP_MAX || op == NRS_OP_MIN)
+      return flat_scan_dtype(h, dtype, op, src, v.total, has_init,
+                             has_init ? seed_from(dtype, initial) : seed_const(0.0), nullptr, out);
+    // subtract / divide: one serial lane.
+    LaneProblem p{};
+    p.dtype = dtype;
+    p.x = src;
+    p.out = out;
+    p.alen = v.total;
+    p.xastride = 1;
+    p.lanes.n = 0;
+    p.n_lanes = 1;
+    p.running = false;
+    p.seed = has_init ? seed_from(dtype, initial) : seed_first();
+    return run_lanes(h, op, p);
+  }
+
+  LaneProblem p{};
+  int ax;
+  if ((st = lane_problem(h, ndim, shape, strides, axis, nullptr, &p, &ax))) return st;
+  if (p.n_lanes == 0) return NRS_OK;
+  if (!out) return nrs_fail(h, NRS_ERR_INVALID, "null output");
+  if (p.alen == 0) {
+    // reduce_lane on empty lanes: initial, else the identity, else an error.
+    if (has_init) return fill(h, dtype, out, p.n_lanes, seed_from(dtype, initial));
+    if (op == NRS_OP_ADD || op == NRS_OP_MUL)
+      return fill(h, dtype, out, p.n_lanes, seed_const(op == NRS_OP_ADD ? 0.0 : 1.0));
+    return nrs_fail(h, NRS_ERR_EMPTY, no_identity);
+  }
+  p.dtype = dtype;
+  p.x = x;
+  p.out = out;
+  p.running = false;
+  p.seed = has_init ? seed_from(dtype, initial) : seed_first();
+  return run_lanes(h, op, p);
+}
+
+extern "C" int nrs_accumulate(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
+                              const int64_t* strides, int64_t axis, const void* x, void* out,
+                              const int64_t* out_strides) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  View v;
+  int st = check_view(h, dtype, op, ndim, shape, strides, &v);
+  if (st) return st;
+  if (v.total == 0) {
+    if (axis != NRS_AXIS_NONE && ndim > 0) {
+      const int64_t ax = axis < 0 ? axis + ndim : axis;
+      if (ax < 0 || ax >= ndim)
+        return nrs_fail(h, NRS_ERR_AXIS, "axis " + std::to_string(axis) +
+                                             " out of bounds for array of dimension " +
+                                             std::to_string(ndim));
+    }
+    return NRS_OK;
+  }
+  if (!x || !out) return nrs_fail(h, NRS_ERR_INVALID, "null input or output");
+  if (out_strides)
+    for (int d = 0; d < ndim; ++d)
+      if (out_strides[d] < 0) return nrs_fail(h, NRS_ERR_STRIDE, "negative stride");
+  if ((st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice"))) return st;
+  // cumsum seeds lanes with 0, cumprod with 1; the other ufuncs with the
+  // lane's first element.
+  const Seed seed = op == NRS_OP_ADD ? seed_const(0.0) : op == NRS_OP_MUL ? seed_const(1.0) : seed_first();
+
+  if (axis == NRS_AXIS_NONE) {
+    // Flattened: out is the n values in logical order, contiguous.
+    const size_t reserve = (size_t)(2 * (v.total / 4096 + 2)) * 8 + 4096;
+    const void* src;
+    if ((st = gathered(h, dtype, x, v, reserve, &src))) return st;
+    const bool order_free = (op == NRS_OP_ADD || op == NRS_OP_MUL || op == NRS_OP_MAX || op == NRS_OP_MIN);
+    if (order_free && v.total >= 64)
+      return flat_scan_dtype(h, dtype, op, src, v.total, !seed.first, seed, out, nullptr);
+    LaneProblem p{};
+    p.dtype = dtype;
+    p.x = src;
+    p.out = out;
+    p.alen = v.total;
+    p.xastride = 1;
+    p.oastride = 1;
+    p.lanes.n = 0;
+    p.n_lanes = 1;
+    p.running = true;
+    p.same_layout = false;
+    p.seed = seed;
+    return run_lanes(h, op, p);
+  }
+
+  int64_t cstr[kMaxDims];
+  if (!out_strides) {
+    int64_t c = 1;
+    for (int d = ndim - 1; d >= 0; --d) {
+      cstr[d] = c;
+      c *= shape[d];
+    }
+  }
+  LaneProblem p{};
+  int ax;
+  if ((st = lane_problem(h, ndim, shape, strides, axis, out_strides ? out_strides : cstr, &p, &ax)))
+    return st;
+  p.dtype = dtype;
+  p.x = x;
+  p.out = out;
+  p.running = true;
+  p.seed = seed;
+  return run_lanes(h, op, p);
+}

@@ -154,6 +154,89 @@ def sum_axis(a, axis: int):
 
 
 # ---------------------------------------------------------------------------
+# Ufunc reduce / accumulate (src/ufunc_ops.rs)
+# ---------------------------------------------------------------------------
+UFUNC_OPS = {"add": L.OP_ADD, "subtract": L.OP_SUB, "multiply": L.OP_MUL, "divide": L.OP_DIV,
+             "maximum": L.OP_MAX, "minimum": L.OP_MIN}
+_CSCALAR = {L.F32: C.c_float, L.F64: C.c_double, L.I64: C.c_int64, L.I32: C.c_int32}
+
+
+def _ufunc_code(op) -> int:
+    if isinstance(op, str):
+        try:
+            return UFUNC_OPS[op]
+        except KeyError:
+            raise L.NumRs2Error(L.ERR_INVALID, f"unknown ufunc {op!r}") from None
+    return int(op)
+
+
+def ufunc_reduce(op, a: torch.Tensor, axis: int | None = None, keepdims: bool = False,
+                 initial=None) -> torch.Tensor:
+    """ufunc_ops::ufunc_reduce (src/ufunc_ops.rs:417): `op` is a UfuncOp name
+    ("add", "subtract", "multiply", "divide", "maximum", "minimum"). Output
+    shape as ufunc_reduce: the axis removed (kept as 1 with keepdims), `[1]`
+    for a full reduction (all-ones dims with keepdims)."""
+    _need_cuda(a)
+    lib = L.load()
+    h = handle(a.device.index)
+    code = dtype_code(a)
+    nd = a.dim()
+    if axis is None:
+        out_shape = [1] * nd if keepdims else [1]
+        ax = L.AXIS_NONE
+    else:
+        ax = axis
+        norm = axis + nd if axis < 0 else axis
+        out_shape = [1]
+        if 0 <= norm < nd:
+            out_shape = list(a.shape)
+            if keepdims:
+                out_shape[norm] = 1
+            else:
+                out_shape.pop(norm)
+            if not out_shape:
+                out_shape = [1]
+    out = torch.empty(out_shape, dtype=a.dtype, device=a.device)
+    seed = None if initial is None else _CSCALAR[code](initial)
+    init = None if seed is None else C.cast(C.pointer(seed), C.c_void_p)
+    st = lib.nrs_ufunc_reduce(h, code, _ufunc_code(op), nd, L.i64_array(a.shape),
+                              L.i64_array(a.stride()), ax, init, _ptr(a), _ptr(out))
+    L.check(st, h)
+    return out
+
+
+def ufunc_accumulate(op, a: torch.Tensor, axis: int | None = None) -> torch.Tensor:
+    """ufunc_ops::ufunc_accumulate (src/ufunc_ops.rs:523): the running fold
+    along `axis` (same shape as `a`, allocated with `a`'s memory layout when
+    that is dense, so a transposed view streams the same way in and out), or
+    over the flattened array for axis=None (1-D, `a.numel()` values)."""
+    _need_cuda(a)
+    lib = L.load()
+    h = handle(a.device.index)
+    code = dtype_code(a)
+    if axis is None:
+        out = torch.empty(a.numel(), dtype=a.dtype, device=a.device)
+        ax, ostr = L.AXIS_NONE, None
+    else:
+        out = torch.empty_like(a)
+        ax, ostr = axis, L.i64_array(out.stride())
+    st = lib.nrs_accumulate(h, code, _ufunc_code(op), a.dim(), L.i64_array(a.shape),
+                            L.i64_array(a.stride()), ax, _ptr(a), _ptr(out), ostr)
+    L.check(st, h)
+    return out
+
+
+def cumsum(a, axis=None):
+    """math::cumsum (src/math/statistics/mod.rs:584): running sum from 0."""
+    return ufunc_accumulate("add", a, axis)
+
+
+def cumprod(a, axis=None):
+    """math::cumprod (src/math/statistics/mod.rs:795): running product from 1."""
+    return ufunc_accumulate("multiply", a, axis)
+
+
+# ---------------------------------------------------------------------------
 # GEMM
 # ---------------------------------------------------------------------------
 def _mat_strides(t: torch.Tensor):

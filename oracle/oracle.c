@@ -414,6 +414,171 @@ void orc_axis_i64(int op, int ndim, const int64_t* shape, const int64_t* strides
 }
 
 /* ------------------------------------------------------------------------ */
+/* Ufunc reduce / accumulate (src/ufunc_ops.rs) and cumsum / cumprod          */
+/* (src/math/statistics/mod.rs:584-900).                                      */
+/*                                                                           */
+/* UfuncOp::apply (src/ufunc_ops.rs:153-181): add/sub/mul/div round once;    */
+/* maximum/minimum give NaN (Rust's quiet-NaN bits) if either side is NaN,   */
+/* else the left operand only if strictly greater (smaller).                 */
+/* reduce_lane (:230-255): seeded by `initial` and folding every element, or */
+/* by the lane's first element; an empty lane gives `initial`, the op's      */
+/* identity (add 0, multiply 1) or an error.                                 */
+/* reduce_full (:265-297): add / multiply on f32/f64 are seed + sum and      */
+/* seed * prod through the tiered flat kernels; every other case is          */
+/* reduce_lane over the flattened array.                                     */
+/* accumulate (:523): add -> cumsum, a zero-seeded running sum per lane or   */
+/* over the flattened array (:596-735); multiply -> cumprod, one-seeded      */
+/* (:807-900); the rest seeded by the first element (accumulate_flat :452,   */
+/* accumulate_along_axis :470). The f32/f64 flat cumsum of 64 or more        */
+/* elements goes through scirs2-core's simd_cumsum, which is outside the     */
+/* repository; it is restated as the same running sum (parity there is      */
+/* tolerance-based).                                                          */
+/* Op codes are nrs_ufunc's: ADD 2, SUB 3, MUL 4, DIV 5, MAX 11, MIN 12.     */
+/* Integer arithmetic wraps (two's complement); integer DIV is not defined.  */
+/* Outputs: reduce -> the kept dims row-major; accumulate -> the full shape  */
+/* row-major (the flat case: n elements).                                    */
+/* ------------------------------------------------------------------------ */
+enum { U_ADD = 2, U_SUB = 3, U_MUL = 4, U_DIV = 5, U_MAX = 11, U_MIN = 12 };
+
+static inline float qnan_f32(void) {
+  uint32_t b = 0x7fc00000u;
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+}
+static inline double qnan_f64(void) {
+  uint64_t b = 0x7ff8000000000000ull;
+  double f;
+  memcpy(&f, &b, 8);
+  return f;
+}
+static inline float uapply_f32(int op, float a, float b) {
+  switch (op) {
+    case U_ADD: return a + b;
+    case U_SUB: return a - b;
+    case U_MUL: return a * b;
+    case U_DIV: return a / b;
+    case U_MAX: return (a != a || b != b) ? qnan_f32() : (a > b ? a : b);
+    default: return (a != a || b != b) ? qnan_f32() : (a < b ? a : b);
+  }
+}
+static inline double uapply_f64(int op, double a, double b) {
+  switch (op) {
+    case U_ADD: return a + b;
+    case U_SUB: return a - b;
+    case U_MUL: return a * b;
+    case U_DIV: return a / b;
+    case U_MAX: return (a != a || b != b) ? qnan_f64() : (a > b ? a : b);
+    default: return (a != a || b != b) ? qnan_f64() : (a < b ? a : b);
+  }
+}
+static inline int64_t uapply_i64(int op, int64_t a, int64_t b) {
+  switch (op) {
+    case U_ADD: return (int64_t)((uint64_t)a + (uint64_t)b);
+    case U_SUB: return (int64_t)((uint64_t)a - (uint64_t)b);
+    case U_MUL: return (int64_t)((uint64_t)a * (uint64_t)b);
+    case U_MAX: return a > b ? a : b;
+    default: return a < b ? a : b;
+  }
+}
+static inline float useq_sum_f32(const float* a, int64_t n) { return orc_sum_f32(a, n); }
+static inline double useq_sum_f64(const double* a, int64_t n) { return orc_sum_f64(a, n); }
+static inline int64_t useq_sum_i64(const int64_t* a, int64_t n) { return orc_sum_i64(a, n); }
+static inline float useq_prod_f32(const float* a, int64_t n) { return orc_prod_f32(a, n); }
+static inline double useq_prod_f64(const double* a, int64_t n) { return orc_prod_f64(a, n); }
+static inline int64_t useq_prod_i64(const int64_t* a, int64_t n) { return orc_prod_i64(a, n); }
+
+/* Offset of logical (row-major) element i of a strided view. */
+static int64_t logical_offset(int ndim, const int64_t* shape, const int64_t* strides, int64_t i) {
+  int64_t off = 0;
+  for (int d = ndim - 1; d >= 0; --d) {
+    off += (i % shape[d]) * strides[d];
+    i /= shape[d];
+  }
+  return off;
+}
+
+#define DEFINE_UFUNC_SCAN(T, SUF)                                                           \
+  /* Returns 0, or -1 for an empty lane with no initial and no identity. */                 \
+  int orc_ufunc_reduce_##SUF(int op, int ndim, const int64_t* shape, const int64_t* strides, \
+                             int axis, int has_init, T init, const T* x, T* out) {          \
+    int64_t n = 1;                                                                          \
+    for (int d = 0; d < ndim; ++d) n *= shape[d];                                           \
+    if (axis < 0) {                                                                         \
+      T* flat = (T*)malloc((size_t)(n > 0 ? n : 1) * sizeof(T));                            \
+      for (int64_t i = 0; i < n; ++i) flat[i] = x[logical_offset(ndim, shape, strides, i)]; \
+      int rc = 0;                                                                           \
+      if (op == U_ADD) {                                                                    \
+        out[0] = uapply_##SUF(U_ADD, has_init ? init : (T)0, useq_sum_##SUF(flat, n));      \
+      } else if (op == U_MUL) {                                                             \
+        out[0] = uapply_##SUF(U_MUL, has_init ? init : (T)1, useq_prod_##SUF(flat, n));     \
+      } else if (n == 0) {                                                                  \
+        if (has_init) out[0] = init; else rc = -1;                                          \
+      } else {                                                                              \
+        T acc = has_init ? uapply_##SUF(op, init, flat[0]) : flat[0];                       \
+        for (int64_t i = 1; i < n; ++i) acc = uapply_##SUF(op, acc, flat[i]);               \
+        out[0] = acc;                                                                       \
+      }                                                                                     \
+      free(flat);                                                                           \
+      return rc;                                                                            \
+    }                                                                                       \
+    int64_t n_out = 1;                                                                      \
+    for (int d = 0; d < ndim; ++d) if (d != axis) n_out *= shape[d];                        \
+    const int64_t alen = shape[axis], ast = strides[axis];                                  \
+    if (alen == 0 && n_out > 0 && !has_init && op != U_ADD && op != U_MUL) return -1;       \
+    for (int64_t o = 0; o < n_out; ++o) {                                                   \
+      int64_t b;                                                                            \
+      lane_bases(ndim, shape, strides, axis, o, &b);                                        \
+      const T* p = x + b;                                                                   \
+      T acc;                                                                                \
+      int64_t j0;                                                                           \
+      if (has_init) { acc = init; j0 = 0; }                                                 \
+      else if (alen == 0) { acc = (op == U_MUL) ? (T)1 : (T)0; j0 = 0; }                    \
+      else { acc = p[0]; j0 = 1; }                                                          \
+      for (int64_t j = j0; j < alen; ++j) acc = uapply_##SUF(op, acc, p[j * ast]);          \
+      out[o] = acc;                                                                         \
+    }                                                                                       \
+    return 0;                                                                               \
+  }                                                                                         \
+  void orc_accumulate_##SUF(int op, int ndim, const int64_t* shape, const int64_t* strides, \
+                            int axis, const T* x, T* out) {                                 \
+    int64_t n = 1;                                                                          \
+    for (int d = 0; d < ndim; ++d) n *= shape[d];                                           \
+    if (n == 0) return;                                                                     \
+    if (axis < 0) {                                                                         \
+      T acc = (op == U_MUL) ? (T)1 : (T)0;                                                  \
+      for (int64_t i = 0; i < n; ++i) {                                                     \
+        T v = x[logical_offset(ndim, shape, strides, i)];                                   \
+        if (i == 0 && op != U_ADD && op != U_MUL) acc = v;                                  \
+        else acc = uapply_##SUF(op, acc, v);                                                \
+        out[i] = acc;                                                                       \
+      }                                                                                     \
+      return;                                                                               \
+    }                                                                                       \
+    int64_t cstr[16];                                                                       \
+    cstr[ndim - 1] = 1;                                                                     \
+    for (int d = ndim - 2; d >= 0; --d) cstr[d] = cstr[d + 1] * shape[d + 1];               \
+    int64_t n_out = n / shape[axis];                                                        \
+    const int64_t alen = shape[axis], ast = strides[axis], ost = cstr[axis];                \
+    _Pragma("omp parallel for schedule(static)")                                            \
+    for (int64_t o = 0; o < n_out; ++o) {                                                   \
+      int64_t b, ob;                                                                        \
+      lane_bases(ndim, shape, strides, axis, o, &b);                                        \
+      lane_bases(ndim, shape, cstr, axis, o, &ob);                                          \
+      T acc = (op == U_MUL) ? (T)1 : (T)0;                                                  \
+      for (int64_t j = 0; j < alen; ++j) {                                                  \
+        T v = x[b + j * ast];                                                               \
+        if (j == 0 && op != U_ADD && op != U_MUL) acc = v;                                  \
+        else acc = uapply_##SUF(op, acc, v);                                                \
+        out[ob + j * ost] = acc;                                                            \
+      }                                                                                     \
+    }                                                                                       \
+  }
+DEFINE_UFUNC_SCAN(float, f32)
+DEFINE_UFUNC_SCAN(double, f64)
+DEFINE_UFUNC_SCAN(int64_t, i64)
+
+/* ------------------------------------------------------------------------ */
 /* Elementwise.                                                              */
 /*                                                                           */
 /* y = exp(a*x + b): the eager spelling is three passes, `x * a` and `+ b`   */

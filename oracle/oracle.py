@@ -96,6 +96,11 @@ def _declare(L):
         fn.argtypes, fn.restype = [i32, i32, vp, vp, i32, vp, vp], None
         fn = getattr(L, f"orc_flat_arg_{suf}")
         fn.argtypes, fn.restype = [i32, vp, i64], i64
+    for suf, T in (("f32", f32), ("f64", f64), ("i64", i64)):
+        fn = getattr(L, f"orc_ufunc_reduce_{suf}")
+        fn.argtypes, fn.restype = [i32, i32, vp, vp, i32, i32, T, vp, vp], i32
+        fn = getattr(L, f"orc_accumulate_{suf}")
+        fn.argtypes, fn.restype = [i32, i32, vp, vp, i32, vp, vp], None
 
 
 _SUF = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.int64): "i64"}
@@ -176,6 +181,41 @@ class Oracle:
         getattr(self.L, f"orc_axis_arg_{_SUF[x.dtype]}")(
             int(want_max), x.ndim, _p(shape), _p(strides), axis,
             C.c_void_p(x.__array_interface__["data"][0]), _p(out))
+        return out
+
+    # -- ufunc reduce / accumulate ----------------------------------------
+    def ufunc_reduce(self, op: int, x: np.ndarray, axis=None, initial=None) -> np.ndarray:
+        """ufunc_ops::ufunc_reduce restated (op codes of nrs_ufunc). Returns
+        the values in row-major order over the kept dims (one value when
+        axis is None); raises ValueError where the reference errors."""
+        item = x.dtype.itemsize
+        shape = np.array(x.shape if x.ndim else [1], dtype=np.int64)
+        strides = np.array([s // item for s in x.strides] if x.ndim else [1], dtype=np.int64)
+        nd = max(x.ndim, 1)
+        if axis is None:
+            ax, n_out = -1, 1
+        else:
+            ax = axis + x.ndim if axis < 0 else axis
+            n_out = int(np.prod([d for i, d in enumerate(x.shape) if i != ax]))
+        out = np.empty(max(n_out, 1), dtype=x.dtype)
+        rc = getattr(self.L, f"orc_ufunc_reduce_{_SUF[x.dtype]}")(
+            op, nd, _p(shape), _p(strides), ax, int(initial is not None),
+            0 if initial is None else initial, C.c_void_p(x.__array_interface__["data"][0]), _p(out))
+        if rc != 0:
+            raise ValueError("zero-size array to reduction operation which has no identity")
+        return out[:n_out]
+
+    def accumulate(self, op: int, x: np.ndarray, axis=None) -> np.ndarray:
+        """ufunc_accumulate / cumsum / cumprod restated: the full shape in
+        row-major order for an axis, the flattened n values for None."""
+        item = x.dtype.itemsize
+        shape = np.array(x.shape if x.ndim else [1], dtype=np.int64)
+        strides = np.array([s // item for s in x.strides] if x.ndim else [1], dtype=np.int64)
+        nd = max(x.ndim, 1)
+        ax = -1 if axis is None else (axis + x.ndim if axis < 0 else axis)
+        out = np.empty(x.shape if axis is not None else (x.size,), dtype=x.dtype)
+        getattr(self.L, f"orc_accumulate_{_SUF[x.dtype]}")(
+            op, nd, _p(shape), _p(strides), ax, C.c_void_p(x.__array_interface__["data"][0]), _p(out))
         return out
 
     # -- elementwise ------------------------------------------------------

@@ -185,3 +185,72 @@ def test_program_evaluator_matches_binary(ora, dtype):
         p = ora.program([(0, 0, 0.0), (0, 1, 0.0), (code, 0, 0.0)], [a, b])
         c = ora.binary(op, a, b)
         np.testing.assert_array_equal(p.view(np.uint8), c.view(np.uint8))
+
+
+# Known answers from the reference's own tests of ufunc reduce / accumulate
+# (src/ufunc_ops.rs, test module from :932) and cumsum / cumprod
+# (tests/test_stats_api_honesty.rs:90-150). Each row: (name, op code, input,
+# shape, axis, initial, expected values in row-major order).
+A23 = [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+UFUNC_KATS = [
+    ("reduce_add_axis_none", "reduce", 2, A23, (2, 3), None, None, [21.0]),
+    ("reduce_add_axis0", "reduce", 2, A23, (2, 3), 0, None, [5.0, 7.0, 9.0]),
+    ("reduce_add_axis1", "reduce", 2, A23, (2, 3), 1, None, [6.0, 15.0]),
+    ("reduce_add_axis_neg1", "reduce", 2, A23, (2, 3), -1, None, [6.0, 15.0]),
+    ("reduce_multiply_axis1", "reduce", 4, A23, (2, 3), 1, None, [6.0, 120.0]),
+    ("reduce_maximum_axis0", "reduce", 11, A23, (2, 3), 0, None, [4.0, 5.0, 6.0]),
+    ("reduce_minimum_axis1", "reduce", 12, A23, (2, 3), 1, None, [1.0, 4.0]),
+    ("reduce_add_initial", "reduce", 2, A23, (2, 3), 1, 100.0, [106.0, 115.0]),
+    ("reduce_multiply_initial", "reduce", 4, A23, (2, 3), 1, 2.0, [12.0, 240.0]),
+    ("reduce_maximum_initial0", "reduce", 11, A23, (2, 3), 1, 0.0, [3.0, 6.0]),
+    ("reduce_maximum_initial100", "reduce", 11, A23, (2, 3), 1, 100.0, [100.0, 100.0]),
+    ("reduce_add_empty", "reduce", 2, [], (0,), None, None, [0.0]),
+    ("reduce_multiply_empty", "reduce", 4, [], (0,), None, None, [1.0]),
+    ("reduce_add_empty_initial", "reduce", 2, [], (0,), None, 5.0, [5.0]),
+    ("reduce_maximum_empty_initial", "reduce", 11, [], (0,), None, 5.0, [5.0]),
+    ("reduce_add_empty_lanes", "reduce", 2, [], (3, 0), 1, None, [0.0, 0.0, 0.0]),
+    ("reduce_add_empty_lanes_initial", "reduce", 2, [], (3, 0), 1, 7.0, [7.0, 7.0, 7.0]),
+    ("reduce_maximum_empty_lanes_initial", "reduce", 11, [], (3, 0), 1, 7.0, [7.0, 7.0, 7.0]),
+    ("reduce_add_3d_axis_neg2", "reduce", 2, [float(i) for i in range(24)], (2, 3, 4), -2, None,
+     [12.0, 15.0, 18.0, 21.0, 48.0, 51.0, 54.0, 57.0]),
+    ("reduce_maximum_3d_axis_neg1", "reduce", 11, [float(i) for i in range(24)], (2, 3, 4), -1, None,
+     [3.0, 7.0, 11.0, 15.0, 19.0, 23.0]),
+    ("reduce_subtract_doc", "reduce", 3, [1.0, 2.0, 3.0], (3,), None, None, [-4.0]),
+    ("accumulate_add", "accumulate", 2, [1.0, 2.0, 3.0, 4.0], (4,), None, None, [1.0, 3.0, 6.0, 10.0]),
+    ("accumulate_multiply", "accumulate", 4, [1.0, 2.0, 3.0, 4.0], (4,), None, None, [1.0, 2.0, 6.0, 24.0]),
+    ("accumulate_maximum", "accumulate", 11, [1.0, 3.0, 2.0, 5.0, 4.0], (5,), None, None,
+     [1.0, 3.0, 3.0, 5.0, 5.0]),
+    ("accumulate_minimum", "accumulate", 12, [5.0, 3.0, 4.0, 1.0, 2.0], (5,), None, None,
+     [5.0, 3.0, 3.0, 1.0, 1.0]),
+    ("accumulate_subtract", "accumulate", 3, [10.0, 1.0, 2.0, 3.0], (4,), None, None, [10.0, 9.0, 7.0, 4.0]),
+    ("accumulate_divide", "accumulate", 5, [10.0, 1.0, 2.0, 3.0], (4,), None, None,
+     [10.0, 10.0, 5.0, 5.0 / 3.0]),
+    ("accumulate_maximum_axis1", "accumulate", 11, [1.0, 5.0, 2.0, 8.0, 1.0, 9.0], (2, 3), 1, None,
+     [1.0, 5.0, 5.0, 8.0, 8.0, 9.0]),
+    ("accumulate_minimum_axis0", "accumulate", 12, [1.0, 5.0, 2.0, 8.0, 1.0, 9.0], (2, 3), 0, None,
+     [1.0, 5.0, 2.0, 1.0, 1.0, 2.0]),
+    ("cumsum_axis1", "accumulate", 2, A23, (2, 3), 1, None, [1.0, 3.0, 6.0, 4.0, 9.0, 15.0]),
+]
+UFUNC_KAT_ERRORS = [  # reduce with no identity and no initial on an empty input
+    ("reduce_maximum_empty", 11, (0,), None),
+    ("reduce_minimum_empty", 12, (0,), None),
+    ("reduce_maximum_empty_lanes", 11, (3, 0), 1),
+]
+
+
+@pytest.mark.parametrize("case", UFUNC_KATS, ids=[c[0] for c in UFUNC_KATS])
+def test_ufunc_scan_known_answers_oracle(ora, case):
+    _, kind, op, data, shape, axis, initial, want = case
+    x = np.array(data, dtype=np.float64).reshape(shape)
+    if kind == "reduce":
+        got = ora.ufunc_reduce(op, x, axis, initial)
+    else:
+        got = ora.accumulate(op, x, axis)
+    np.testing.assert_allclose(got.ravel(), want, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("case", UFUNC_KAT_ERRORS, ids=[c[0] for c in UFUNC_KAT_ERRORS])
+def test_ufunc_scan_known_errors_oracle(ora, case):
+    _, op, shape, axis = case
+    with pytest.raises(ValueError):
+        ora.ufunc_reduce(op, np.zeros(shape), axis, None)
