@@ -145,12 +145,6 @@ __global__ void __launch_bounds__(256)
 // Lanes adjacent in memory (stride 1), axis strided: tiles of 64 lanes x
 // (8 KB / 64 / sizeof(T)) axis positions through an 8-stage TMA ring (the
 // geometry of the column reductions). Thread t owns lane l0 + t.
-//
-// RUNNING: thread t overwrites column t of the staged tile with its prefix
-// values; after a proxy fence and a CTA barrier one thread TMA-stores the
-// tile into the output (same dims and strides, positions outside the array
-// are clipped by the store) and re-arms the buffer only once that store has
-// finished reading it (bulk async-group wait), one iteration later.
 constexpr int kLanesPerCta = 64;
 constexpr int kScanStages = 8;
 constexpr int kTileBytes = 8192;
@@ -158,105 +152,72 @@ constexpr int kTileBytes = 8192;
 template <typename T>
 constexpr int col_rows() { return kTileBytes / (kLanesPerCta * (int)sizeof(T)); }
 
-template <typename T, int OP, bool RUNNING>
-__global__ void __launch_bounds__(kLanesPerCta)
-    lane_scan_cols_tma(const __grid_constant__ CUtensorMap xmap,
-                       const __grid_constant__ CUtensorMap omap, int64_t alen, int64_t lanes,
-                       T* __restrict__ out, uint32_t* err, Seed seed) {
-  constexpr int LW = kLanesPerCta;
+// 16-byte chunk j of row r of a 128-byte-swizzled tile.
+NRS_DEV int swz(int r, int j) { return r * 128 + ((j ^ (r & 7)) << 4); }
+
+// Folds one staged column (cols) / row (rows) of a tile into `acc`; with
+// WRITE the prefix values replace the staged ones. `first` seeds the lane
+// from its first element (the tile's element 0).
+template <typename T, int OP, bool WRITE>
+NRS_DEV T fold_col(T* tile, int t, int cnt, bool first, T acc) {
   constexpr int RB = col_rows<T>();
-  constexpr int S = kScanStages;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTileBytes * S);
-  __shared__ int abort_flag;
-
-  const int t = threadIdx.x;
-  const int64_t l0 = (int64_t)blockIdx.x * LW;
-  const int32_t batch = blockIdx.y;
-  const int64_t n_tiles = (alen + RB - 1) / RB;
-
-  if (t == 0) {
-    prefetch_tensormap(&xmap);
-    if (RUNNING) prefetch_tensormap(&omap);
-    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
-    fence_mbar_init();
-    abort_flag = 0;
-  }
-  __syncthreads();
-  if (t == 0) {
-    for (int s = 0; s < S && s < n_tiles; ++s) {
-      mbar_arrive_expect_tx(&full[s], kTileBytes);
-      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
+  constexpr int LW = kLanesPerCta;
+  if (cnt == RB) {
+    T v[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) v[r] = tile[r * LW + t];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) {
+      acc = (r == 0 && first) ? v[0] : apply<T, OP>(acc, v[r]);
+      v[r] = acc;
     }
-  }
-  T acc = seed.get<T>();
-  int64_t it = 0;
-  for (; it < n_tiles; ++it) {
-    const int s = (int)(it % S);
-    if (!mbar_wait_bounded(&full[s], (uint32_t)((it / S) & 1), NRS_WAIT_LIMIT)) abort_flag = 1;
-    __syncthreads();
-    if (abort_flag) break;
-    T* tile = reinterpret_cast<T*>(smem + s * kTileBytes);
-    const int64_t y0 = it * RB;
-    const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
-    int r = 0;
-    if (it == 0 && seed.first) {
-      acc = tile[t];
-      r = 1;
+    if (WRITE) {
+#pragma unroll
+      for (int r = 0; r < RB; ++r) tile[r * LW + t] = v[r];
     }
-    for (; r < cnt; ++r) {
-      acc = apply<T, OP>(acc, tile[r * LW + t]);
-      if (RUNNING) tile[r * LW + t] = acc;
-    }
-    if (RUNNING) fence_proxy_async_smem();
-    __syncthreads();
-    if (t == 0) {
-      if (RUNNING) {
-        tma_store_3d(&omap, tile, (int32_t)l0, (int32_t)y0, batch);
-        bulk_commit();
-        const int64_t nt = it - 1 + S;  // refill the previous iteration's buffer
-        if (it >= 1 && nt < n_tiles) {
-          bulk_wait_read<1>();
-          const int ps = (int)((it - 1) % S);
-          mbar_arrive_expect_tx(&full[ps], kTileBytes);
-          tma_load_3d(smem + ps * kTileBytes, &xmap, &full[ps], (int32_t)l0, (int32_t)(nt * RB), batch);
-        }
-      } else if (it + S < n_tiles) {
-        mbar_arrive_expect_tx(&full[s], kTileBytes);
-        tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)l0, (int32_t)((it + S) * RB), batch);
-      }
-    }
-  }
-  if (abort_flag) {
-    if (t == 0) {
-      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (3u << 8));
-      // Loads issued and not consumed: tiles it .. it + S - 1 at most.
-      for (int64_t j = it; j < n_tiles && j < it + S; ++j)
-        mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
-      if (RUNNING) bulk_wait<0>();
-    }
-    return;
-  }
-  if (RUNNING) {
-    if (t == 0) bulk_wait<0>();
   } else {
-    const int64_t lane = l0 + t;
-    if (lane < lanes) out[(int64_t)batch * lanes + lane] = acc;
+    for (int r = 0; r < cnt; ++r) {
+      acc = (r == 0 && first) ? tile[t] : apply<T, OP>(acc, tile[r * LW + t]);
+      if (WRITE) tile[r * LW + t] = acc;
+    }
   }
+  return acc;
 }
 
-// Lanes contiguous along the axis: tiles of 64 lanes x 128 bytes of axis with
-// the 128-byte swizzle (16-byte chunk j of tile row r at r*128 +
-// ((j ^ (r & 7)) * 16)); thread t owns row t. RUNNING rewrites the row in
-// place (same swizzled positions) and TMA-stores it like the column kernel.
-template <typename T, int OP, bool RUNNING>
-__global__ void __launch_bounds__(kLanesPerCta)
-    lane_scan_rows_tma(const __grid_constant__ CUtensorMap xmap,
-                       const __grid_constant__ CUtensorMap omap, int64_t alen, int64_t lanes,
-                       T* __restrict__ out, uint32_t* err, Seed seed) {
+template <typename T, int OP, bool WRITE>
+NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
   constexpr int XB = 128 / sizeof(T);
   constexpr int PER16 = 16 / sizeof(T);
+  T v[XB];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], tile + swz(t, j), 16);
+  if (cnt == XB) {
+#pragma unroll
+    for (int e = 0; e < XB; ++e) {
+      acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
+      v[e] = acc;
+    }
+  } else {
+    for (int e = 0; e < cnt; ++e) {
+      acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
+      v[e] = acc;
+    }
+  }
+  if (WRITE) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) memcpy(tile + swz(t, j), &v[j * PER16], 16);
+  }
+  return acc;
+}
+
+// Reduction along lanes (one value per lane): the axis-reduction pipeline.
+// COLS: lanes adjacent, map dims (lanes, axis, batch); else lanes along
+// rows, map dims (axis, lanes, batch) with the 128-byte swizzle.
+template <typename T, int OP, bool COLS>
+__global__ void __launch_bounds__(kLanesPerCta)
+    lane_reduce_tma(const __grid_constant__ CUtensorMap xmap, int64_t alen, int64_t lanes,
+                    T* __restrict__ out, uint32_t* err, Seed seed) {
+  constexpr int TB = COLS ? col_rows<T>() : 128 / (int)sizeof(T);  // axis positions per tile
   constexpr int S = kScanStages;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -266,92 +227,193 @@ __global__ void __launch_bounds__(kLanesPerCta)
   const int t = threadIdx.x;
   const int64_t l0 = (int64_t)blockIdx.x * kLanesPerCta;
   const int32_t batch = blockIdx.y;
-  const int64_t n_tiles = (alen + XB - 1) / XB;
+  const int64_t n_tiles = (alen + TB - 1) / TB;
+  auto load = [&](int s, int64_t tile) {
+    mbar_arrive_expect_tx(&full[s], kTileBytes);
+    if (COLS)
+      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)l0, (int32_t)(tile * TB), batch);
+    else
+      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)(tile * TB), (int32_t)l0, batch);
+  };
 
   if (t == 0) {
     prefetch_tensormap(&xmap);
-    if (RUNNING) prefetch_tensormap(&omap);
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
     fence_mbar_init();
     abort_flag = 0;
   }
   __syncthreads();
-  if (t == 0) {
-    for (int s = 0; s < S && s < n_tiles; ++s) {
-      mbar_arrive_expect_tx(&full[s], kTileBytes);
-      tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
-    }
-  }
+  if (t == 0)
+    for (int s = 0; s < S && s < n_tiles; ++s) load(s, s);
   T acc = seed.get<T>();
-  const int sw = t & 7;
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
     const int s = (int)(it % S);
     if (!mbar_wait_bounded(&full[s], (uint32_t)((it / S) & 1), NRS_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     if (abort_flag) break;
-    uint8_t* row = smem + s * kTileBytes + t * 128;
-    const int64_t x0 = it * XB;
-    const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
-    T v[XB];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], row + ((j ^ sw) << 4), 16);
-    int e0 = 0;
-    if (it == 0 && seed.first) {
-      acc = v[0];
-      e0 = 1;
-    }
-    if (cnt == XB) {
-#pragma unroll
-      for (int e = 0; e < XB; ++e) {
-        if (e >= e0) {
-          acc = apply<T, OP>(acc, v[e]);
-          v[e] = acc;
-        }
-      }
-    } else {
-      for (int e = e0; e < cnt; ++e) {
-        acc = apply<T, OP>(acc, v[e]);
-        v[e] = acc;
-      }
-    }
-    if (RUNNING) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) memcpy(row + ((j ^ sw) << 4), &v[j * PER16], 16);
-      fence_proxy_async_smem();
-    }
-    __syncthreads();
-    if (t == 0) {
-      if (RUNNING) {
-        tma_store_3d(&omap, smem + s * kTileBytes, (int32_t)x0, (int32_t)l0, batch);
-        bulk_commit();
-        const int64_t nt = it - 1 + S;
-        if (it >= 1 && nt < n_tiles) {
-          bulk_wait_read<1>();
-          const int ps = (int)((it - 1) % S);
-          mbar_arrive_expect_tx(&full[ps], kTileBytes);
-          tma_load_3d(smem + ps * kTileBytes, &xmap, &full[ps], (int32_t)(nt * XB), (int32_t)l0, batch);
-        }
-      } else if (it + S < n_tiles) {
-        mbar_arrive_expect_tx(&full[s], kTileBytes);
-        tma_load_3d(smem + s * kTileBytes, &xmap, &full[s], (int32_t)((it + S) * XB), (int32_t)l0, batch);
-      }
-    }
+    const int cnt = (int)((alen - it * TB) < TB ? (alen - it * TB) : TB);
+    const bool first = (it == 0) && seed.first;
+    if (COLS)
+      acc = fold_col<T, OP, false>(reinterpret_cast<T*>(smem + s * kTileBytes), t, cnt, first, acc);
+    else
+      acc = fold_row<T, OP, false>(smem + s * kTileBytes, t, cnt, first, acc);
+    __syncthreads();  // every thread is done with stage s
+    if (t == 0 && it + S < n_tiles) load(s, it + S);
   }
   if (abort_flag) {
     if (t == 0) {
-      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (4u << 8));
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | ((COLS ? 3u : 4u) << 8));
       for (int64_t j = it; j < n_tiles && j < it + S; ++j)
         mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
-      if (RUNNING) bulk_wait<0>();
     }
     return;
   }
-  if (RUNNING) {
-    if (t == 0) bulk_wait<0>();
-  } else {
-    const int64_t lane = l0 + t;
-    if (lane < lanes) out[(int64_t)batch * lanes + lane] = acc;
+  const int64_t lane = l0 + t;
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = acc;
+}
+
+// Running fold (accumulate) with warp-specialised roles, 96 threads:
+//  * warps 0-1 (consumers), thread t owns lane l0 + t: wait for the stage,
+//    rewrite its column / row with the prefix values, fence the writes for
+//    the TMA (async) proxy and arrive on `done[s]`;
+//  * warp 2, lane 0 (producer): keeps the ring full, TMA-stores each stage
+//    once `done[s]` completes (positions outside the array are clipped by
+//    the store) and refills a buffer only when its store has finished
+//    reading it: after committing the store of stage i it waits until at
+//    most LAG stores are still reading, then reloads the buffer of stage
+//    i - LAG with stage i - LAG + S.
+// A stage holds A consecutive 8 KB tiles along the axis (one barrier pair),
+// so a row segment moved per stage is A x 128 B for lanes along rows.
+// Every wait is bounded; a give-up sets the shared abort flag and the error
+// word, and the producer drains its outstanding copies before returning.
+// Ring shape (compile-time; measured on 16384^2 f32/f64 cumsum along both
+// axes): 3 stages of 4 tiles (96 KB, two CTAs per SM), store lag 1. Deeper
+// rings of single tiles, or a longer lag, were slower or no faster.
+#ifndef NRS_RUN_STAGES
+#define NRS_RUN_STAGES 3
+#endif
+#ifndef NRS_RUN_TILES_PER_STAGE
+#define NRS_RUN_TILES_PER_STAGE 4
+#endif
+#ifndef NRS_RUN_STORE_LAG
+#define NRS_RUN_STORE_LAG 1
+#endif
+constexpr int kRunStages = NRS_RUN_STAGES;
+constexpr int kRunTiles = NRS_RUN_TILES_PER_STAGE;
+constexpr int kStoreLag = NRS_RUN_STORE_LAG;
+static_assert(kStoreLag >= 0 && kStoreLag < kRunStages, "the ring must run ahead of the store lag");
+
+template <typename T, int OP, bool COLS>
+__global__ void __launch_bounds__(96)
+    lane_running_tma(const __grid_constant__ CUtensorMap xmap,
+                     const __grid_constant__ CUtensorMap omap, int64_t alen, uint32_t* err,
+                     Seed seed) {
+  constexpr int TB = COLS ? col_rows<T>() : 128 / (int)sizeof(T);  // axis positions per tile
+  constexpr int S = kRunStages;
+  constexpr int A = kRunTiles;
+  constexpr int STAGE = A * kTileBytes;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGE * S);
+  uint64_t* done = full + S;
+  __shared__ volatile int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * kLanesPerCta;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + TB - 1) / TB;       // 8 KB tiles along the axis
+  const int64_t n_stages = (n_tiles + A - 1) / A;      // ring steps
+  // tiles of step i inside the array
+  auto tiles_in = [&](int64_t i) { return (int)((n_tiles - i * A) < A ? (n_tiles - i * A) : A); };
+  auto xy = [&](int64_t tile, int32_t* x, int32_t* y) {
+    if (COLS) {
+      *x = (int32_t)l0;
+      *y = (int32_t)(tile * TB);
+    } else {
+      *x = (int32_t)(tile * TB);
+      *y = (int32_t)l0;
+    }
+  };
+
+  if (t == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&done[s], kLanesPerCta);
+    }
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+
+  if (t >= kLanesPerCta) {  // producer warp
+    if (t != kLanesPerCta) return;
+    prefetch_tensormap(&xmap);
+    prefetch_tensormap(&omap);
+    auto load = [&](int s, int64_t i) {
+      const int na = tiles_in(i);
+      mbar_arrive_expect_tx(&full[s], (uint32_t)(na * kTileBytes));
+      for (int a = 0; a < na; ++a) {
+        int32_t x, y;
+        xy(i * A + a, &x, &y);
+        tma_load_3d(smem + s * STAGE + a * kTileBytes, &xmap, &full[s], x, y, batch);
+      }
+    };
+    int64_t issued = 0;
+    for (; issued < S && issued < n_stages; ++issued) load((int)issued, issued);
+    bool ok = true;
+    for (int64_t i = 0; i < n_stages; ++i) {
+      const int s = (int)(i % S);
+      if (abort_flag || !mbar_wait_bounded(&done[s], (uint32_t)((i / S) & 1), NRS_WAIT_LIMIT)) {
+        ok = false;
+        break;
+      }
+      const int na = tiles_in(i);
+      for (int a = 0; a < na; ++a) {
+        int32_t x, y;
+        xy(i * A + a, &x, &y);
+        tma_store_3d(&omap, smem + s * STAGE + a * kTileBytes, x, y, batch);
+      }
+      bulk_commit();
+      const int64_t r = i - kStoreLag;  // its store has now finished reading
+      if (r >= 0 && r + S < n_stages) {
+        bulk_wait_read<kStoreLag>();
+        load((int)(r % S), r + S);
+        issued = r + S + 1;
+      }
+    }
+    if (!ok) {
+      abort_flag = 1;
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | ((COLS ? 5u : 6u) << 8));
+      // Loads issued into the ring: steps issued - S .. issued - 1.
+      for (int64_t j = (issued > S ? issued - S : 0); j < issued; ++j)
+        mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
+    }
+    bulk_wait<0>();
+    return;
+  }
+
+  // consumers
+  T acc = seed.get<T>();
+  for (int64_t i = 0; i < n_stages; ++i) {
+    const int s = (int)(i % S);
+    if (abort_flag || !mbar_wait_bounded(&full[s], (uint32_t)((i / S) & 1), NRS_WAIT_LIMIT)) {
+      abort_flag = 1;
+      return;
+    }
+    const int na = tiles_in(i);
+    for (int a = 0; a < na; ++a) {
+      const int64_t tile = i * A + a;
+      const int cnt = (int)((alen - tile * TB) < TB ? (alen - tile * TB) : TB);
+      const bool first = (tile == 0) && seed.first;
+      uint8_t* base = smem + s * STAGE + a * kTileBytes;
+      if (COLS)
+        acc = fold_col<T, OP, true>(reinterpret_cast<T*>(base), t, cnt, first, acc);
+      else
+        acc = fold_row<T, OP, true>(base, t, cnt, first, acc);
+    }
+    fence_proxy_async_smem();
+    mbar_arrive(&done[s]);
   }
 }
 
@@ -565,43 +627,39 @@ int launch_lane_tma(nrs_handle* h, const LaneProblem& p) {
   const int64_t batch = (k.n == 2) ? k.size[0] : 1;
   const int64_t bstride = (k.n == 2) ? k.xstride[0] : 0;
   if (batch > 65535) return NRS_ERR_UNSUPPORTED;
-  const size_t smem = (size_t)kTileBytes * kScanStages + 8 * kScanStages + 1024;
+  const size_t smem = (size_t)kTileBytes * kScanStages + 16 * kScanStages + 1024;
+  const bool cols = (lstride == 1 && p.xastride > 1);
+  const bool rows = (p.xastride == 1 && lstride > 1);
+  if (!cols && !rows) return NRS_ERR_UNSUPPORTED;
+  uint64_t dims[3], strides[2];
+  uint32_t box[3];
+  if (cols) {
+    dims[0] = (uint64_t)lanes; dims[1] = (uint64_t)p.alen; dims[2] = (uint64_t)batch;
+    strides[0] = (uint64_t)p.xastride * es;
+    strides[1] = (uint64_t)(batch > 1 ? bstride : p.xastride * p.alen) * es;
+    box[0] = kLanesPerCta; box[1] = col_rows<T>(); box[2] = 1;
+  } else {
+    dims[0] = (uint64_t)p.alen; dims[1] = (uint64_t)lanes; dims[2] = (uint64_t)batch;
+    strides[0] = (uint64_t)lstride * es;
+    strides[1] = (uint64_t)(batch > 1 ? bstride : lstride * lanes) * es;
+    box[0] = 128 / es; box[1] = kLanesPerCta; box[2] = 1;
+  }
+  const CUtensorMapSwizzle sw = cols ? CU_TENSOR_MAP_SWIZZLE_NONE : CU_TENSOR_MAP_SWIZZLE_128B;
   CUtensorMap xmap, omap;
-  if (lstride == 1 && p.xastride > 1) {
-    const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
-    const uint64_t sb = (uint64_t)(batch > 1 ? bstride : p.xastride * p.alen) * es;
-    const uint64_t strides[2] = {(uint64_t)p.xastride * es, sb};
-    const uint32_t box[3] = {(uint32_t)kLanesPerCta, (uint32_t)col_rows<T>(), 1};
-    if (!encode_map(&xmap, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
-      return NRS_ERR_UNSUPPORTED;
-    if (RUNNING && !encode_map(&omap, p.dtype, p.out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
-      return NRS_ERR_UNSUPPORTED;
-    if (!RUNNING) omap = xmap;
-    auto kern = lane_scan_cols_tma<T, OP, RUNNING>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((lanes + kLanesPerCta - 1) / kLanesPerCta), (unsigned)batch);
-    kern<<<grid, kLanesPerCta, smem, h->stream>>>(xmap, omap, p.alen, lanes, (T*)p.out, h->dev_error,
-                                                   p.seed);
-    return nrs_after_launch(h, "lane_scan_cols_tma");
+  if (!encode_map(&xmap, p.dtype, p.x, dims, strides, box, sw)) return NRS_ERR_UNSUPPORTED;
+  if (RUNNING && !encode_map(&omap, p.dtype, p.out, dims, strides, box, sw)) return NRS_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)((lanes + kLanesPerCta - 1) / kLanesPerCta), (unsigned)batch);
+  if (RUNNING) {
+    const size_t rsmem = (size_t)kTileBytes * kRunTiles * kRunStages + 16 * kRunStages + 1024;
+    auto kern = cols ? lane_running_tma<T, OP, true> : lane_running_tma<T, OP, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+    kern<<<grid, 96, rsmem, h->stream>>>(xmap, omap, p.alen, h->dev_error, p.seed);
+    return nrs_after_launch(h, "lane_running_tma");
   }
-  if (p.xastride == 1 && lstride > 1) {
-    const uint64_t dims[3] = {(uint64_t)p.alen, (uint64_t)lanes, (uint64_t)batch};
-    const uint64_t sb = (uint64_t)(batch > 1 ? bstride : lstride * lanes) * es;
-    const uint64_t strides[2] = {(uint64_t)lstride * es, sb};
-    const uint32_t box[3] = {(uint32_t)(128 / es), (uint32_t)kLanesPerCta, 1};
-    if (!encode_map(&xmap, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
-      return NRS_ERR_UNSUPPORTED;
-    if (RUNNING && !encode_map(&omap, p.dtype, p.out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
-      return NRS_ERR_UNSUPPORTED;
-    if (!RUNNING) omap = xmap;
-    auto kern = lane_scan_rows_tma<T, OP, RUNNING>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((lanes + kLanesPerCta - 1) / kLanesPerCta), (unsigned)batch);
-    kern<<<grid, kLanesPerCta, smem, h->stream>>>(xmap, omap, p.alen, lanes, (T*)p.out, h->dev_error,
-                                                   p.seed);
-    return nrs_after_launch(h, "lane_scan_rows_tma");
-  }
-  return NRS_ERR_UNSUPPORTED;
+  auto kern = cols ? lane_reduce_tma<T, OP, true> : lane_reduce_tma<T, OP, false>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<grid, kLanesPerCta, smem, h->stream>>>(xmap, p.alen, lanes, (T*)p.out, h->dev_error, p.seed);
+  return nrs_after_launch(h, "lane_reduce_tma");
 }
 
 template <typename T, int OP, bool RUNNING>

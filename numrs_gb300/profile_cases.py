@@ -27,6 +27,9 @@ CASES = {
     "ozaki_f64": ("f64", None, None),
     "dmma_f64": ("f64", None, None),
     "grouped": (None, None, None),
+    "cumsum_cols_f32": ("f32", "add", 0),
+    "cumsum_rows_f32": ("f32", "add", 1),
+    "cumsum_flat_f32": ("f32", "add", None),
 }
 
 
@@ -47,6 +50,10 @@ def main():
             x = torch.empty((n, n), dtype=torch.int64, device="cuda")
             K.fill_random(x, L.RNG_INT, 4, -(1 << 20), float(1 << 21))
         fn = lambda: K.reduce(x, op, axis)  # noqa: E731
+    elif a.case.startswith("cumsum"):
+        x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        fn = lambda: K.ufunc_accumulate(op, x, axis)  # noqa: E731
     elif a.case == "exp_affine_f32":
         x = torch.empty((n, n), dtype=torch.float32, device="cuda")
         K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
