@@ -30,6 +30,8 @@ CASES = {
     "cumsum_cols_f32": ("f32", "add", 0),
     "cumsum_rows_f32": ("f32", "add", 1),
     "cumsum_flat_f32": ("f32", "add", None),
+    "expr_abc_f32": ("f32", None, None),
+    "add_row_f32": ("f32", None, None),
 }
 
 
@@ -54,6 +56,18 @@ def main():
         x = torch.empty((n, n), dtype=torch.float32, device="cuda")
         K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
         fn = lambda: K.ufunc_accumulate(op, x, axis)  # noqa: E731
+    elif a.case in ("expr_abc_f32", "add_row_f32"):
+        x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        if a.case == "expr_abc_f32":
+            b, c = torch.empty_like(x), torch.empty_like(x)
+            K.fill_random(b, L.RNG_NORMAL, 4, 0.0, 1.0)
+            K.fill_random(c, L.RNG_NORMAL, 5, 0.0, 1.0)
+            E = K.Expr.leaf
+            fn = lambda: ((E(x) * E(b)) + E(c)).eval()  # noqa: E731
+        else:
+            row = x[0].clone()
+            fn = lambda: K.add(x, row)  # noqa: E731
     elif a.case == "exp_affine_f32":
         x = torch.empty((n, n), dtype=torch.float32, device="cuda")
         K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
