@@ -325,6 +325,48 @@ def scan_section(K, L):
     return out
 
 
+def io_section(K, L):
+    """NPY straight to / from device memory (io::npy_npz): a 16384x16384 f32
+    array (1 GiB) saved with save_npy and loaded with load_npy through the
+    page cache of a temporary directory, beside a single-threaded host read
+    of the same file into a host array (the shape of the reference's
+    read_exact + decode)."""
+    import tempfile
+    import numpy as np
+    import torch
+    x = torch.empty((R, C_), device="cuda")
+    K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+    nbytes = x.numel() * 4
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "x.npy")
+        K.save_npy(path, x)  # warm the page cache
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        K.save_npy(path, x)
+        torch.cuda.synchronize()
+        out["save_npy_gbs"] = round(nbytes / (time.perf_counter() - t0) / 1e9, 2)
+        K.load_npy(path)
+        torch.cuda.synchronize()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            y = K.load_npy(path)
+        torch.cuda.synchronize()
+        out["load_npy_gbs"] = round(reps * nbytes / (time.perf_counter() - t0) / 1e9, 2)
+        out["load_bit_exact"] = bool(torch.equal(x.view(torch.int32), y.view(torch.int32)))
+        t0 = time.perf_counter()
+        with open(path, "rb") as f:
+            f.seek(K.npy_info(path)["data_offset"])
+            host = np.fromfile(f, dtype=np.float32, count=R * C_)
+        out["host_read_gbs"] = round(nbytes / (time.perf_counter() - t0) / 1e9, 2)
+        del host, y
+    del x
+    torch.cuda.empty_cache()
+    out["bytes"] = nbytes
+    return out
+
+
 def grouped_section(K, L, seed: int = 7):
     """4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64) and
     4096 row reductions (length log-uniform in [64, 65536]) in one persistent
@@ -406,6 +448,7 @@ def main():
     ap.add_argument("--no-grouped", action="store_true")
     ap.add_argument("--no-elementwise", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
+    ap.add_argument("--no-io", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -584,6 +627,8 @@ def main():
         out["elementwise"] = elementwise_section(K, L)
     if rank == 0 and not args.no_scan:
         out["scan"] = scan_section(K, L)
+    if rank == 0 and not args.no_io:
+        out["io"] = io_section(K, L)
     if rank == 0 and not args.no_grouped:
         out["grouped"] = grouped_section(K, L)
     if rank == 0:

@@ -55,7 +55,8 @@ typedef enum nrs_status {
   NRS_ERR_TIMEOUT = -8,     /* a device-side bounded wait gave up          */
   NRS_ERR_ALLOC = -9,       /* workspace allocation failed                 */
   NRS_ERR_UNSUPPORTED = -10,
-  NRS_ERR_TOO_LARGE = -11   /* size beyond a documented maximum            */
+  NRS_ERR_TOO_LARGE = -11,  /* size beyond a documented maximum            */
+  NRS_ERR_IO = -12          /* a file could not be opened, read or written */
 } nrs_status;
 
 /* ---------------------------------------------------------------------- */
@@ -259,6 +260,57 @@ int nrs_ufunc_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* 
 int nrs_accumulate(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
                    const int64_t* strides, int64_t axis, const void* x, void* out,
                    const int64_t* out_strides);
+
+/* ---------------------------------------------------------------------- */
+/* NPY / NPZ files straight to and from device memory                       */
+/* ---------------------------------------------------------------------- */
+/* Replaces io::npy_npz (src/io/npy_npz.rs): the payload moves between the
+ * file and device memory through pinned staging slots (parallel pread /
+ * pwrite overlapped with cudaMemcpyAsync on the handle's stream); it never
+ * lands in a pageable host array. */
+#define NRS_NPY_MAX_DIMS 32
+
+typedef struct nrs_npy_info {
+  char descr[16];        /* the header's 'descr', e.g. "<f4"                    */
+  int dtype;             /* NRS_F32/F64/I32/I64 for <f4 <f8 <i4 <i8, else -1    */
+  int itemsize;          /* bytes per element                                   */
+  int fortran_order;     /* 1 if the header says True (the payload is moved as
+                            stored, as the reference reads it)                 */
+  int ndim;
+  int64_t shape[NRS_NPY_MAX_DIMS];
+  int64_t data_offset;   /* file offset of the first payload byte               */
+  int64_t nbytes;        /* payload bytes (prod(shape) * itemsize)               */
+} nrs_npy_info;
+
+/* Parses the NPY header that starts at file offset `offset` (0 for an .npy
+ * file, nrs_npz_locate's offset for an NPZ member) with parse_npy_header's
+ * rules (src/io/npy_npz.rs:263-339): magic, version 1.0 only
+ * (NRS_ERR_UNSUPPORTED otherwise), 'descr' and 'shape' by string search.
+ * Checks that the file holds the whole payload. `h` may be NULL (no GPU is
+ * touched; errors then have no message). */
+int nrs_npy_inspect(nrs_handle* h, const char* path, int64_t offset, nrs_npy_info* info);
+
+/* Finds NPZ member "<array_name>.npy" (load_npz_array, :541) or, with
+ * array_name NULL, the first ".npy" member (read_npz_generic, :465) through
+ * the ZIP central directory (ZIP64 included) and returns the file offset of
+ * its embedded NPY file. Compressed members return NRS_ERR_UNSUPPORTED: only
+ * stored members (what serialize_to_file writes, :369-375) are read in
+ * place. `h` may be NULL. */
+int nrs_npz_locate(nrs_handle* h, const char* path, const char* array_name, int64_t* npy_offset,
+                   int64_t* npy_bytes);
+
+/* Copies the payload described by `info` (from nrs_npy_inspect) into device
+ * memory `dst` (dst_bytes >= info->nbytes), enqueued on the handle's stream;
+ * returns once every byte has been copied. */
+int nrs_npy_read(nrs_handle* h, const char* path, const nrs_npy_info* info, void* dst,
+                 int64_t dst_bytes);
+
+/* Writes device array `src` (row-major contiguous, dtype F32/F64/I32/I64) as
+ * an NPY file with construct_npy_header's header, byte for byte
+ * (src/io/npy_npz.rs:48-99: version 1.0, no trailing newline). Returns once
+ * the file is written. */
+int nrs_npy_write(nrs_handle* h, const char* path, int dtype, int ndim, const int64_t* shape,
+                  const void* src);
 
 /* ---------------------------------------------------------------------- */
 /* GEMM                                                                     */

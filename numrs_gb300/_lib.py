@@ -16,7 +16,8 @@ LIB_PATH = os.path.join(_HERE, "libnumrs_gb300.so")
 F32, F64, I32, I64 = 0, 1, 2, 3
 OK = 0
 ERR_INVALID, ERR_SHAPE, ERR_DTYPE, ERR_AXIS, ERR_EMPTY, ERR_STRIDE = -1, -2, -3, -4, -5, -6
-ERR_CUDA, ERR_TIMEOUT, ERR_ALLOC, ERR_UNSUPPORTED, ERR_TOO_LARGE = -7, -8, -9, -10, -11
+ERR_CUDA, ERR_TIMEOUT, ERR_ALLOC, ERR_UNSUPPORTED, ERR_TOO_LARGE, ERR_IO = -7, -8, -9, -10, -11, -12
+NPY_MAX_DIMS = 32
 SUM, MEAN, MAX, MIN, PROD, VAR, STD, ARGMAX, ARGMIN = 0, 1, 2, 3, 4, 5, 6, 7, 8
 AXIS_NONE = -(2 ** 63)
 OP_INPUT, OP_SCALAR, OP_ADD, OP_SUB, OP_MUL, OP_DIV = 0, 1, 2, 3, 4, 5
@@ -25,6 +26,13 @@ GEMM_ACCUMULATE, GEMM_TRANS_A, GEMM_TRANS_B = 1, 2, 4
 GEMM_AUTO, GEMM_DMMA, GEMM_SIMT, GEMM_GENERIC, GEMM_SIMT_SMALL = 0, 1, 2, 3, 4
 RNG_UNIFORM, RNG_NORMAL, RNG_INT, RNG_OZAKI = 0, 1, 2, 3
 TILE_VARIANTS = 6
+
+
+class NpyInfo(C.Structure):
+    """nrs_npy_info."""
+    _fields_ = [("descr", C.c_char * 16), ("dtype", C.c_int), ("itemsize", C.c_int),
+                ("fortran_order", C.c_int), ("ndim", C.c_int), ("shape", C.c_int64 * NPY_MAX_DIMS),
+                ("data_offset", C.c_int64), ("nbytes", C.c_int64)]
 
 
 class UfuncOp(C.Structure):
@@ -76,6 +84,10 @@ SIGNATURES = {
     "nrs_ufunc": (_i, [_vp, _i, C.POINTER(UfuncOp), _i, _i, _P64, _i, C.POINTER(_vp), _P64, _vp, _P64]),
     "nrs_exp_affine": (_i, [_vp, _i, _i64, _vp, _d, _d, _vp]),
     "nrs_ufunc_reduce": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _vp]),
+    "nrs_npy_inspect": (_i, [_vp, C.c_char_p, _i64, C.POINTER(NpyInfo)]),
+    "nrs_npz_locate": (_i, [_vp, C.c_char_p, C.c_char_p, C.POINTER(_i64), C.POINTER(_i64)]),
+    "nrs_npy_read": (_i, [_vp, C.c_char_p, C.POINTER(NpyInfo), _vp, _i64]),
+    "nrs_npy_write": (_i, [_vp, C.c_char_p, _i, _i, _P64, _vp]),
     "nrs_accumulate": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _P64]),
     "nrs_gemm": (_i, [_vp, _i, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u, _i]),
     "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i,

@@ -1,0 +1,457 @@
+// NPY / NPZ files straight to and from device memory: io::npy_npz
+// (src/io/npy_npz.rs).
+//
+// Header rules follow the reference: parse_npy_header (:263-339) accepts
+// format version 1.0 only, takes 'descr' and 'shape' from the header dict by
+// string search and ignores 'fortran_order' (reported here, the payload is
+// moved as stored); construct_npy_header (:48-99) writes
+// {'descr': '<f4', 'fortran_order': False, 'shape': (2, 3), } padded with
+// 16 - ((len + 10) % 16) spaces and no newline. NPZ members are found the
+// way load_npz_array (:541) and read_npz_generic (:465) find them ("name.npy",
+// or the first ".npy"); only stored (uncompressed) members can be read in
+// place, as serialize_to_file writes them (:369-375).
+//
+// The payload never lands in a pageable host array: it streams through a
+// ring of pinned staging slots, each filled by parallel pread()s and sent
+// with cudaMemcpyAsync on the handle's stream while the next slot is read
+// (writing: cudaMemcpyAsync into a slot, then parallel pwrite()s while the
+// next slot comes down).
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "nrs_internal.cuh"
+
+struct nrs_host_stage {
+  static constexpr int kSlots = 4;
+  static constexpr size_t kSlotBytes = size_t(32) << 20;
+  uint8_t* buf = nullptr;  // kSlots * kSlotBytes, pinned
+  cudaEvent_t ev[kSlots] = {};
+  bool pending[kSlots] = {};
+};
+
+void nrs_stage_free(nrs_handle* h) {
+  if (!h || !h->stage) return;
+  for (int i = 0; i < nrs_host_stage::kSlots; ++i)
+    if (h->stage->ev[i]) cudaEventDestroy(h->stage->ev[i]);
+  if (h->stage->buf) cudaFreeHost(h->stage->buf);
+  delete h->stage;
+  h->stage = nullptr;
+}
+
+namespace {
+
+constexpr char kMagic[6] = {'\x93', 'N', 'U', 'M', 'P', 'Y'};
+
+int fail(nrs_handle* h, int st, const std::string& msg) { return h ? nrs_fail(h, st, msg) : st; }
+
+struct File {
+  int fd = -1;
+  ~File() {
+    if (fd >= 0) close(fd);
+  }
+};
+
+int64_t file_size(int fd) {
+  struct stat s;
+  return fstat(fd, &s) == 0 ? (int64_t)s.st_size : -1;
+}
+
+bool pread_all(int fd, void* dst, size_t n, int64_t off) {
+  uint8_t* p = static_cast<uint8_t*>(dst);
+  while (n > 0) {
+    const ssize_t r = pread(fd, p, n, off);
+    if (r <= 0) return false;
+    p += r;
+    n -= (size_t)r;
+    off += r;
+  }
+  return true;
+}
+
+bool pwrite_all(int fd, const void* src, size_t n, int64_t off) {
+  const uint8_t* p = static_cast<const uint8_t*>(src);
+  while (n > 0) {
+    const ssize_t r = pwrite(fd, p, n, off);
+    if (r <= 0) return false;
+    p += r;
+    n -= (size_t)r;
+    off += r;
+  }
+  return true;
+}
+
+int io_threads() {
+  const unsigned hc = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(8u, hc));
+}
+
+// [off, off + n) of the file <-> buf, split across threads.
+template <bool READ>
+bool parallel_io(int fd, uint8_t* buf, size_t n, int64_t off) {
+  const int nt = io_threads();
+  const size_t part = std::max<size_t>((n + nt - 1) / nt, size_t(1) << 20);
+  std::vector<std::thread> ts;
+  std::vector<char> ok((n + part - 1) / part, 1);
+  for (size_t i = 0, k = 0; i < n; i += part, ++k) {
+    const size_t len = std::min(part, n - i);
+    ts.emplace_back([&, i, k, len] {
+      ok[k] = READ ? pread_all(fd, buf + i, len, off + (int64_t)i)
+                   : pwrite_all(fd, buf + i, len, off + (int64_t)i);
+    });
+  }
+  for (auto& t : ts) t.join();
+  for (char c : ok)
+    if (!c) return false;
+  return true;
+}
+
+nrs_host_stage* stage(nrs_handle* h, int* st) {
+  *st = NRS_OK;
+  if (h->stage) return h->stage;
+  auto* s = new nrs_host_stage();
+  if (cudaHostAlloc((void**)&s->buf, nrs_host_stage::kSlots * nrs_host_stage::kSlotBytes,
+                    cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    *st = nrs_fail(h, NRS_ERR_ALLOC, "pinned staging allocation failed");
+    return nullptr;
+  }
+  for (int i = 0; i < nrs_host_stage::kSlots; ++i)
+    cudaEventCreateWithFlags(&s->ev[i], cudaEventDisableTiming);
+  h->stage = s;
+  return s;
+}
+
+// Waits for every slot's outstanding copy.
+int drain(nrs_handle* h, nrs_host_stage* s) {
+  int st = NRS_OK;
+  for (int i = 0; i < nrs_host_stage::kSlots; ++i) {
+    if (s->pending[i]) {
+      const int e = nrs_cuda_check(h, cudaEventSynchronize(s->ev[i]), "cudaEventSynchronize");
+      if (e && !st) st = e;
+      s->pending[i] = false;
+    }
+  }
+  return st;
+}
+
+// "<f4" -> (itemsize 4, NRS_F32); other fixed-size numeric or byte-string
+// descrs: their size, dtype -1; anything else (objects, datetimes,
+// structured types): itemsize 0.
+void describe(const char* descr, int* itemsize, int* dtype) {
+  *dtype = -1;
+  *itemsize = 0;
+  const size_t n = strlen(descr);
+  if (n < 3 || !strchr("<>|=", descr[0]) || !strchr("biufcSU", descr[1])) return;
+  int size = 0;
+  for (size_t i = 2; i < n; ++i) {
+    if (descr[i] < '0' || descr[i] > '9' || size > 100000000) return;
+    size = size * 10 + (descr[i] - '0');
+  }
+  *itemsize = descr[1] == 'U' ? 4 * size : size;
+  if (!strcmp(descr, "<f4")) *dtype = NRS_F32;
+  else if (!strcmp(descr, "<f8")) *dtype = NRS_F64;
+  else if (!strcmp(descr, "<i4")) *dtype = NRS_I32;
+  else if (!strcmp(descr, "<i8")) *dtype = NRS_I64;
+}
+
+const char* descr_of(int dtype) {
+  switch (dtype) {
+    case NRS_F32: return "<f4";
+    case NRS_F64: return "<f8";
+    case NRS_I32: return "<i4";
+    case NRS_I64: return "<i8";
+    default: return nullptr;
+  }
+}
+
+// parse_npy_header restated (src/io/npy_npz.rs:263-339) over the header
+// bytes `hdr` (magic .. end of dict) of a file whose NPY data starts at
+// file offset `base`.
+int parse_header(nrs_handle* h, const std::string& hdr, int64_t base, nrs_npy_info* info) {
+  if (hdr.size() < 10 || memcmp(hdr.data(), kMagic, 6) != 0)
+    return fail(h, NRS_ERR_INVALID, "Invalid NPY file: missing magic string");
+  const int major = (uint8_t)hdr[6], minor = (uint8_t)hdr[7];
+  if (major != 1 || minor != 0)
+    return fail(h, NRS_ERR_UNSUPPORTED,
+                "Unsupported NPY version: " + std::to_string(major) + "." + std::to_string(minor));
+  const size_t hl = (uint8_t)hdr[8] | ((size_t)(uint8_t)hdr[9] << 8);
+  if (hdr.size() < 10 + hl) return fail(h, NRS_ERR_INVALID, "Invalid NPY file: header too short");
+  const std::string dict = hdr.substr(10, hl);
+  size_t d = dict.find("'descr': '");
+  if (d == std::string::npos) return fail(h, NRS_ERR_INVALID, "Invalid NPY header: missing 'descr'");
+  d += strlen("'descr': '");
+  const size_t de = dict.find('\'', d);
+  if (de == std::string::npos) return fail(h, NRS_ERR_INVALID, "Invalid NPY header: malformed 'descr'");
+  const std::string descr = dict.substr(d, de - d);
+  if (descr.size() >= sizeof(info->descr))
+    return fail(h, NRS_ERR_UNSUPPORTED, "NPY descr too long: " + descr);
+  size_t sp = dict.find("'shape': (");
+  if (sp == std::string::npos) return fail(h, NRS_ERR_INVALID, "Invalid NPY header: missing 'shape'");
+  sp += strlen("'shape': (");
+  const size_t se = dict.find(')', sp);
+  if (se == std::string::npos) return fail(h, NRS_ERR_INVALID, "Invalid NPY header: malformed 'shape'");
+  const std::string shape_str = dict.substr(sp, se - sp);
+
+  memset(info, 0, sizeof(*info));
+  memcpy(info->descr, descr.c_str(), descr.size() + 1);
+  describe(info->descr, &info->itemsize, &info->dtype);
+  info->fortran_order = dict.find("'fortran_order': True") != std::string::npos;
+  int nd = 0;
+  size_t pos = 0;
+  while (pos <= shape_str.size()) {
+    size_t comma = shape_str.find(',', pos);
+    if (comma == std::string::npos) comma = shape_str.size();
+    std::string tok = shape_str.substr(pos, comma - pos);
+    const size_t a = tok.find_first_not_of(" \t"), b = tok.find_last_not_of(" \t");
+    tok = (a == std::string::npos) ? std::string() : tok.substr(a, b - a + 1);
+    if (!tok.empty()) {
+      if (nd >= NRS_NPY_MAX_DIMS) return fail(h, NRS_ERR_UNSUPPORTED, "NPY array has too many dimensions");
+      int64_t v = 0;
+      for (char c : tok) {
+        if (c < '0' || c > '9' || v > (INT64_MAX - 9) / 10)
+          return fail(h, NRS_ERR_INVALID, "Invalid shape dimension in NPY header: " + tok);
+        v = v * 10 + (c - '0');
+      }
+      info->shape[nd++] = v;
+    }
+    pos = comma + 1;
+  }
+  info->ndim = nd;
+  int64_t count = 1;
+  for (int i = 0; i < nd; ++i) count *= info->shape[i];
+  info->data_offset = base + 10 + (int64_t)hl;
+  info->nbytes = count * info->itemsize;
+  return NRS_OK;
+}
+
+uint32_t le16(const uint8_t* p) { return p[0] | (p[1] << 8); }
+uint32_t le32(const uint8_t* p) { return p[0] | (p[1] << 8) | (p[2] << 16) | ((uint32_t)p[3] << 24); }
+uint64_t le64(const uint8_t* p) { return le32(p) | ((uint64_t)le32(p + 4) << 32); }
+
+}  // namespace
+
+extern "C" int nrs_npy_inspect(nrs_handle* h, const char* path, int64_t offset, nrs_npy_info* info) {
+  if (h) h->last_error.clear();
+  if (!path || !info || offset < 0) return fail(h, NRS_ERR_INVALID, "null path/info or negative offset");
+  File f;
+  f.fd = open(path, O_RDONLY);
+  if (f.fd < 0) return fail(h, NRS_ERR_IO, std::string("cannot open ") + path);
+  std::string hdr(10, '\0');
+  if (!pread_all(f.fd, &hdr[0], 10, offset))
+    return fail(h, NRS_ERR_INVALID, "Failed to read NPY header");
+  if (memcmp(hdr.data(), kMagic, 6) != 0)
+    return fail(h, NRS_ERR_INVALID, "Invalid NPY file: missing magic string");
+  const size_t hl = (uint8_t)hdr[8] | ((size_t)(uint8_t)hdr[9] << 8);
+  hdr.resize(10 + hl);
+  if (hl && !pread_all(f.fd, &hdr[10], hl, offset + 10))
+    return fail(h, NRS_ERR_INVALID, "Failed to read NPY header data");
+  int st = parse_header(h, hdr, offset, info);
+  if (st) return st;
+  if (info->itemsize <= 0) return fail(h, NRS_ERR_UNSUPPORTED, std::string("unsupported NPY descr ") + info->descr);
+  if (file_size(f.fd) < info->data_offset + info->nbytes)
+    return fail(h, NRS_ERR_INVALID, "Failed to read NPY data: the file is shorter than its header says");
+  return NRS_OK;
+}
+
+extern "C" int nrs_npz_locate(nrs_handle* h, const char* path, const char* array_name,
+                              int64_t* npy_offset, int64_t* npy_bytes) {
+  if (h) h->last_error.clear();
+  if (!path || !npy_offset) return fail(h, NRS_ERR_INVALID, "null path/offset");
+  File f;
+  f.fd = open(path, O_RDONLY);
+  if (f.fd < 0) return fail(h, NRS_ERR_IO, std::string("cannot open ") + path);
+  const int64_t size = file_size(f.fd);
+  // End of central directory: the last 22 + comment (<= 65535) bytes.
+  const int64_t tail = std::min<int64_t>(size, 22 + 65535);
+  std::vector<uint8_t> t((size_t)tail);
+  if (tail < 22 || !pread_all(f.fd, t.data(), (size_t)tail, size - tail))
+    return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: not a ZIP archive");
+  int64_t eocd = -1;
+  for (int64_t i = tail - 22; i >= 0; --i)
+    if (le32(&t[(size_t)i]) == 0x06054b50u) {
+      eocd = i;
+      break;
+    }
+  if (eocd < 0) return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: no end of central directory");
+  const uint8_t* e = &t[(size_t)eocd];
+  uint64_t n_entries = le16(e + 10), cd_size = le32(e + 12), cd_off = le32(e + 16);
+  if (n_entries == 0xFFFF || cd_size == 0xFFFFFFFFu || cd_off == 0xFFFFFFFFu) {
+    // ZIP64: the locator sits right before the end record.
+    const int64_t loc = size - tail + eocd - 20;
+    uint8_t l[20], z[56];
+    if (loc < 0 || !pread_all(f.fd, l, 20, loc) || le32(l) != 0x07064b50u)
+      return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: bad ZIP64 locator");
+    if (!pread_all(f.fd, z, 56, (int64_t)le64(l + 8)) || le32(z) != 0x06064b50u)
+      return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: bad ZIP64 end record");
+    n_entries = le64(z + 32);
+    cd_size = le64(z + 40);
+    cd_off = le64(z + 48);
+  }
+  if ((int64_t)(cd_off + cd_size) > size) return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: bad directory");
+  std::vector<uint8_t> cd((size_t)cd_size);
+  if (cd_size && !pread_all(f.fd, cd.data(), (size_t)cd_size, (int64_t)cd_off))
+    return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: cannot read the directory");
+  const std::string want = array_name ? std::string(array_name) + ".npy" : std::string();
+  size_t p = 0;
+  for (uint64_t k = 0; k < n_entries; ++k) {
+    if (p + 46 > cd.size() || le32(&cd[p]) != 0x02014b50u)
+      return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: bad directory entry");
+    const uint32_t method = le16(&cd[p + 10]);
+    uint64_t csize = le32(&cd[p + 20]), usize = le32(&cd[p + 24]);
+    const uint32_t nlen = le16(&cd[p + 28]), xlen = le16(&cd[p + 30]), clen = le16(&cd[p + 32]);
+    uint64_t lho = le32(&cd[p + 42]);
+    if (p + 46 + nlen + xlen > cd.size()) return fail(h, NRS_ERR_INVALID, "Failed to open NPZ file: truncated entry");
+    const std::string name(reinterpret_cast<const char*>(&cd[p + 46]), nlen);
+    // ZIP64 extra field: the 64-bit values of the saturated 32-bit fields.
+    for (size_t x = p + 46 + nlen; x + 4 <= p + 46 + nlen + xlen;) {
+      const uint32_t id = le16(&cd[x]), len = le16(&cd[x + 2]);
+      if (id == 0x0001) {
+        size_t q = x + 4;
+        if (usize == 0xFFFFFFFFu && q + 8 <= x + 4 + len) { usize = le64(&cd[q]); q += 8; }
+        if (csize == 0xFFFFFFFFu && q + 8 <= x + 4 + len) { csize = le64(&cd[q]); q += 8; }
+        if (lho == 0xFFFFFFFFu && q + 8 <= x + 4 + len) { lho = le64(&cd[q]); q += 8; }
+      }
+      x += 4 + len;
+    }
+    const bool match = array_name ? (name == want)
+                                  : (name.size() >= 4 && name.compare(name.size() - 4, 4, ".npy") == 0);
+    if (match) {
+      if (method != 0)
+        return fail(h, NRS_ERR_UNSUPPORTED,
+                    "NPZ member " + name + " is compressed; only stored members load straight to the device");
+      uint8_t lh[30];
+      if (!pread_all(f.fd, lh, 30, (int64_t)lho) || le32(lh) != 0x04034b50u)
+        return fail(h, NRS_ERR_INVALID, "Failed to extract NPY file from NPZ: bad local header");
+      *npy_offset = (int64_t)lho + 30 + le16(lh + 26) + le16(lh + 28);
+      if (npy_bytes) *npy_bytes = (int64_t)usize;
+      return NRS_OK;
+    }
+    p += 46 + nlen + xlen + clen;
+  }
+  return fail(h, NRS_ERR_INVALID, array_name ? "Array '" + std::string(array_name) + "' not found in NPZ archive"
+                                             : std::string("No .npy files found in NPZ archive"));
+}
+
+extern "C" int nrs_npy_read(nrs_handle* h, const char* path, const nrs_npy_info* info, void* dst,
+                            int64_t dst_bytes) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  if (!path || !info) return nrs_fail(h, NRS_ERR_INVALID, "null path/info");
+  if (info->nbytes < 0 || info->data_offset < 0) return nrs_fail(h, NRS_ERR_INVALID, "bad info");
+  if (info->nbytes == 0) return NRS_OK;
+  if (!dst || dst_bytes < info->nbytes)
+    return nrs_fail(h, NRS_ERR_INVALID, "destination smaller than the NPY payload");
+  File f;
+  f.fd = open(path, O_RDONLY);
+  if (f.fd < 0) return nrs_fail(h, NRS_ERR_IO, std::string("cannot open ") + path);
+  if (file_size(f.fd) < info->data_offset + info->nbytes)
+    return nrs_fail(h, NRS_ERR_INVALID, "Failed to read NPY data: the file is shorter than its header says");
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  nrs_host_stage* s = stage(h, &st);
+  if (!s) return st;
+  const size_t slot_bytes = nrs_host_stage::kSlotBytes;
+  uint8_t* out = static_cast<uint8_t*>(dst);
+  int64_t c = 0;
+  for (int64_t off = 0; off < info->nbytes; off += (int64_t)slot_bytes, ++c) {
+    const int k = (int)(c % nrs_host_stage::kSlots);
+    if (s->pending[k]) {
+      if ((st = nrs_cuda_check(h, cudaEventSynchronize(s->ev[k]), "cudaEventSynchronize"))) break;
+      s->pending[k] = false;
+    }
+    const size_t len = (size_t)std::min<int64_t>((int64_t)slot_bytes, info->nbytes - off);
+    uint8_t* slot = s->buf + (size_t)k * slot_bytes;
+    if (!parallel_io<true>(f.fd, slot, len, info->data_offset + off)) {
+      st = nrs_fail(h, NRS_ERR_IO, "Failed to read NPY data");
+      break;
+    }
+    if ((st = nrs_cuda_check(h, cudaMemcpyAsync(out + off, slot, len, cudaMemcpyHostToDevice, h->stream),
+                             "cudaMemcpyAsync")))
+      break;
+    cudaEventRecord(s->ev[k], h->stream);
+    s->pending[k] = true;
+  }
+  const int d = drain(h, s);
+  return st ? st : d;
+}
+
+extern "C" int nrs_npy_write(nrs_handle* h, const char* path, int dtype, int ndim,
+                             const int64_t* shape, const void* src) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  const char* descr = descr_of(dtype);
+  if (!descr) return nrs_fail(h, NRS_ERR_DTYPE, "unsupported dtype for NPY");
+  if (!path || ndim < 0 || ndim > NRS_NPY_MAX_DIMS || (ndim && !shape))
+    return nrs_fail(h, NRS_ERR_INVALID, "bad path/ndim/shape");
+  int64_t count = 1;
+  for (int i = 0; i < ndim; ++i) {
+    if (shape[i] < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative dimension");
+    count *= shape[i];
+  }
+  const int64_t nbytes = count * (int64_t)nrs_dtype_size(dtype);
+  if (nbytes && !src) return nrs_fail(h, NRS_ERR_INVALID, "null source");
+  // construct_npy_header (src/io/npy_npz.rs:48-99)
+  std::string dict = std::string("{'descr': '") + descr + "', 'fortran_order': False, 'shape': (";
+  for (int i = 0; i < ndim; ++i) {
+    if (i > 0) dict += ", ";
+    dict += std::to_string(shape[i]);
+    if (ndim == 1) dict += ",";
+  }
+  dict += "), }";
+  dict.append(16 - ((dict.size() + 10) % 16), ' ');
+  if (dict.size() > 0xFFFF) return nrs_fail(h, NRS_ERR_UNSUPPORTED, "NPY header too long for version 1.0");
+  std::string hdr(kMagic, 6);
+  hdr += '\x01';
+  hdr += '\x00';
+  hdr += (char)(dict.size() & 0xFF);
+  hdr += (char)(dict.size() >> 8);
+  hdr += dict;
+
+  File f;
+  f.fd = open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  if (f.fd < 0) return nrs_fail(h, NRS_ERR_IO, std::string("cannot create ") + path);
+  if (!pwrite_all(f.fd, hdr.data(), hdr.size(), 0)) return nrs_fail(h, NRS_ERR_IO, "Failed to write NPY data");
+  if (nbytes == 0) return NRS_OK;
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  nrs_host_stage* s = stage(h, &st);
+  if (!s) return st;
+  const size_t slot_bytes = nrs_host_stage::kSlotBytes;
+  const int64_t n_chunks = (nbytes + (int64_t)slot_bytes - 1) / (int64_t)slot_bytes;
+  const uint8_t* in = static_cast<const uint8_t*>(src);
+  auto fetch = [&](int64_t c) {  // device -> slot c % kSlots
+    const int k = (int)(c % nrs_host_stage::kSlots);
+    const int64_t off = c * (int64_t)slot_bytes;
+    const size_t len = (size_t)std::min<int64_t>((int64_t)slot_bytes, nbytes - off);
+    int e = nrs_cuda_check(h, cudaMemcpyAsync(s->buf + (size_t)k * slot_bytes, in + off, len,
+                                              cudaMemcpyDeviceToHost, h->stream),
+                           "cudaMemcpyAsync");
+    if (!e) {
+      cudaEventRecord(s->ev[k], h->stream);
+      s->pending[k] = true;
+    }
+    return e;
+  };
+  // Keep kSlots - 1 downloads ahead of the file writes.
+  for (int64_t c = 0; c < n_chunks && c < nrs_host_stage::kSlots - 1 && !st; ++c) st = fetch(c);
+  for (int64_t c = 0; c < n_chunks && !st; ++c) {
+    const int k = (int)(c % nrs_host_stage::kSlots);
+    if ((st = nrs_cuda_check(h, cudaEventSynchronize(s->ev[k]), "cudaEventSynchronize"))) break;
+    s->pending[k] = false;
+    if (c + nrs_host_stage::kSlots - 1 < n_chunks && (st = fetch(c + nrs_host_stage::kSlots - 1))) break;
+    const int64_t off = c * (int64_t)slot_bytes;
+    const size_t len = (size_t)std::min<int64_t>((int64_t)slot_bytes, nbytes - off);
+    if (!parallel_io<false>(f.fd, s->buf + (size_t)k * slot_bytes, len, (int64_t)hdr.size() + off))
+      st = nrs_fail(h, NRS_ERR_IO, "Failed to write NPY data");
+  }
+  const int d = drain(h, s);
+  return st ? st : d;
+}

@@ -22,6 +22,7 @@ enum : uint32_t {
 };
 
 struct nrs_tuner_table;
+struct nrs_host_stage;  // pinned staging slots for file I/O (npy.cu)
 
 struct nrs_handle {
   int device = 0;
@@ -37,6 +38,8 @@ struct nrs_handle {
   nrs_tuner_table* tuner = nullptr;
   // Learned selector consulted for shapes the tuner table lacks (not owned).
   nrs_selector* selector = nullptr;
+  // Pinned staging for NPY reads/writes, allocated on first use.
+  nrs_host_stage* stage = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -49,6 +52,8 @@ void* nrs_workspace(nrs_handle* h, size_t bytes, int* status);
 size_t nrs_dtype_size(int dtype);
 // Checks launch errors right after a launch.
 int nrs_after_launch(nrs_handle* h, const char* what);
+// Frees the handle's pinned staging slots (npy.cu).
+void nrs_stage_free(nrs_handle* h);
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
 typedef CUresult (*nrs_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,

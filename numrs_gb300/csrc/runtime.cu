@@ -21,6 +21,7 @@ extern "C" const char* nrs_status_string(int s) {
     case NRS_ERR_ALLOC: return "allocation failed";
     case NRS_ERR_UNSUPPORTED: return "unsupported";
     case NRS_ERR_TOO_LARGE: return "size beyond the supported maximum";
+    case NRS_ERR_IO: return "file I/O error";
     default: return "unknown status";
   }
 }
@@ -127,6 +128,7 @@ extern "C" int nrs_destroy(nrs_handle* h) {
   if (h->dev_error) cudaFree(h->dev_error);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   nrs_tuner_free(h);
+  nrs_stage_free(h);
   delete h;
   return NRS_OK;
 }

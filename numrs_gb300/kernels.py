@@ -237,6 +237,65 @@ def cumprod(a, axis=None):
 
 
 # ---------------------------------------------------------------------------
+# NPY / NPZ (src/io/npy_npz.rs)
+# ---------------------------------------------------------------------------
+_NPY_TORCH = {L.F32: torch.float32, L.F64: torch.float64, L.I32: torch.int32, L.I64: torch.int64}
+
+
+def npy_info(path: str, offset: int = 0) -> dict:
+    """Header of the NPY file at `offset` (parse_npy_header's rules); touches
+    no GPU."""
+    lib = L.load()
+    info = L.NpyInfo()
+    L.check(lib.nrs_npy_inspect(None, str(path).encode(), int(offset), C.byref(info)))
+    return {"descr": info.descr.decode(), "dtype": info.dtype, "itemsize": info.itemsize,
+            "fortran_order": bool(info.fortran_order), "shape": tuple(info.shape[:info.ndim]),
+            "data_offset": info.data_offset, "nbytes": info.nbytes}
+
+
+def _load_at(path: str, offset: int, device) -> torch.Tensor:
+    lib = L.load()
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    h = handle(dev.index)
+    info = L.NpyInfo()
+    L.check(lib.nrs_npy_inspect(h, str(path).encode(), int(offset), C.byref(info)), h)
+    if info.dtype not in _NPY_TORCH:
+        raise L.NumRs2Error(L.ERR_DTYPE, f"NPY descr {info.descr.decode()!r} is not f32/f64/i32/i64")
+    out = torch.empty(tuple(info.shape[:info.ndim]), dtype=_NPY_TORCH[info.dtype], device=dev)
+    L.check(lib.nrs_npy_read(h, str(path).encode(), C.byref(info), _ptr(out), info.nbytes), h)
+    return out
+
+
+def load_npy(path: str, device=None) -> torch.Tensor:
+    """io::npy_npz read_npy_generic (src/io/npy_npz.rs:390): the file's array
+    straight into device memory."""
+    return _load_at(path, 0, device)
+
+
+def load_npz(path: str, name: str | None = None, device=None) -> torch.Tensor:
+    """load_npz_array (src/io/npy_npz.rs:541): member `name`.npy (or, with no
+    name, the first .npy member as read_npz_generic does); stored members
+    only."""
+    lib = L.load()
+    off = C.c_int64()
+    L.check(lib.nrs_npz_locate(None, str(path).encode(), None if name is None else name.encode(),
+                               C.byref(off), None))
+    return _load_at(path, off.value, device)
+
+
+def save_npy(path: str, t: torch.Tensor) -> None:
+    """serialize_to_file(..., Npy) (src/io/npy_npz.rs:342): construct_npy_header
+    then the row-major payload, written from device memory."""
+    _need_cuda(t)
+    if not t.is_contiguous():
+        raise L.NumRs2Error(L.ERR_STRIDE, "save_npy needs a contiguous array")
+    lib = L.load()
+    h = handle(t.device.index)
+    L.check(lib.nrs_npy_write(h, str(path).encode(), dtype_code(t), t.dim(), L.i64_array(t.shape),
+                              _ptr(t)), h)
+
+
+# ---------------------------------------------------------------------------
 # GEMM
 # ---------------------------------------------------------------------------
 def _mat_strides(t: torch.Tensor):
