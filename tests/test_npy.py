@@ -158,7 +158,7 @@ def test_npz_locate(tmp_path):
                                          (np.float32, (9000, 1000 + 7))])
 def test_load_numpy_files_bit_exact(K, tmp_path, dtype, shape):
     r = np.random.default_rng(1)
-    a = (r.standard_normal(shape) * 1e3).astype(dtype)
+    a = np.asarray((r.standard_normal(shape) * 1e3).astype(dtype))
     p = tmp_path / "a.npy"
     np.save(p, a)
     t = K.load_npy(p)
@@ -174,7 +174,7 @@ def test_load_numpy_files_bit_exact(K, tmp_path, dtype, shape):
 def test_save_matches_reference_writer(K, tmp_path, dtype, shape):
     import torch
     r = np.random.default_rng(2)
-    a = (r.standard_normal(shape) * 1e3).astype(dtype)
+    a = np.asarray((r.standard_normal(shape) * 1e3).astype(dtype))
     p = tmp_path / "s.npy"
     K.save_npy(p, torch.from_numpy(a).cuda())
     want = ON.construct_npy_header(np.dtype(dtype).str, list(shape)) + a.tobytes()
