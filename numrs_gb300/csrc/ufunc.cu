@@ -168,6 +168,8 @@ __device__ __forceinline__ void binary_vec(int code, const T (&lhs)[W], T (&acc)
 // program reaches, so a shallow program holds only D - 1 slots in registers.
 template <typename T, int D>
 struct ProgEval {
+  // 16-byte vectors per thread step in the vector kernels (register budget).
+  static constexpr int kUnroll = D <= 4 ? 2 : 1;
   Prog prog;
   template <int W>
   __device__ __forceinline__ void run(const T (&in)[kMaxIn][W], T (&res)[W]) const {
@@ -201,6 +203,7 @@ struct ProgEval {
 // `inputs[0] op inputs[1]`: the operators and binary closures.
 template <typename T, int OP>
 struct BinEval {
+  static constexpr int kUnroll = 4;
   template <int W>
   __device__ __forceinline__ void run(const T (&in)[kMaxIn][W], T (&res)[W]) const {
 #pragma unroll
@@ -290,23 +293,34 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int k = 0; k < kMaxIn; ++k)
       bcast[k] = (k < g.n_inputs && g.in_stride[k][last] == 0) ? static_cast<const T*>(g.in[k])[off[k]] : T(0);
-    for (int64_t j = threadIdx.x; j < nv; j += blockDim.x) {
-      T x[kMaxIn][PER];
+    // U vectors per thread step, all loads issued before any compute.
+    constexpr int U = Eval::kUnroll;
+    for (int64_t j = threadIdx.x; j < nv; j += (int64_t)blockDim.x * U) {
+      T x[U][kMaxIn][PER];
 #pragma unroll
-      for (int k = 0; k < kMaxIn; ++k) {
-        if (k < g.n_inputs && g.in_stride[k][last] != 0) {
-          const V q = __ldcs(reinterpret_cast<const V*>(static_cast<const T*>(g.in[k]) + off[k]) + j);
-          memcpy(x[k], &q, 16);
-        } else {
+      for (int u = 0; u < U; ++u) {
+        const int64_t jj = j + (int64_t)u * blockDim.x;
 #pragma unroll
-          for (int e = 0; e < PER; ++e) x[k][e] = bcast[k];
+        for (int k = 0; k < kMaxIn; ++k) {
+          if (jj < nv && k < g.n_inputs && g.in_stride[k][last] != 0) {
+            const V q = __ldcs(reinterpret_cast<const V*>(static_cast<const T*>(g.in[k]) + off[k]) + jj);
+            memcpy(x[u][k], &q, 16);
+          } else {
+#pragma unroll
+            for (int e = 0; e < PER; ++e) x[u][k][e] = bcast[k];
+          }
         }
       }
-      T res[PER];
-      ev.template run<PER>(x, res);
-      V q;
-      memcpy(&q, res, 16);
-      __stcs(reinterpret_cast<V*>(out + ooff) + j, q);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t jj = j + (int64_t)u * blockDim.x;
+        if (jj >= nv) break;
+        T res[PER];
+        ev.template run<PER>(x[u], res);
+        V q;
+        memcpy(&q, res, 16);
+        __stcs(reinterpret_cast<V*>(out + ooff) + jj, q);
+      }
     }
   }
 }
@@ -319,24 +333,36 @@ __global__ void __launch_bounds__(256)
   using V = typename std::conditional<sizeof(T) == 4, int4, longlong2>::type;
   constexpr int PER = 16 / sizeof(T);
   const int64_t nv = n / PER;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv; i += stride) {
-    T x[kMaxIn][PER];
+  // A block covers U * blockDim consecutive vectors per step (coalesced for
+  // each u); all loads are issued before any compute.
+  constexpr int U = Eval::kUnroll;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * U;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x * U + threadIdx.x; i < nv; i += step) {
+    T x[U][kMaxIn][PER];
 #pragma unroll
-    for (int k = 0; k < kMaxIn; ++k) {
-      if (k < g.n_inputs) {
-        const V q = __ldcs(reinterpret_cast<const V*>(g.in[k]) + i);
-        memcpy(x[k], &q, 16);
-      } else {
+    for (int u = 0; u < U; ++u) {
+      const int64_t ii = i + (int64_t)u * blockDim.x;
 #pragma unroll
-        for (int e = 0; e < PER; ++e) x[k][e] = T(0);
+      for (int k = 0; k < kMaxIn; ++k) {
+        if (ii < nv && k < g.n_inputs) {
+          const V q = __ldcs(reinterpret_cast<const V*>(g.in[k]) + ii);
+          memcpy(x[u][k], &q, 16);
+        } else {
+#pragma unroll
+          for (int e = 0; e < PER; ++e) x[u][k][e] = T(0);
+        }
       }
     }
-    T res[PER];
-    ev.template run<PER>(x, res);
-    V q;
-    memcpy(&q, res, 16);
-    __stcs(reinterpret_cast<V*>(out) + i, q);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t ii = i + (int64_t)u * blockDim.x;
+      if (ii >= nv) break;
+      T res[PER];
+      ev.template run<PER>(x[u], res);
+      V q;
+      memcpy(&q, res, 16);
+      __stcs(reinterpret_cast<V*>(out) + ii, q);
+    }
   }
   // scalar tail (< PER elements)
   const int64_t t = nv * PER + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -462,7 +488,8 @@ int launch_eval(nrs_handle* h, const Eval& ev, const Geometry& g, int64_t n, Acc
   if (n == 0) return NRS_OK;
   const int cap = h->num_sms * 8;
   if (acc == Access::kFlat) {
-    const int64_t need = (n / (16 / (int64_t)sizeof(T)) + 255) / 256 + 1;
+    const int64_t per_block = 256 * (int64_t)Eval::kUnroll;
+    const int64_t need = (n / (16 / (int64_t)sizeof(T)) + per_block - 1) / per_block + 1;
     const int grid = (int)(need < cap ? need : cap);
     ufunc_flat_vec<T, Eval><<<grid, 256, 0, h->stream>>>(ev, g, n, (T*)out);
     return nrs_after_launch(h, "ufunc_flat_vec");
