@@ -8,12 +8,12 @@
 // 1. Scaling: e_a[i] = frexp exponent of max_k |a_ik| (|a_ik| < 2^e_a[i]),
 //    e_b[j] likewise over column j of B. Powers of two: exact.
 // 2. Slicing: x = a_ik * 2^-e_a[i] in (-1, 1) becomes the 126-bit fixed-point
-//    integer X = round(x * 2^126), split into signed digits by
-//    round-to-nearest: digit 0 = round(X / 2^121), then digit t =
-//    round(rest / 2^(121 - 6t)). Every digit lies in [-32, 32], exactly
-//    representable in BF16, and x = sum_t digit_t * 2^-(5 + 6t) up to
-//    2^-(6 + 6(S-1)). Slices are stored K-major ([S][rows][kpad] bf16) for
-//    A and for B^T (the B slicer transposes through shared memory).
+//    integer X = round(x * 2^126), split into S signed 6-bit digits whose
+//    weighted sum is X rounded to the nearest multiple of 2^(121 - 6(S-1)):
+//    each digit lies in [-32, 32], exactly representable in BF16, and
+//    x = sum_t digit_t * 2^-(5 + 6t) up to 2^-(6 + 6(S-1)). Slices are stored
+//    K-major ([S][rows][kpad] bf16) for A and for B^T (the B slicer
+//    transposes through shared memory).
 // 3. Products: for every slice pair (s, t) with s + t <= S-1 (the pairs
 //    whose weight 2^-(10 + 6(s+t)) matters), P = A_s * B_t^T on the tensor
 //    cores with FP32 accumulation. |digit products| <= 2^10, so every partial
@@ -36,6 +36,7 @@
 //                 splitting the 256 columns) into int32 diagonal sums.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
 // word, drains its own copies and MMAs (bounded), frees TMEM and returns.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -467,8 +468,8 @@ __global__ void exponents_from_bits(const unsigned long long* __restrict__ mx, i
   e[i] = ((b >> 52) == 0) ? -1021 : (int)(b >> 52) - 1022;
 }
 
-// Signed 6-bit digits of x * 2^-e (|x| < 2^e): see the file header.
-__device__ __forceinline__ void digits(double x, int e, int S, int16_t* out) {
+// X = round(x * 2^(126 - e)) as a signed 128-bit integer (|x| < 2^e).
+__device__ __forceinline__ __int128 fixed126(double x, int e) {
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const bool neg = bits >> 63;
   const int biased = (int)((bits >> 52) & 0x7FF);
@@ -480,7 +481,6 @@ __device__ __forceinline__ void digits(double x, int e, int S, int16_t* out) {
     mant |= 1ULL << 52;
     E = biased - 1023 - 52;  // x = mant * 2^E
   }
-  // X = x * 2^(126 - e) = mant * 2^(E + 126 - e)
   const int sh = E + 126 - e;
   __int128 X;
   if (mant == 0) {
@@ -492,62 +492,102 @@ __device__ __forceinline__ void digits(double x, int e, int S, int16_t* out) {
   } else {
     X = 0;
   }
-  if (neg) X = -X;
-  int p = 121;
-  for (int t = 0; t < S; ++t, p -= OZ_DIGIT_BITS) {
-    const __int128 d = (X + ((__int128)1 << (p - 1))) >> p;  // round to nearest (ties up)
-    X -= d << p;
-    out[t] = (int16_t)d;
+  return neg ? -X : X;
+}
+
+// Signed 6-bit digits of X at positions p_t = 121 - 6t, t < S, with
+//   sum_t d_t 2^p_t = X rounded to the nearest multiple of 2^p_(S-1) (ties up).
+// Z = X + 32 * sum_t 2^p_t + 2^(p_(S-1) - 1) makes every 6-bit field of Z the
+// digit plus 32, so each digit is one shift and mask: d_t in [-32, 31] for
+// t >= 1, the top digit (Z >> 121) - 32 in [-32, 32]. Every digit is exact in
+// BF16 and |d_s d_t| <= 2^10, as the file header requires.
+// Z is unsigned: X + C lies in (0, 2^127 + 2^122), beyond the signed range.
+__device__ __forceinline__ unsigned __int128 digit_offset(int S) {
+  unsigned __int128 c = (unsigned __int128)1 << (121 - OZ_DIGIT_BITS * (S - 1) - 1);
+  for (int t = 0; t < S; ++t) c += (unsigned __int128)32 << (121 - OZ_DIGIT_BITS * t);
+  return c;
+}
+__device__ __forceinline__ int digit_at(unsigned __int128 Z, int t) {
+  const int p = 121 - OZ_DIGIT_BITS * t;
+  const int f = (int)(uint32_t)(uint64_t)(Z >> p);
+  return (t == 0 ? f : (f & 63)) - 32;
+}
+
+__device__ __forceinline__ uint32_t bf16_of_int(int v) {
+  // |v| <= 32: exact in bf16; its fp32 bit pattern's top half.
+  return __float_as_uint((float)v) >> 16;
+}
+
+// A (m x k) -> slices [S][m][kpad], K-major; zero beyond k. A thread takes 8
+// consecutive k of one row (kpad is a multiple of 8) and writes one 16-byte
+// vector per slice.
+__global__ void __launch_bounds__(256)
+    slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda, int64_t kpad,
+               const int* __restrict__ ea, int S, uint16_t* __restrict__ out) {
+  const int64_t gpr = kpad / 8;
+  const int64_t total = m * gpr;
+  const unsigned __int128 C = digit_offset(S);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = g / gpr, j0 = (g - i * gpr) * 8;
+    const int e = ea[i];
+    uint32_t pk[OZ_MAX_SLICES][4];
+#pragma unroll
+    for (int t = 0; t < OZ_MAX_SLICES; ++t) pk[t][0] = pk[t][1] = pk[t][2] = pk[t][3] = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int64_t j = j0 + q;
+      const unsigned __int128 Z = (unsigned __int128)(j < k ? fixed126(A[i * lda + j], e) : (__int128)0) + C;
+#pragma unroll
+      for (int t = 0; t < OZ_MAX_SLICES; ++t)
+        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at(Z, t)) << (16 * (q & 1));
+    }
+    uint16_t* o = out + i * kpad + j0;
+#pragma unroll
+    for (int t = 0; t < OZ_MAX_SLICES; ++t)
+      if (t < S)
+        *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
   }
 }
 
-__device__ __forceinline__ uint16_t bf16_of_int(int v) {
-  // |v| <= 32: exact in bf16; build it from the fp32 bit pattern.
-  const float f = (float)v;
-  return (uint16_t)(__float_as_uint(f) >> 16);
-}
-
-// A (m x k) -> slices [S][m][kpad], K-major; zero beyond k.
-__global__ void slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda,
-                           int64_t kpad, const int* __restrict__ ea, int S,
-                           uint16_t* __restrict__ out) {
-  const int64_t total = m * kpad;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = idx / kpad, j = idx % kpad;
-    int16_t d[OZ_MAX_SLICES];
-    if (j < k) {
-      digits(A[i * lda + j], ea[i], S, d);
-    } else {
-      for (int t = 0; t < S; ++t) d[t] = 0;
+// B (k x n row-major) -> slices of B^T [S][n][kpad]. A block takes 64 k x 32 n:
+// thread (nn = tid % 32, kk pair) reads B coalesced along n, packs the digits
+// of two consecutive k into one 32-bit word of a shared tile [S][32 n][33
+// words] (the pad word keeps both phases free of bank conflicts), then every
+// thread writes one 16-byte vector (8 k of one n row) per slice.
+constexpr int kSliceColK = 64, kSliceColN = 32, kSliceColPitch = kSliceColK / 2 + 1;
+__global__ void __launch_bounds__(256)
+    slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb, int64_t kpad,
+               const int* __restrict__ eb, int S, uint16_t* __restrict__ out) {
+  extern __shared__ uint32_t tile[];  // [S][32][33]
+  const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const unsigned __int128 C = digit_offset(S);
+  {
+    const int64_t nn = n0 + tx;
+    const int e = nn < n ? eb[nn] : 0;
+#pragma unroll
+    for (int r = 0; r < kSliceColK / 16; ++r) {  // word column w = ty + 8r: k rows 2w, 2w+1
+      const int w = ty + 8 * r;
+      const int64_t kk = k0 + 2 * w;
+      const unsigned __int128 Z0 =
+          (unsigned __int128)(kk < k && nn < n ? fixed126(B[kk * ldb + nn], e) : (__int128)0) + C;
+      const unsigned __int128 Z1 =
+          (unsigned __int128)(kk + 1 < k && nn < n ? fixed126(B[(kk + 1) * ldb + nn], e) : (__int128)0) + C;
+      for (int t = 0; t < S; ++t)
+        tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+            bf16_of_int(digit_at(Z0, t)) | (bf16_of_int(digit_at(Z1, t)) << 16);
     }
-    for (int t = 0; t < S; ++t) out[(int64_t)t * m * kpad + idx] = bf16_of_int(d[t]);
-  }
-}
-
-// B (k x n row-major) -> slices of B^T [S][n][kpad], transposed through a
-// 32 x 32 shared tile so both the read of B and the write of B^T coalesce.
-__global__ void slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
-                           int64_t kpad, const int* __restrict__ eb, int S,
-                           uint16_t* __restrict__ out) {
-  __shared__ uint16_t tile[OZ_MAX_SLICES][32][33];
-  const int64_t k0 = (int64_t)blockIdx.y * 32, n0 = (int64_t)blockIdx.x * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
-  for (int r = ty; r < 32; r += 8) {
-    const int64_t kk = k0 + r, nn = n0 + tx;
-    int16_t d[OZ_MAX_SLICES];
-    if (kk < k && nn < n) {
-      digits(B[kk * ldb + nn], eb[nn], S, d);
-    } else {
-      for (int t = 0; t < S; ++t) d[t] = 0;
-    }
-    for (int t = 0; t < S; ++t) tile[t][r][tx] = bf16_of_int(d[t]);
   }
   __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int64_t nn = n0 + r, kk = k0 + tx;
-    if (nn < n && kk < kpad)
-      for (int t = 0; t < S; ++t) out[(int64_t)t * n * kpad + nn * kpad + kk] = tile[t][tx][r];
+  const int r = threadIdx.x >> 3, c = threadIdx.x & 7;  // n row, 16-byte chunk (8 k)
+  const int64_t nn = n0 + r, kk = k0 + c * 8;
+  if (nn < n && kk < kpad) {
+    for (int t = 0; t < S; ++t) {
+      const uint32_t* src = tile + (t * kSliceColN + r) * kSliceColPitch + c * 4;
+      *reinterpret_cast<uint4*>(out + (int64_t)t * n * kpad + nn * kpad + kk) =
+          make_uint4(src[0], src[1], src[2], src[3]);
+    }
   }
 }
 
@@ -622,10 +662,18 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   col_max_bits<<<dim3((unsigned)((n + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip)), 256, 0,
                  s>>>(B, k, n, ldb, colmax);
   exponents_from_bits<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(colmax, n, eb);
-  int grid = h->num_sms * 8;
+  const int64_t groups = m * (kpad / 8);
+  const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
   slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
-  dim3 g2((unsigned)((n + 31) / 32), (unsigned)((kpad + 31) / 32));
-  slice_cols<<<g2, 256, 0, s>>>(B, k, n, ldb, kpad, eb, S, sb);
+  const size_t col_smem = (size_t)S * kSliceColN * kSliceColPitch * 4;
+  static bool col_attr = false;
+  if (!col_attr) {
+    cudaFuncSetAttribute(slice_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((size_t)OZ_MAX_SLICES * kSliceColN * kSliceColPitch * 4));
+    col_attr = true;
+  }
+  dim3 g2((unsigned)((n + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
+  slice_cols<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, sb);
   if ((st = nrs_after_launch(h, "ozaki slicing"))) return st;
 
   CUtensorMap mapA, mapB;
