@@ -255,6 +255,9 @@ def gemm_section(K, L, quick: bool):
     AB = torch.empty_like(A)
     flops = 2.0 * n ** 3
     res = {}
+    # the library's default slice count (equal error with FP64 for phi = 0)
+    z = torch.zeros((8, 8), dtype=torch.float64, device="cuda")
+    s0 = K.gemm_ozaki(z, z)[1]["slices"]
     for phi in (0.0, 1.0, 4.0):
         K.fill_random(A, L.RNG_OZAKI, 5, phi, 0.0)
         K.fill_random(B, L.RNG_OZAKI, 6, phi, 0.0)
@@ -263,7 +266,7 @@ def gemm_section(K, L, quick: bool):
         torch.abs(B, out=Ba)
         K.gemm_2d(n, n, n, Aa, Ba, AB, variant=L.GEMM_DMMA)
         entry = {"dmma_ms": round(ms_d, 2), "dmma_tflops": round(flops / ms_d / 1e9, 3), "ozaki": []}
-        for s in ((7, 9, 11) if phi == 0.0 else (9, 12, 14, 16)):
+        for s in ((s0 - 1, s0, s0 + 2) if phi == 0.0 else (s0, s0 + 3, s0 + 5, min(s0 + 7, 16))):
             ms_o = _time_ms(lambda: K.gemm_ozaki(A, B, slices=s, out=Co), 2, stream)
             err = float(((Co - Cd).abs() / AB.clamp_min(1e-300)).max())
             entry["ozaki"].append({"slices": s, "ms": round(ms_o, 2), "tflops": round(flops / ms_o / 1e9, 2),

@@ -8,22 +8,22 @@
 // 1. Scaling: e_a[i] = frexp exponent of max_k |a_ik| (|a_ik| < 2^e_a[i]),
 //    e_b[j] likewise over column j of B. Powers of two: exact.
 // 2. Slicing: x = a_ik * 2^-e_a[i] in (-1, 1) becomes the 126-bit fixed-point
-//    integer X = round(x * 2^126), split into S signed 6-bit digits whose
-//    weighted sum is X rounded to the nearest multiple of 2^(121 - 6(S-1)):
-//    each digit lies in [-32, 32], exactly representable in BF16, and
-//    x = sum_t digit_t * 2^-(5 + 6t) up to 2^-(6 + 6(S-1)). Slices are stored
-//    K-major ([S][rows][kpad] bf16) for A and for B^T (the B slicer
-//    transposes through shared memory).
+//    integer X = round(x * 2^126), split into S signed b-bit digits
+//    (b = OZ_DIGIT_BITS = 7) whose weighted sum is X rounded to the nearest
+//    multiple of 2^(127 - b - b(S-1)): each digit lies in [-2^(b-1), 2^(b-1)],
+//    exactly representable in BF16, and x = sum_t digit_t * 2^-(b - 1 + bt)
+//    up to 2^-(bS). Slices are stored K-major ([S][rows][kpad] bf16) for A
+//    and for B^T (the B slicer transposes through shared memory).
 // 3. Products: for every slice pair (s, t) with s + t <= S-1 (the pairs
-//    whose weight 2^-(10 + 6(s+t)) matters), P = A_s * B_t^T on the tensor
-//    cores with FP32 accumulation. |digit products| <= 2^10, so every partial
-//    sum of a K <= 16384 chunk is an integer below 2^24: the FP32
-//    accumulation is EXACT.
+//    whose weight 2^-(2b - 2 + b(s+t)) matters), P = A_s * B_t^T on the
+//    tensor cores with FP32 accumulation. |digit products| <= 2^(2b-2), so
+//    every partial sum of a K <= 2^(26-2b) chunk (4096 for b = 7) is an
+//    integer of at most 2^24: the FP32 accumulation is EXACT.
 // 4. Cross-slice accumulation: the exact products of one diagonal
-//    (s + t = d) are summed in int32 registers, then added once per diagonal
-//    into a per-element 128-bit integer at weight 2^(6(S-1-d)) -- exact, no
-//    FP64 op -- and the most significant diagonal converts the total once to
-//    f64 and applies 2^(e_a[i] + e_b[j] - 10 - 6(S-1)).
+//    (s + t = d) are summed as int32, then added once per diagonal into a
+//    per-element 128-bit integer at weight 2^(b(S-1-d)) -- exact, no FP64
+//    op -- and the most significant diagonal converts the total once to f64
+//    and applies 2^(e_a[i] + e_b[j] + 2 - 2b - b(S-1)).
 //
 // The tensor-core kernel is persistent (one CTA per SM) and warp-specialised:
 //   warp 0      : TMA producer, 4-stage ring of A (128x64) + B (256x64) bf16
@@ -43,6 +43,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 
 #include "nrs_internal.cuh"
 
@@ -60,9 +61,19 @@ constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 32 KB
 constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
 constexpr int OZ_THREADS = 320;                 // 10 warps: TMA, MMA, 8 epilogue
 constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
-constexpr int OZ_KCHUNK = 16384;                // exact fp32 accumulation bound
+// Signed digits of OZ_DIGIT_BITS bits: |digit| <= 2^(b-1), exact in BF16
+// (8-bit significand) for b <= 8; products <= 2^(2b-2), so a K chunk of
+// 2^(26-2b) sums exactly in FP32 (< 2^24 + 1). 7-bit digits need S = 8 for
+// 56 bits (36 slice pairs) where 6-bit digits need S = 9 (45 pairs).
+#ifndef NRS_OZ_DIGIT_BITS
+#define NRS_OZ_DIGIT_BITS 7
+#endif
+constexpr int OZ_DIGIT_BITS = NRS_OZ_DIGIT_BITS;
+static_assert(OZ_DIGIT_BITS >= 4 && OZ_DIGIT_BITS <= 8, "digits must stay exact in BF16");
+constexpr int OZ_KCHUNK = 1 << (26 - 2 * OZ_DIGIT_BITS);  // exact fp32 accumulation bound
+constexpr int OZ_TOP = 127 - OZ_DIGIT_BITS;               // position of the top digit in X
+constexpr int OZ_DEFAULT_SLICES = (54 + OZ_DIGIT_BITS - 1) / OZ_DIGIT_BITS;
 constexpr int OZ_MAX_SLICES = 16;
-constexpr int OZ_DIGIT_BITS = 6;
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 
 
@@ -185,7 +196,7 @@ struct OzParams {
   __int128* acc;   // m x n exact accumulators
   double* C;
   int64_t ldc;
-  int final_shift; // -10 - 6(S-1)
+  int final_shift; // 2 - 2b - b(S-1) for b-bit digits
   uint32_t* err;
 };
 
@@ -528,26 +539,29 @@ __device__ __forceinline__ __int128 fixed126(double x, int e) {
   return neg ? -X : X;
 }
 
-// Signed 6-bit digits of X at positions p_t = 121 - 6t, t < S, with
+// Signed b-bit digits (b = OZ_DIGIT_BITS) of X at positions
+// p_t = OZ_TOP - b t, t < S, with
 //   sum_t d_t 2^p_t = X rounded to the nearest multiple of 2^p_(S-1) (ties up).
-// Z = X + 32 * sum_t 2^p_t + 2^(p_(S-1) - 1) makes every 6-bit field of Z the
-// digit plus 32, so each digit is one shift and mask: d_t in [-32, 31] for
-// t >= 1, the top digit (Z >> 121) - 32 in [-32, 32]. Every digit is exact in
-// BF16 and |d_s d_t| <= 2^10, as the file header requires.
+// Z = X + h * sum_t 2^p_t + 2^(p_(S-1) - 1), h = 2^(b-1), makes every b-bit
+// field of Z the digit plus h, so each digit is one shift and mask: d_t in
+// [-h, h - 1] for t >= 1, the top digit (Z >> OZ_TOP) - h in [-h, h]. Every
+// digit is exact in BF16 and |d_s d_t| <= 2^(2b-2), as the file header
+// requires.
 // Z is unsigned: X + C lies in (0, 2^127 + 2^122), beyond the signed range.
 __device__ __forceinline__ unsigned __int128 digit_offset(int S) {
-  unsigned __int128 c = (unsigned __int128)1 << (121 - OZ_DIGIT_BITS * (S - 1) - 1);
-  for (int t = 0; t < S; ++t) c += (unsigned __int128)32 << (121 - OZ_DIGIT_BITS * t);
+  unsigned __int128 c = (unsigned __int128)1 << (OZ_TOP - OZ_DIGIT_BITS * (S - 1) - 1);
+  for (int t = 0; t < S; ++t)
+    c += (unsigned __int128)(1u << (OZ_DIGIT_BITS - 1)) << (OZ_TOP - OZ_DIGIT_BITS * t);
   return c;
 }
 __device__ __forceinline__ int digit_at(unsigned __int128 Z, int t) {
-  const int p = 121 - OZ_DIGIT_BITS * t;
+  const int p = OZ_TOP - OZ_DIGIT_BITS * t;
   const int f = (int)(uint32_t)(uint64_t)(Z >> p);
-  return (t == 0 ? f : (f & 63)) - 32;
+  return (t == 0 ? f : (f & ((1 << OZ_DIGIT_BITS) - 1))) - (1 << (OZ_DIGIT_BITS - 1));
 }
 
 __device__ __forceinline__ uint32_t bf16_of_int(int v) {
-  // |v| <= 32: exact in bf16; its fp32 bit pattern's top half.
+  // |v| <= 2^(b-1) <= 128: exact in bf16; its fp32 bit pattern's top half.
   return __float_as_uint((float)v) >> 16;
 }
 
@@ -649,21 +663,22 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
     return nrs_fail(h, NRS_ERR_SHAPE, "leading dimension too small");
   if (slices < 0 || slices > OZ_MAX_SLICES)
     return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
-  const int S = slices == 0 ? 9 : slices;
+  const int S = slices == 0 ? OZ_DEFAULT_SLICES : slices;
   const int64_t kpad = ((k + 7) / 8) * 8;
   const int kchunks = (int)((kpad + OZ_KCHUNK - 1) / OZ_KCHUNK);
   const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
-  // A diagonal's int32 register sum holds at most kchunks * S products of
+  // A diagonal's int32 sum holds at most kchunks * S chunk sums of
   // magnitude <= 2^24 each: keep it below 2^31.
   if ((int64_t)kchunks * S >= 128)
-    return nrs_fail(h, NRS_ERR_TOO_LARGE, "k too large for this slice count (k * S < 128 * 16384)");
+    return nrs_fail(h, NRS_ERR_TOO_LARGE,
+                    "k too large for this slice count (ceil(k / " + std::to_string(OZ_KCHUNK) + ") * S must be < 128)");
   if (info) {
     info->slices = S;
     info->products = n_pairs;
     info->slice_bits = OZ_DIGIT_BITS;
     info->k_chunk = OZ_KCHUNK;
     // truncation of both operands: 2 * 2^-(6 + 6(S-1)) relative to rowmax*colmax per term
-    info->est_rel_error = std::ldexp(2.0, -(6 + OZ_DIGIT_BITS * (S - 1)));
+    info->est_rel_error = std::ldexp(2.0, -OZ_DIGIT_BITS * S);
   }
   if (m == 0 || n == 0) return NRS_OK;
   if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
@@ -729,7 +744,7 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   P.acc = acc;
   P.C = C;
   P.ldc = ldc;
-  P.final_shift = -10 - OZ_DIGIT_BITS * (S - 1);
+  P.final_shift = 2 - 2 * OZ_DIGIT_BITS - OZ_DIGIT_BITS * (S - 1);
   P.err = h->dev_error;
   static bool attr_set = false;
   if (!attr_set) {

@@ -40,7 +40,7 @@ def main():
     ap.add_argument("--case", required=True, choices=sorted(CASES))
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--launches", type=int, default=3)
-    ap.add_argument("--slices", type=int, default=9)
+    ap.add_argument("--slices", type=int, default=0)  # 0: the library's default
     a = ap.parse_args()
     dt, op, axis = CASES[a.case]
     n = a.n
