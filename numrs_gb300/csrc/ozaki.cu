@@ -9,7 +9,8 @@
 //    e_b[j] likewise over column j of B. Powers of two: exact.
 // 2. Slicing: x = a_ik * 2^-e_a[i] in (-1, 1) becomes the 126-bit fixed-point
 //    integer X = round(x * 2^126), split into S signed b-bit digits
-//    (b = OZ_DIGIT_BITS = 7) whose weighted sum is X rounded to the nearest
+//    (b = 8, 7 or 6: the widest whose exactness bounds below hold for the
+//    call's K and S) whose weighted sum is X rounded to the nearest
 //    multiple of 2^(127 - b - b(S-1)): each digit lies in [-2^(b-1), 2^(b-1)],
 //    exactly representable in BF16, and x = sum_t digit_t * 2^-(b - 1 + bt)
 //    up to 2^-(bS). Slices are stored K-major ([S][rows][kpad] bf16) for A
@@ -61,18 +62,13 @@ constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 32 KB
 constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
 constexpr int OZ_THREADS = 320;                 // 10 warps: TMA, MMA, 8 epilogue
 constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
-// Signed digits of OZ_DIGIT_BITS bits: |digit| <= 2^(b-1), exact in BF16
-// (8-bit significand) for b <= 8; products <= 2^(2b-2), so a K chunk of
-// 2^(26-2b) sums exactly in FP32 (< 2^24 + 1). 7-bit digits need S = 8 for
-// 56 bits (36 slice pairs) where 6-bit digits need S = 9 (45 pairs).
-#ifndef NRS_OZ_DIGIT_BITS
-#define NRS_OZ_DIGIT_BITS 7
-#endif
-constexpr int OZ_DIGIT_BITS = NRS_OZ_DIGIT_BITS;
-static_assert(OZ_DIGIT_BITS >= 4 && OZ_DIGIT_BITS <= 8, "digits must stay exact in BF16");
-constexpr int OZ_KCHUNK = 1 << (26 - 2 * OZ_DIGIT_BITS);  // exact fp32 accumulation bound
-constexpr int OZ_TOP = 127 - OZ_DIGIT_BITS;               // position of the top digit in X
-constexpr int OZ_DEFAULT_SLICES = (54 + OZ_DIGIT_BITS - 1) / OZ_DIGIT_BITS;
+// Signed digits of b bits: |digit| <= 2^(b-1), exact in BF16 (8-bit
+// significand) for b <= 8; products <= 2^(2b-2), so a K chunk of 2^(26-2b)
+// sums exactly in FP32 (at most 2^24). Wider digits need fewer slices for
+// the same precision (S = ceil(54 / b): 7 slices and 28 pairs for b = 8,
+// 8 and 36 for b = 7, 9 and 45 for b = 6) but shorter exact K chunks.
+constexpr int kChunkOf(int b) { return 1 << (26 - 2 * b); }
+constexpr int kTopOf(int b) { return 127 - b; }  // position of the top digit in X
 constexpr int OZ_MAX_SLICES = 16;
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 
@@ -197,6 +193,8 @@ struct OzParams {
   double* C;
   int64_t ldc;
   int final_shift; // 2 - 2b - b(S-1) for b-bit digits
+  int digit_bits;  // b
+  int kchunk;      // exact FP32 K chunk, 2^(26-2b)
   uint32_t* err;
 };
 
@@ -288,8 +286,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tile_coords(tile, P, tm, tn);
         for (int u = 0; u < P.n_pairs && ok; ++u) {
           const PairOf pr = pair_of(u, P.slices, P.kchunks);
-          const int kb0 = pr.chunk * (OZ_KCHUNK / OZ_BK);
-          int kb1 = kb0 + OZ_KCHUNK / OZ_BK;
+          const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
+          int kb1 = kb0 + P.kchunk / OZ_BK;
           if (kb1 > kblocks_full) kb1 = kblocks_full;
           for (int kb = kb0; kb < kb1; ++kb, ++it) {
             const int s = it % OZ_STAGES;
@@ -316,8 +314,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         for (int u = 0; u < P.n_pairs && ok; ++u, ++ai) {
           const PairOf pr = pair_of(u, P.slices, P.kchunks);
-          const int kb0 = pr.chunk * (OZ_KCHUNK / OZ_BK);
-          int kb1 = kb0 + OZ_KCHUNK / OZ_BK;
+          const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
+          int kb1 = kb0 + P.kchunk / OZ_BK;
           if (kb1 > kblocks_full) kb1 = kblocks_full;
           // One accumulator (TMEM columns 0..255); the epilogue frees it as
           // soon as it has folded it into the diagonal sums (columns 256..511).
@@ -417,7 +415,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                                                       pair_of(u + 1, P.slices, P.kchunks).t) != d;
         if (!diag_end) continue;
         const bool first = (d == P.slices - 1), last = (d == 0);
-        const int shift = OZ_DIGIT_BITS * (P.slices - 1 - d);
+        const int shift = P.digit_bits * (P.slices - 1 - d);
         const int ecol_base = (last && row_ok) ? P.ea[row] + P.final_shift : 0;
         __int128* accp = P.acc + (row_ok ? row : 0) * P.n + col0;
 #pragma unroll 1
@@ -539,25 +537,23 @@ __device__ __forceinline__ __int128 fixed126(double x, int e) {
   return neg ? -X : X;
 }
 
-// Signed b-bit digits (b = OZ_DIGIT_BITS) of X at positions
-// p_t = OZ_TOP - b t, t < S, with
+// Signed b-bit digits of X at positions p_t = 127 - b - b t, t < S, with
 //   sum_t d_t 2^p_t = X rounded to the nearest multiple of 2^p_(S-1) (ties up).
 // Z = X + h * sum_t 2^p_t + 2^(p_(S-1) - 1), h = 2^(b-1), makes every b-bit
 // field of Z the digit plus h, so each digit is one shift and mask: d_t in
-// [-h, h - 1] for t >= 1, the top digit (Z >> OZ_TOP) - h in [-h, h]. Every
+// [-h, h - 1] for t >= 1, the top digit (Z >> p_0) - h in [-h, h]. Every
 // digit is exact in BF16 and |d_s d_t| <= 2^(2b-2), as the file header
 // requires.
 // Z is unsigned: X + C lies in (0, 2^127 + 2^122), beyond the signed range.
-__device__ __forceinline__ unsigned __int128 digit_offset(int S) {
-  unsigned __int128 c = (unsigned __int128)1 << (OZ_TOP - OZ_DIGIT_BITS * (S - 1) - 1);
-  for (int t = 0; t < S; ++t)
-    c += (unsigned __int128)(1u << (OZ_DIGIT_BITS - 1)) << (OZ_TOP - OZ_DIGIT_BITS * t);
+__device__ __forceinline__ unsigned __int128 digit_offset(int S, int b) {
+  unsigned __int128 c = (unsigned __int128)1 << (kTopOf(b) - b * (S - 1) - 1);
+  for (int t = 0; t < S; ++t) c += (unsigned __int128)(1u << (b - 1)) << (kTopOf(b) - b * t);
   return c;
 }
-__device__ __forceinline__ int digit_at(unsigned __int128 Z, int t) {
-  const int p = OZ_TOP - OZ_DIGIT_BITS * t;
+__device__ __forceinline__ int digit_at(unsigned __int128 Z, int t, int b) {
+  const int p = kTopOf(b) - b * t;
   const int f = (int)(uint32_t)(uint64_t)(Z >> p);
-  return (t == 0 ? f : (f & ((1 << OZ_DIGIT_BITS) - 1))) - (1 << (OZ_DIGIT_BITS - 1));
+  return (t == 0 ? f : (f & ((1 << b) - 1))) - (1 << (b - 1));
 }
 
 __device__ __forceinline__ uint32_t bf16_of_int(int v) {
@@ -570,10 +566,10 @@ __device__ __forceinline__ uint32_t bf16_of_int(int v) {
 // vector per slice.
 __global__ void __launch_bounds__(256)
     slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda, int64_t kpad,
-               const int* __restrict__ ea, int S, uint16_t* __restrict__ out) {
+               const int* __restrict__ ea, int S, int b, uint16_t* __restrict__ out) {
   const int64_t gpr = kpad / 8;
   const int64_t total = m * gpr;
-  const unsigned __int128 C = digit_offset(S);
+  const unsigned __int128 C = digit_offset(S, b);
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = g / gpr, j0 = (g - i * gpr) * 8;
@@ -587,7 +583,7 @@ __global__ void __launch_bounds__(256)
       const unsigned __int128 Z = (unsigned __int128)(j < k ? fixed126(A[i * lda + j], e) : (__int128)0) + C;
 #pragma unroll
       for (int t = 0; t < OZ_MAX_SLICES; ++t)
-        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at(Z, t)) << (16 * (q & 1));
+        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at(Z, t, b)) << (16 * (q & 1));
     }
     uint16_t* o = out + i * kpad + j0;
 #pragma unroll
@@ -605,11 +601,11 @@ __global__ void __launch_bounds__(256)
 constexpr int kSliceColK = 64, kSliceColN = 32, kSliceColPitch = kSliceColK / 2 + 1;
 __global__ void __launch_bounds__(256)
     slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb, int64_t kpad,
-               const int* __restrict__ eb, int S, uint16_t* __restrict__ out) {
+               const int* __restrict__ eb, int S, int b, uint16_t* __restrict__ out) {
   extern __shared__ uint32_t tile[];  // [S][32][33]
   const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const unsigned __int128 C = digit_offset(S);
+  const unsigned __int128 C = digit_offset(S, b);
   {
     const int64_t nn = n0 + tx;
     const int e = nn < n ? eb[nn] : 0;
@@ -623,7 +619,7 @@ __global__ void __launch_bounds__(256)
           (unsigned __int128)(kk + 1 < k && nn < n ? fixed126(B[(kk + 1) * ldb + nn], e) : (__int128)0) + C;
       for (int t = 0; t < S; ++t)
         tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
-            bf16_of_int(digit_at(Z0, t)) | (bf16_of_int(digit_at(Z1, t)) << 16);
+            bf16_of_int(digit_at(Z0, t, b)) | (bf16_of_int(digit_at(Z1, t, b)) << 16);
     }
   }
   __syncthreads();
@@ -663,22 +659,32 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
     return nrs_fail(h, NRS_ERR_SHAPE, "leading dimension too small");
   if (slices < 0 || slices > OZ_MAX_SLICES)
     return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
-  const int S = slices == 0 ? OZ_DEFAULT_SLICES : slices;
+  // Widest digits whose int32 diagonal sums stay exact for this K and S:
+  // a diagonal sums at most kchunks * S chunk sums of magnitude <= 2^24.
   const int64_t kpad = ((k + 7) / 8) * 8;
-  const int kchunks = (int)((kpad + OZ_KCHUNK - 1) / OZ_KCHUNK);
-  const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
-  // A diagonal's int32 sum holds at most kchunks * S chunk sums of
-  // magnitude <= 2^24 each: keep it below 2^31.
-  if ((int64_t)kchunks * S >= 128)
+  int b = 0, S = 0, kchunks = 0;
+  for (int cand = 8; cand >= 6 && !b; --cand) {
+    const int s_c = slices == 0 ? (54 + cand - 1) / cand : slices;
+    const int kc = (int)((kpad + kChunkOf(cand) - 1) / kChunkOf(cand));
+    // ... and every digit position (127 - b - b t, t < S) lies inside X's
+    // 126 fraction bits: b * S <= 126.
+    if ((int64_t)(kc > 0 ? kc : 1) * s_c < 128 && cand * s_c <= 126) {
+      b = cand;
+      S = s_c;
+      kchunks = kc;
+    }
+  }
+  if (!b)
     return nrs_fail(h, NRS_ERR_TOO_LARGE,
-                    "k too large for this slice count (ceil(k / " + std::to_string(OZ_KCHUNK) + ") * S must be < 128)");
+                    "k too large for this slice count (ceil(k / 16384) * S must be < 128)");
+  const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
   if (info) {
     info->slices = S;
     info->products = n_pairs;
-    info->slice_bits = OZ_DIGIT_BITS;
-    info->k_chunk = OZ_KCHUNK;
-    // truncation of both operands: 2 * 2^-(6 + 6(S-1)) relative to rowmax*colmax per term
-    info->est_rel_error = std::ldexp(2.0, -OZ_DIGIT_BITS * S);
+    info->slice_bits = b;
+    info->k_chunk = kChunkOf(b);
+    // each operand is rounded at 2^-(bS) of its row (column) maximum
+    info->est_rel_error = std::ldexp(2.0, -b * S);
   }
   if (m == 0 || n == 0) return NRS_OK;
   if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
@@ -712,7 +718,7 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   exponents_from_bits<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(colmax, n, eb);
   const int64_t groups = m * (kpad / 8);
   const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
-  slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
+  slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, b, sa);
   const size_t col_smem = (size_t)S * kSliceColN * kSliceColPitch * 4;
   static bool col_attr = false;
   if (!col_attr) {
@@ -721,7 +727,7 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
     col_attr = true;
   }
   dim3 g2((unsigned)((n + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
-  slice_cols<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, sb);
+  slice_cols<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, b, sb);
   if ((st = nrs_after_launch(h, "ozaki slicing"))) return st;
 
   CUtensorMap mapA, mapB;
@@ -744,7 +750,9 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   P.acc = acc;
   P.C = C;
   P.ldc = ldc;
-  P.final_shift = 2 - 2 * OZ_DIGIT_BITS - OZ_DIGIT_BITS * (S - 1);
+  P.final_shift = 2 - 2 * b - b * (S - 1);
+  P.digit_bits = b;
+  P.kchunk = kChunkOf(b);
   P.err = h->dev_error;
   static bool attr_set = false;
   if (!attr_set) {

@@ -77,3 +77,20 @@ def test_ozaki_zero_and_errors(K):
     Z = torch.zeros((64, 0), dtype=torch.float64, device="cuda")
     C, _ = K.gemm_ozaki(Z, torch.zeros((0, 8), dtype=torch.float64, device="cuda"))
     assert torch.all(C == 0)
+
+
+@pytest.mark.parametrize("k,bits", [(2048, 8), (20000, 7)])
+def test_ozaki_digit_width_follows_k(K, ora, k, bits):
+    """The widest digits whose int32 diagonal sums stay exact: 8-bit digits
+    (1024-wide exact FP32 chunks) while ceil(k / 1024) * S < 128, else 7-bit
+    (4096-wide chunks); both at the FP64 error level."""
+    m = n = 128
+    A = ora.gen_uniform_pm1(7, m * k).reshape(m, k)
+    B = ora.gen_uniform_pm1(8, k * n).reshape(k, n)
+    C, info = K.gemm_ozaki(_dev(A), _dev(B))
+    assert info["slice_bits"] == bits, info
+    assert info["k_chunk"] == 1 << (26 - 2 * bits)
+    Cdd, ab = ora.gemm_dd(A, B)
+    e_oz = _err(to_np(C), Cdd, ab)
+    e_dmma = _err(to_np(K.matmul(_dev(A), _dev(B), variant=L.GEMM_DMMA)), Cdd, ab)
+    assert e_oz <= 1e-14 and e_oz <= max(3 * e_dmma, 5e-16), (e_oz, e_dmma, info)
