@@ -305,6 +305,34 @@ def elementwise_section(K, L):
     return out
 
 
+def reductions_extra_section(K, L):
+    """The reductions outside the C2 step, on the same 16384x16384 f32
+    N(0,1) array (1 GiB, seed 3): flat sum / mean / max / var (the
+    reference's 8192-chunk tiering; var reads the array twice), axis var
+    (two passes: lane means, then squared deviations) and axis argmax.
+    GB/s = algorithmic bytes (every pass's read) / time."""
+    import torch
+    n = R * C_
+    stream = torch.cuda.current_stream()
+    x = torch.empty((R, C_), device="cuda")
+    K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+    cases = {"flat_sum": (lambda: K.sum(x), 4 * n),
+             "flat_mean": (lambda: K.mean(x), 4 * n),
+             "flat_max": (lambda: K.max(x), 4 * n),
+             "flat_var": (lambda: K.var(x), 8 * n),
+             "var_axis0": (lambda: K.var(x, 0), 8 * n),
+             "var_axis1": (lambda: K.var(x, 1), 8 * n),
+             "argmax_axis1": (lambda: K.argmax(x, 1), 4 * n),
+             "argmax_flat": (lambda: K.argmax(x), 4 * n)}
+    out = {}
+    for name, (fn, nbytes) in cases.items():
+        ms = _time_ms(fn, 5, stream)
+        out[name] = {"ms": round(ms, 4), "gbs": round(nbytes / ms / 1e6, 1)}
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 def scan_section(K, L):
     """Running folds on 16384x16384 f32 N(0,1) (seed 3): cumsum along axis 0
     (column pipeline), axis 1 (row pipeline) and over the flattened array
@@ -452,6 +480,7 @@ def main():
     ap.add_argument("--no-elementwise", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
     ap.add_argument("--no-io", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -628,6 +657,8 @@ def main():
         out["gemm"] = gemm_section(K, L, quick=args.quick_gemm)
     if rank == 0 and not args.no_elementwise:
         out["elementwise"] = elementwise_section(K, L)
+    if rank == 0 and not args.no_extra:
+        out["reductions_extra"] = reductions_extra_section(K, L)
     if rank == 0 and not args.no_scan:
         out["scan"] = scan_section(K, L)
     if rank == 0 and not args.no_io:

@@ -155,26 +155,42 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Combines the chunk candidates. arg_better is a strict preference (better
+// value, then smaller index; a NaN is never better), so picking the best
+// candidate in any grouping gives the same answer: 1024 threads take runs of
+// candidates, then a shared-memory tree.
 template <typename T, bool MAX>
-__global__ void arg_finish(const T* __restrict__ x, const ArgCand<T>* __restrict__ part,
-                           int64_t nchunks, int64_t* out) {
-  if (threadIdx.x != 0) return;
-  const T x0 = x[0];
-  if (x0 != x0) {  // a NaN first element is never replaced
-    out[0] = 0;
-    return;
-  }
+__global__ void __launch_bounds__(1024)
+    arg_finish(const T* __restrict__ x, const ArgCand<T>* __restrict__ part, int64_t nchunks,
+               int64_t* out) {
+  __shared__ T sv[1024];
+  __shared__ int64_t si[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (nchunks + 1023) / 1024;
   T bv = T(0);
   int64_t bi = -1;
-  for (int64_t c = 0; c < nchunks; ++c) {
+  for (int64_t c = t * per; c < (t + 1) * per && c < nchunks; ++c) {
     if (part[c].idx < 0) continue;
-    const T v = part[c].v;
-    if (arg_better<T, MAX>(v, part[c].idx, bv, bi)) {
-      bv = v;
+    if (arg_better<T, MAX>(part[c].v, part[c].idx, bv, bi)) {
+      bv = part[c].v;
       bi = part[c].idx;
     }
   }
-  out[0] = bi < 0 ? 0 : bi;  // all NaN (after element 0 checked): index 0
+  sv[t] = bv;
+  si[t] = bi;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (t < s && si[t + s] >= 0 && arg_better<T, MAX>(sv[t + s], si[t + s], sv[t], si[t])) {
+      sv[t] = sv[t + s];
+      si[t] = si[t + s];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const T x0 = x[0];
+    // a NaN first element is never replaced; all-NaN tails give index 0
+    out[0] = (x0 != x0 || si[0] < 0) ? 0 : si[0];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -351,6 +367,92 @@ __global__ void __launch_bounds__(64)
   if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
+// argmax / argmin along lanes through the same TMA pipelines: each thread
+// scans its lane in order keeping (best, index) -- the first element starts
+// the lane, a later one replaces it only if strictly greater (smaller), so
+// ties keep the first index and a NaN is chosen only as element 0.
+template <typename T, bool MAX, bool COLS, int STAGES>
+__global__ void __launch_bounds__(64)
+    arg_lane_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
+                 int64_t* __restrict__ out, uint32_t* err) {
+  constexpr int TB = COLS ? col_rows<T>() : 128 / (int)sizeof(T);  // axis positions per tile
+  constexpr int TILE = 8192;
+  constexpr int PER16 = 16 / sizeof(T);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TILE * STAGES);
+  __shared__ int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * 64;
+  const int32_t batch = blockIdx.y;
+  const int64_t n_tiles = (alen + TB - 1) / TB;
+  auto load = [&](int s, int64_t tile) {
+    mbar_arrive_expect_tx(&full[s], TILE);
+    if (COLS)
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(tile * TB), batch);
+    else
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(tile * TB), (int32_t)l0, batch);
+  };
+  if (t == 0) {
+    prefetch_tensormap(&map);
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (t == 0)
+    for (int s = 0; s < STAGES && s < n_tiles; ++s) load(s, s);
+  T best = T(0);
+  int64_t bi = 0;
+  const int sw = t & 7;
+  int64_t it = 0;
+  for (; it < n_tiles; ++it) {
+    const int s = (int)(it % STAGES);
+    if (!mbar_wait_bounded(&full[s], (uint32_t)((it / STAGES) & 1), NRS_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) break;
+    const int64_t j0 = it * TB;
+    const int cnt = (int)((alen - j0) < TB ? (alen - j0) : TB);
+    T v[TB];
+    if (COLS) {
+      const T* tile = reinterpret_cast<const T*>(smem + s * TILE);
+#pragma unroll
+      for (int r = 0; r < TB; ++r) v[r] = tile[r * 64 + t];
+    } else {
+      const uint8_t* row = smem + s * TILE + t * 128;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) memcpy(&v[c * PER16], row + ((c ^ sw) << 4), 16);
+    }
+    // Unrolled over the tile with constant indices (v stays in registers);
+    // positions past the end of the axis are skipped.
+#pragma unroll
+    for (int e = 0; e < TB; ++e) {
+      if (e < cnt) {
+        if (it == 0 && e == 0) {
+          best = v[0];
+          bi = 0;
+        } else if (MAX ? (v[e] > best) : (v[e] < best)) {
+          best = v[e];
+          bi = j0 + e;
+        }
+      }
+    }
+    __syncthreads();  // every thread is done with stage s
+    if (t == 0 && it + STAGES < n_tiles) load(s, it + STAGES);
+  }
+  if (abort_flag) {
+    if (t == 0) {
+      atomicOr(err, NRS_DEVERR_REDUCE_TMA | (7u << 8));
+      for (int64_t j = it; j < n_tiles && j < it + STAGES; ++j)
+        mbar_wait_bounded(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), NRS_WAIT_LIMIT);
+    }
+    return;
+  }
+  const int64_t lane = l0 + t;
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = bi;
+}
+
 constexpr int kStages = 8;
 
 // ---------------------------------------------------------------------------
@@ -373,6 +475,9 @@ __global__ void __launch_bounds__(256)
     const int64_t len = (n - lo) < chunk ? (n - lo) : chunk;
     T acc = Fold<T, OP>::init();
     int nan = 0;
+    // Unrolled so eight loads are in flight; each thread still folds its
+    // elements t, t+256, ... in order.
+#pragma unroll 8
     for (int64_t i = threadIdx.x; i < len; i += 256) {
       T v = x[lo + i];
       if constexpr (SSD) {
@@ -511,7 +616,14 @@ int launch_generic(nrs_handle* h, const AxisProblem& p) {
 }
 
 template <typename T, bool MAX>
+int launch_arg_tma(nrs_handle* h, const AxisProblem& p);
+
+template <typename T, bool MAX>
 int launch_arg(nrs_handle* h, const AxisProblem& p) {
+  if (p.alen >= 256 && p.n_out >= 64) {
+    const int st = launch_arg_tma<T, MAX>(h, p);
+    if (st != NRS_ERR_UNSUPPORTED) return st;
+  }
   int64_t blocks = (p.n_out + 255) / 256;
   int grid = (int)(blocks < (int64_t)h->num_sms * 16 ? blocks : (int64_t)h->num_sms * 16);
   if (grid < 1) grid = 1;
@@ -585,6 +697,43 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
     return nrs_after_launch(h, "fold_rows_tma");
   }
   (void)tile_bytes;
+  return NRS_ERR_UNSUPPORTED;
+}
+
+// argmax / argmin through the TMA lane pipelines (the fold kernels'
+// geometry); NRS_ERR_UNSUPPORTED when the view does not qualify.
+template <typename T, bool MAX>
+int launch_arg_tma(nrs_handle* h, const AxisProblem& p) {
+  const int es = sizeof(T);
+  const KeptDims& k = p.kept;
+  if (k.n < 1 || k.n > 2 || p.alen < 1) return NRS_ERR_UNSUPPORTED;
+  const int64_t lanes = k.size[k.n - 1], lstride = k.stride[k.n - 1];
+  const int64_t batch = (k.n == 2) ? k.size[0] : 1;
+  const int64_t bstride = (k.n == 2) ? k.stride[0] : 0;
+  if (batch > 65535) return NRS_ERR_UNSUPPORTED;
+  const size_t smem = PipeSmem<8192, kStages>::kBytes;
+  CUtensorMap map;
+  dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch);
+  if (lstride == 1 && p.astride > 1) {
+    const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
+    const uint64_t strides[2] = {(uint64_t)p.astride * es, (uint64_t)(batch > 1 ? bstride : p.astride * p.alen) * es};
+    const uint32_t box[3] = {(uint32_t)kColLanes, (uint32_t)col_rows<T>(), 1};
+    if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE)) return NRS_ERR_UNSUPPORTED;
+    auto kern = arg_lane_tma<T, MAX, true, kStages>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (int64_t*)p.out, h->dev_error);
+    return nrs_after_launch(h, "arg_lane_tma");
+  }
+  if (p.astride == 1 && lstride > 1) {
+    const uint64_t dims[3] = {(uint64_t)p.alen, (uint64_t)lanes, (uint64_t)batch};
+    const uint64_t strides[2] = {(uint64_t)lstride * es, (uint64_t)(batch > 1 ? bstride : lstride * lanes) * es};
+    const uint32_t box[3] = {(uint32_t)(128 / es), 64, 1};
+    if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B)) return NRS_ERR_UNSUPPORTED;
+    auto kern = arg_lane_tma<T, MAX, false, kStages>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (int64_t*)p.out, h->dev_error);
+    return nrs_after_launch(h, "arg_lane_tma");
+  }
   return NRS_ERR_UNSUPPORTED;
 }
 
@@ -696,7 +845,7 @@ int flat_arg(nrs_handle* h, int64_t n, const void* x, void* out) {
   if (!part) return st;
   const int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
   arg_partials<T, MAX><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
-  arg_finish<T, MAX><<<1, 32, 0, h->stream>>>((const T*)x, part, nchunks, (int64_t*)out);
+  arg_finish<T, MAX><<<1, 1024, 0, h->stream>>>((const T*)x, part, nchunks, (int64_t*)out);
   return nrs_after_launch(h, "flat argmax/argmin");
 }
 
