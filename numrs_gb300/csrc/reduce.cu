@@ -122,43 +122,74 @@ __device__ __forceinline__ bool arg_better(T v, int64_t i, T w, int64_t j) {
   return v == w && i < j;
 }
 
-template <typename T, bool MAX>
-__global__ void __launch_bounds__(256)
+// One candidate per 8192-element chunk, one warp per chunk with eight
+// consecutive elements per thread and step (the flat_partials layout below).
+// arg_better is a strict preference, so the scan and combine order are free.
+template <typename T, bool MAX, bool VEC>
+__global__ void __launch_bounds__(256, 4)
     arg_partials(const T* __restrict__ x, int64_t n, ArgCand<T>* __restrict__ part) {
-  __shared__ T sv[256];
-  __shared__ int64_t si[256];
+  constexpr int LPT = 8;
+  constexpr int UNROLL = sizeof(T) == 8 ? 2 : 4;
   const int64_t nchunks = (n + kChunk - 1) / kChunk;
-  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int64_t lo = c * kChunk, hi = (lo + kChunk < n) ? lo + kChunk : n;
+  const int t = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
+    const int64_t lo = c * kChunk;
+    const int64_t len = (n - lo) < kChunk ? (n - lo) : kChunk;
+    const int64_t base = lo + LPT * t;
     T bv = T(0);
     int64_t bi = -1;
-    for (int64_t i = lo + threadIdx.x; i < hi; i += 256) {
-      const T v = x[i];
-      if (arg_better<T, MAX>(v, i, bv, bi)) {
-        bv = v;
-        bi = i;
+    const int64_t full = len / 256;
+#pragma unroll UNROLL
+    for (int64_t k = 0; k < full; ++k) {
+      T v[LPT];
+      const T* p = x + base + 256 * k;
+      if constexpr (VEC) {
+        constexpr int NV = LPT * (int)sizeof(T) / 16;
+        uint4 u[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) u[q] = reinterpret_cast<const uint4*>(p)[q];
+        memcpy(v, u, sizeof(v));
+      } else {
+#pragma unroll
+        for (int j = 0; j < LPT; ++j) v[j] = p[j];
+      }
+#pragma unroll
+      for (int j = 0; j < LPT; ++j) {
+        if (arg_better<T, MAX>(v[j], base + 256 * k + j, bv, bi)) {
+          bv = v[j];
+          bi = base + 256 * k + j;
+        }
       }
     }
-    sv[threadIdx.x] = bv;
-    si[threadIdx.x] = bi;
-    __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-      if (threadIdx.x < s && si[threadIdx.x + s] >= 0 &&
-          arg_better<T, MAX>(sv[threadIdx.x + s], si[threadIdx.x + s], sv[threadIdx.x], si[threadIdx.x])) {
-        sv[threadIdx.x] = sv[threadIdx.x + s];
-        si[threadIdx.x] = si[threadIdx.x + s];
+    const int64_t rest = len - 256 * full;
+#pragma unroll
+    for (int j = 0; j < LPT; ++j) {
+      if (LPT * t + j < rest) {
+        const int64_t i = base + 256 * full + j;
+        if (arg_better<T, MAX>(x[i], i, bv, bi)) {
+          bv = x[i];
+          bi = i;
+        }
       }
-      __syncthreads();
     }
-    if (threadIdx.x == 0) part[c] = ArgCand<T>{sv[0], si[0]};
-    __syncthreads();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, bv, off);
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (oi >= 0 && arg_better<T, MAX>(ov, oi, bv, bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (t == 0) part[c] = ArgCand<T>{bv, bi};
   }
 }
 
 // Combines the chunk candidates. arg_better is a strict preference (better
 // value, then smaller index; a NaN is never better), so picking the best
-// candidate in any grouping gives the same answer: 1024 threads take runs of
-// candidates, then a shared-memory tree.
+// candidate in any grouping gives the same answer: thread t takes candidates
+// t, t+1024, ... (coalesced), then a shared-memory tree.
 template <typename T, bool MAX>
 __global__ void __launch_bounds__(1024)
     arg_finish(const T* __restrict__ x, const ArgCand<T>* __restrict__ part, int64_t nchunks,
@@ -166,14 +197,14 @@ __global__ void __launch_bounds__(1024)
   __shared__ T sv[1024];
   __shared__ int64_t si[1024];
   const int t = threadIdx.x;
-  const int64_t per = (nchunks + 1023) / 1024;
   T bv = T(0);
   int64_t bi = -1;
-  for (int64_t c = t * per; c < (t + 1) * per && c < nchunks; ++c) {
-    if (part[c].idx < 0) continue;
-    if (arg_better<T, MAX>(part[c].v, part[c].idx, bv, bi)) {
-      bv = part[c].v;
-      bi = part[c].idx;
+#pragma unroll 4
+  for (int64_t c = t; c < nchunks; c += 1024) {
+    const ArgCand<T> q = part[c];
+    if (q.idx >= 0 && arg_better<T, MAX>(q.v, q.idx, bv, bi)) {
+      bv = q.v;
+      bi = q.idx;
     }
   }
   sv[t] = bv;
@@ -458,49 +489,124 @@ constexpr int kStages = 8;
 // ---------------------------------------------------------------------------
 // Flat reductions
 // ---------------------------------------------------------------------------
-// Per-chunk partials. Thread t folds elements t, t+256, ... of its chunk
-// (lane-striped, the shape of a SIMD sum), then the block combines. MIN/MAX
-// fold with a NaN flag and ignore NaNs in the value, as chunk_min/chunk_max
-// do (src/kernels/reduce.rs:337-350). SSD folds (x - mean)^2.
-template <typename T, int OP, bool SSD>
-__global__ void __launch_bounds__(256)
-    flat_partials(const T* __restrict__ x, int64_t n, int64_t chunk, const T* mean_ptr,
-                  Partial<T>* __restrict__ part) {
-  __shared__ T sh[8];
-  __shared__ int shn[8];
-  const int64_t nchunks = (n + chunk - 1) / chunk;
-  const T mean = SSD ? *mean_ptr : T(0);
-  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int64_t lo = c * chunk;
-    const int64_t len = (n - lo) < chunk ? (n - lo) : chunk;
-    T acc = Fold<T, OP>::init();
-    int nan = 0;
-    // Unrolled so eight loads are in flight; each thread still folds its
-    // elements t, t+256, ... in order.
-#pragma unroll 8
-    for (int64_t i = threadIdx.x; i < len; i += 256) {
-      T v = x[lo + i];
-      if constexpr (SSD) {
-        T d = v - mean;
-        v = d * d;
-      }
-      if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
-        nan |= is_nan(v);
-        if (!is_nan(v)) acc = Fold<T, OP>::step(acc, v);
-      } else {
-        acc = Fold<T, OP>::step(acc, v);
-      }
-    }
-    T r = block_combine<T, OP>(acc, sh);
-    int anynan = __syncthreads_or(nan);
-    (void)shn;
-    if (threadIdx.x == 0) part[c] = Partial<T>{r, anynan};
+// Per-chunk partials in the lane-striped order of a 256-lane SIMD sum: lane L
+// folds elements L, L+256, ... of its chunk in order, then the 256 lanes
+// combine as eight groups of 32 (xor butterfly over offsets 16, 8, 4, 2, 1,
+// the lower-index side first) whose eight results fold in group order
+// (block_combine's tree). MIN/MAX fold with a NaN flag and ignore NaNs in
+// the value, as chunk_min/chunk_max do (src/kernels/reduce.rs:337-350). SSD
+// folds (x - mean)^2.
+//
+// One warp owns a chunk and each thread eight consecutive lanes (8t..8t+7),
+// so a step of the order is one contiguous 256-element row read with 16-byte
+// loads, and the combine needs no block barrier: butterfly offsets 16 and 8
+// are thread xor 2 and 1, offsets 4, 2, 1 stay inside a thread, and group g's
+// result sits in thread 4g.
+constexpr int kFlatLanesPerThread = 8;
+constexpr int kFlatBlocksPerSM = 4;
+
+template <typename T, bool VEC>
+__device__ __forceinline__ void load_lanes(const T* p, T (&v)[kFlatLanesPerThread]) {
+  if constexpr (VEC) {
+    constexpr int NV = kFlatLanesPerThread * (int)sizeof(T) / 16;
+    uint4 u[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) u[i] = reinterpret_cast<const uint4*>(p)[i];
+    memcpy(v, u, sizeof(v));
+  } else {
+#pragma unroll
+    for (int j = 0; j < kFlatLanesPerThread; ++j) v[j] = p[j];
   }
 }
 
-// Folds the chunk partials in chunk order (the reference's sequential fold of
-// the collected Vec). Runs of consecutive partials per thread first when there
-// are more than 1024 chunks; 1024 or fewer are folded by one thread in order.
+template <typename T, int OP, bool SSD>
+__device__ __forceinline__ void fold_lane(T& acc, int& nan, T v, T mean) {
+  if constexpr (SSD) {
+    T d = v - mean;
+    v = d * d;
+  }
+  if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+    nan |= is_nan(v);
+    if (!is_nan(v)) acc = Fold<T, OP>::step(acc, v);
+  } else {
+    acc = Fold<T, OP>::step(acc, v);
+  }
+}
+
+template <typename T, int OP, bool SSD, bool VEC>
+__global__ void __launch_bounds__(256, kFlatBlocksPerSM)
+    flat_partials(const T* __restrict__ x, int64_t n, int64_t chunk, const T* mean_ptr,
+                  Partial<T>* __restrict__ part) {
+  constexpr int LPT = kFlatLanesPerThread;
+  constexpr int UNROLL = sizeof(T) == 8 ? 2 : 4;  // 128 bytes of loads in flight per thread
+  const int64_t nchunks = (n + chunk - 1) / chunk;
+  const T mean = SSD ? *mean_ptr : T(0);
+  const int t = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
+    const int64_t lo = c * chunk;
+    const int64_t len = (n - lo) < chunk ? (n - lo) : chunk;
+    const T* p = x + lo + LPT * t;
+    T acc[LPT];
+#pragma unroll
+    for (int j = 0; j < LPT; ++j) acc[j] = Fold<T, OP>::init();
+    int nan = 0;
+    const int64_t full = len / 256;  // steps in which all 256 lanes have an element
+#pragma unroll UNROLL
+    for (int64_t k = 0; k < full; ++k) {
+      T v[LPT];
+      load_lanes<T, VEC>(p + 256 * k, v);
+#pragma unroll
+      for (int j = 0; j < LPT; ++j) fold_lane<T, OP, SSD>(acc[j], nan, v[j], mean);
+    }
+    const int64_t rest = len - 256 * full;
+#pragma unroll
+    for (int j = 0; j < LPT; ++j)
+      if (LPT * t + j < rest) fold_lane<T, OP, SSD>(acc[j], nan, p[256 * full + j], mean);
+#pragma unroll
+    for (int j = 0; j < LPT; ++j) {
+      acc[j] = Fold<T, OP>::step(acc[j], __shfl_xor_sync(0xffffffffu, acc[j], 2));
+      acc[j] = Fold<T, OP>::step(acc[j], __shfl_xor_sync(0xffffffffu, acc[j], 1));
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j] = Fold<T, OP>::step(acc[j], acc[j + 4]);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) acc[j] = Fold<T, OP>::step(acc[j], acc[j + 2]);
+    acc[0] = Fold<T, OP>::step(acc[0], acc[1]);
+    T r = __shfl_sync(0xffffffffu, acc[0], 0);
+#pragma unroll
+    for (int g = 1; g < 8; ++g) r = Fold<T, OP>::step(r, __shfl_sync(0xffffffffu, acc[0], 4 * g));
+    const int anynan = __any_sync(0xffffffffu, nan);
+    if (t == 0) part[c] = Partial<T>{r, anynan};
+  }
+}
+
+// Blocks of 256 threads for one warp per chunk: about the same number of
+// chunks per warp, on a grid that is resident at once.
+inline int flat_warp_grid(int64_t nchunks, int sms) {
+  const int64_t cap = (int64_t)sms * kFlatBlocksPerSM * 8;  // resident warps
+  const int64_t per = (nchunks + cap - 1) / cap;
+  const int64_t warps = (nchunks + per - 1) / per;
+  return (int)((warps + 7) / 8);
+}
+
+// Launches flat_partials: 16-byte loads when the array is 16-byte aligned
+// (chunk starts then are too: a chunk is 8192 elements or the whole array).
+template <typename T, int OP, bool SSD>
+void launch_partials(cudaStream_t s, int sms, const T* x, int64_t n, int64_t chunk, const T* mean,
+                     Partial<T>* part) {
+  const int grid = flat_warp_grid((n + chunk - 1) / chunk, sms);
+  if ((reinterpret_cast<uintptr_t>(x) & 15) == 0)
+    flat_partials<T, OP, SSD, true><<<grid, 256, 0, s>>>(x, n, chunk, mean, part);
+  else
+    flat_partials<T, OP, SSD, false><<<grid, 256, 0, s>>>(x, n, chunk, mean, part);
+}
+
+// Folds the chunk partials: 1024 or fewer in chunk order by one thread (the
+// reference's sequential fold of the collected Vec); more than 1024 first as
+// 1024 interleaved runs (thread t folds partials t, t+1024, ... in order: a
+// warp reads 32 consecutive partials per step), then the runs in order. The
+// order does not depend on the grid or the device.
 // `fin_op` says what to write: the folded value (SUM/MAX/MIN/PROD), the mean
 // (MEAN; f64 for integers), the mean into `mean_out` for the variance's second
 // pass (-1), or VAR/STD from the folded squared deviations.
@@ -511,12 +617,13 @@ __global__ void __launch_bounds__(1024)
   __shared__ T run[1024];
   __shared__ int runnan[1024];
   const int t = threadIdx.x;
-  const int64_t per = (nchunks + 1023) / 1024;
   T acc = Fold<T, OP>::init();
   int nan = 0;
-  for (int64_t i = t * per; i < (t + 1) * per && i < nchunks; ++i) {
-    acc = Fold<T, OP>::step(acc, part[i].v);
-    nan |= part[i].nan;
+#pragma unroll 8
+  for (int64_t i = t; i < nchunks; i += 1024) {
+    const Partial<T> p = part[i];
+    acc = Fold<T, OP>::step(acc, p.v);
+    nan |= p.nan;
   }
   run[t] = acc;
   runnan[t] = nan;
@@ -524,8 +631,9 @@ __global__ void __launch_bounds__(1024)
   if (t != 0) return;
   T r = Fold<T, OP>::init();
   int anynan = 0;
-  for (int i = 0; i < 1024; ++i) {
-    if ((int64_t)i * per >= nchunks) break;
+  const int nruns = nchunks < 1024 ? (int)nchunks : 1024;
+#pragma unroll 8
+  for (int i = 0; i < nruns; ++i) {
     r = Fold<T, OP>::step(r, run[i]);
     anynan |= runnan[i];
   }
@@ -799,8 +907,6 @@ int flat_reduce(nrs_handle* h, int op, int64_t n, int64_t ddof, const T* x, void
   if (!ws) return st;
   Partial<T>* part = reinterpret_cast<Partial<T>*>(ws);
   T* mean_slot = reinterpret_cast<T*>(ws + (size_t)(nchunks + 1) * sizeof(Partial<T>));
-  int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
-  if (grid < 1) grid = 1;
   if (n == 0) {
     T v = (op == NRS_PROD) ? T(1) : T(0);
     write_scalar<T><<<1, 1, 0, h->stream>>>((T*)out, v);
@@ -809,26 +915,26 @@ int flat_reduce(nrs_handle* h, int op, int64_t n, int64_t ddof, const T* x, void
   switch (op) {
     case NRS_SUM:
     case NRS_MEAN:
-      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_SUM, false>(h->stream, h->num_sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     case NRS_VAR:
     case NRS_STD:
-      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_SUM, false>(h->stream, h->num_sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, -1, 0.0, mean_slot, nullptr);
-      flat_partials<T, NRS_SUM, true><<<grid, 256, 0, h->stream>>>(x, n, chunk, mean_slot, part);
+      launch_partials<T, NRS_SUM, true>(h->stream, h->num_sms, x, n, chunk, mean_slot, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, (double)ddof, nullptr, out);
       break;
     case NRS_MAX:
-      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_MAX, false>(h->stream, h->num_sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_MAX><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     case NRS_MIN:
-      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_MIN, false>(h->stream, h->num_sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_MIN><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     case NRS_PROD:
-      flat_partials<T, NRS_PROD, false><<<grid, 256, 0, h->stream>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_PROD, false>(h->stream, h->num_sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_PROD><<<1, 1024, 0, h->stream>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     default:
@@ -843,8 +949,11 @@ int flat_arg(nrs_handle* h, int64_t n, const void* x, void* out) {
   int st;
   ArgCand<T>* part = (ArgCand<T>*)nrs_workspace(h, (size_t)(nchunks + 1) * sizeof(ArgCand<T>), &st);
   if (!part) return st;
-  const int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
-  arg_partials<T, MAX><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
+  const int grid = flat_warp_grid(nchunks, h->num_sms);
+  if ((reinterpret_cast<uintptr_t>(x) & 15) == 0)
+    arg_partials<T, MAX, true><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
+  else
+    arg_partials<T, MAX, false><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
   arg_finish<T, MAX><<<1, 1024, 0, h->stream>>>((const T*)x, part, nchunks, (int64_t*)out);
   return nrs_after_launch(h, "flat argmax/argmin");
 }
@@ -866,26 +975,25 @@ int flat_reduce_int(nrs_handle* h, int op, int64_t n, const T* x, void* out) {
   int st;
   Partial<T>* part = (Partial<T>*)nrs_workspace(h, (size_t)(nchunks + 1) * sizeof(Partial<T>), &st);
   if (!part) return st;
-  int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
   switch (op) {
     case NRS_SUM:
-      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      launch_partials<T, NRS_SUM, false>(h->stream, h->num_sms, x, n, kChunk, nullptr, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_SUM, 0.0, nullptr, out);
       break;
     case NRS_MEAN:
-      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      launch_partials<T, NRS_SUM, false>(h->stream, h->num_sms, x, n, kChunk, nullptr, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MEAN, 0.0, nullptr, out);
       break;
     case NRS_MAX:
-      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      launch_partials<T, NRS_MAX, false>(h->stream, h->num_sms, x, n, kChunk, nullptr, part);
       flat_finish<T, NRS_MAX><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MAX, 0.0, nullptr, out);
       break;
     case NRS_MIN:
-      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      launch_partials<T, NRS_MIN, false>(h->stream, h->num_sms, x, n, kChunk, nullptr, part);
       flat_finish<T, NRS_MIN><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_MIN, 0.0, nullptr, out);
       break;
     default:
-      flat_partials<T, NRS_PROD, false><<<grid, 256, 0, h->stream>>>(x, n, kChunk, nullptr, part);
+      launch_partials<T, NRS_PROD, false>(h->stream, h->num_sms, x, n, kChunk, nullptr, part);
       flat_finish<T, NRS_PROD><<<1, 1024, 0, h->stream>>>(part, nchunks, n, NRS_PROD, 0.0, nullptr, out);
       break;
   }
@@ -1078,19 +1186,18 @@ int noalloc_flat(cudaStream_t s, int op, int64_t n, const T* x, void* out, void*
   const int64_t chunk = ((op == NRS_SUM || op == NRS_MEAN) && n < kParallelMin) ? n : kChunk;
   const int64_t nchunks = (n + chunk - 1) / chunk;
   Partial<T>* part = static_cast<Partial<T>*>(scratch);
-  const int grid = (int)(nchunks < (int64_t)sms * 8 ? nchunks : (int64_t)sms * 8);
   switch (op) {
     case NRS_SUM:
     case NRS_MEAN:
-      flat_partials<T, NRS_SUM, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_SUM, false>(s, sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_SUM><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     case NRS_MAX:
-      flat_partials<T, NRS_MAX, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_MAX, false>(s, sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_MAX><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
     default:
-      flat_partials<T, NRS_MIN, false><<<grid, 256, 0, s>>>(x, n, chunk, nullptr, part);
+      launch_partials<T, NRS_MIN, false>(s, sms, x, n, chunk, nullptr, part);
       flat_finish<T, NRS_MIN><<<1, 1024, 0, s>>>(part, nchunks, n, op, 0.0, nullptr, out);
       break;
   }
