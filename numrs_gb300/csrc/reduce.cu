@@ -136,53 +136,56 @@ __global__ void __launch_bounds__(256, 4)
   for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
     const int64_t lo = c * kChunk;
     const int64_t len = (n - lo) < kChunk ? (n - lo) : kChunk;
-    const int64_t base = lo + LPT * t;
+    const T* p = x + lo + LPT * t;
+    // A thread meets its elements in increasing index order and never keeps a
+    // NaN, so arg_better reduces to "strictly better, or the first non-NaN":
+    // ties keep the earlier index. `bi` is the offset 256k + 8t + j.
     T bv = T(0);
-    int64_t bi = -1;
-    const int64_t full = len / 256;
+    int bi = -1;
+    const int full = (int)(len / 256);
 #pragma unroll UNROLL
-    for (int64_t k = 0; k < full; ++k) {
+    for (int k = 0; k < full; ++k) {
       T v[LPT];
-      const T* p = x + base + 256 * k;
       if constexpr (VEC) {
         constexpr int NV = LPT * (int)sizeof(T) / 16;
         uint4 u[NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) u[q] = reinterpret_cast<const uint4*>(p)[q];
+        for (int q = 0; q < NV; ++q) u[q] = reinterpret_cast<const uint4*>(p + 256 * k)[q];
         memcpy(v, u, sizeof(v));
       } else {
 #pragma unroll
-        for (int j = 0; j < LPT; ++j) v[j] = p[j];
+        for (int j = 0; j < LPT; ++j) v[j] = p[256 * k + j];
       }
 #pragma unroll
       for (int j = 0; j < LPT; ++j) {
-        if (arg_better<T, MAX>(v[j], base + 256 * k + j, bv, bi)) {
+        if ((MAX ? (v[j] > bv) : (v[j] < bv)) || (bi < 0 && v[j] == v[j])) {
           bv = v[j];
-          bi = base + 256 * k + j;
+          bi = 256 * k + LPT * t + j;
         }
       }
     }
-    const int64_t rest = len - 256 * full;
+    const int rest = (int)(len - 256 * (int64_t)full);
 #pragma unroll
     for (int j = 0; j < LPT; ++j) {
       if (LPT * t + j < rest) {
-        const int64_t i = base + 256 * full + j;
-        if (arg_better<T, MAX>(x[i], i, bv, bi)) {
-          bv = x[i];
-          bi = i;
+        const T v = p[256 * full + j];
+        if ((MAX ? (v > bv) : (v < bv)) || (bi < 0 && v == v)) {
+          bv = v;
+          bi = 256 * full + LPT * t + j;
         }
       }
     }
+    int64_t gi = bi < 0 ? -1 : lo + bi;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const T ov = __shfl_xor_sync(0xffffffffu, bv, off);
-      const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (oi >= 0 && arg_better<T, MAX>(ov, oi, bv, bi)) {
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, gi, off);
+      if (oi >= 0 && arg_better<T, MAX>(ov, oi, bv, gi)) {
         bv = ov;
-        bi = oi;
+        gi = oi;
       }
     }
-    if (t == 0) part[c] = ArgCand<T>{bv, bi};
+    if (t == 0) part[c] = ArgCand<T>{bv, gi};
   }
 }
 
@@ -625,17 +628,26 @@ __global__ void __launch_bounds__(1024)
     acc = Fold<T, OP>::step(acc, p.v);
     nan |= p.nan;
   }
-  run[t] = acc;
-  runnan[t] = nan;
-  __syncthreads();
-  if (t != 0) return;
   T r = Fold<T, OP>::init();
   int anynan = 0;
-  const int nruns = nchunks < 1024 ? (int)nchunks : 1024;
+  if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+    // The partials hold no NaN (a flag carries it), and without NaNs max/min
+    // do not depend on the grouping (only which of two equal zeros is kept),
+    // so the runs combine as a tree rather than a 1024-step chain.
+    r = block_combine<T, OP>(acc, run);
+    anynan = __syncthreads_or(nan);
+    if (t != 0) return;
+  } else {
+    run[t] = acc;
+    runnan[t] = nan;
+    __syncthreads();
+    if (t != 0) return;
+    const int nruns = nchunks < 1024 ? (int)nchunks : 1024;
 #pragma unroll 8
-  for (int i = 0; i < nruns; ++i) {
-    r = Fold<T, OP>::step(r, run[i]);
-    anynan |= runnan[i];
+    for (int i = 0; i < nruns; ++i) {
+      r = Fold<T, OP>::step(r, run[i]);
+      anynan |= runnan[i];
+    }
   }
   if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
     if constexpr (std::is_floating_point<T>::value) {
