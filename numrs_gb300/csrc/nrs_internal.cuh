@@ -147,6 +147,22 @@ NRS_DEV void tma_store_3d(const CUtensorMap* map, const void* src, int32_t x, in
       "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
       : "memory");
 }
+// Untiled bulk copies (no tensor map): both addresses 16-byte aligned and
+// `bytes` a multiple of 16. The load signals `bar` with complete_tx; the store
+// joins the issuing thread's bulk async-group like tma_store_3d.
+NRS_DEV void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+NRS_DEV void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                   reinterpret_cast<uint64_t>(dst)),
+               "r"(smem_u32(src)), "r"(bytes)
+               : "memory");
+}
 NRS_DEV void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 template <int N>
 NRS_DEV void bulk_wait_read() {

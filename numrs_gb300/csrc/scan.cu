@@ -21,6 +21,8 @@
 // parallel scan is exact; integer add/multiply wrap and are exact in any
 // order; float add/multiply reassociate (tolerance-based, as the flat
 // product is). subtract/divide are inherently serial and run as one lane.
+#include <mutex>
+#include <cmath>
 #include <limits>
 #include <string>
 #include <type_traits>
@@ -417,6 +419,163 @@ __global__ void __launch_bounds__(96)
   }
 }
 
+// Running fold along rows whose positions are contiguous (axis stride 1) and
+// 16-byte aligned: each stage holds kRowSegBytes of up to kRowLanes rows,
+// moved per row by untiled bulk copies (one contiguous request per row and
+// stage, where the tiled form issues 128-byte box rows), into rows padded to
+// kRowSegBytes + 16 bytes so that thread t's 16-byte reads of its own row hit
+// distinct banks across each quarter warp. The last warp moves data (lane i:
+// rows i, i + 32, ...), the others fold (thread t: row t). The rows per CTA
+// are chosen at launch so the CTAs fill whole waves. Waits are bounded as in
+// lane_running_tma.
+#ifndef NRS_ROW_SEG_BYTES
+#define NRS_ROW_SEG_BYTES 1024
+#endif
+#ifndef NRS_ROW_STAGES
+#define NRS_ROW_STAGES 3
+#endif
+#ifndef NRS_ROW_LANES
+#define NRS_ROW_LANES 32
+#endif
+constexpr int kRowSegBytes = NRS_ROW_SEG_BYTES;
+constexpr int kRowPitch = kRowSegBytes + 16;
+constexpr int kRowStages = NRS_ROW_STAGES;
+constexpr int kRowLanes = NRS_ROW_LANES;  // most rows per CTA, one folding thread each
+constexpr size_t row_smem(int rows) { return (size_t)rows * kRowPitch * kRowStages + 16 * kRowStages + 16; }
+static_assert(kRowSegBytes % 128 == 0, "segments are whole 128-byte blocks");
+static_assert(kRowLanes % 32 == 0, "whole folding warps");
+static_assert(kStoreLag < kRowStages, "the ring must run ahead of the store lag");
+
+// Folds `cnt` staged values of one padded row in place (prefix values).
+template <typename T, int OP>
+NRS_DEV T fold_seg(uint8_t* row, int cnt, bool first, T acc) {
+  constexpr int SUB = 128 / (int)sizeof(T);
+  constexpr int PER16 = 16 / (int)sizeof(T);
+#pragma unroll 1
+  for (int b = 0; b < kRowSegBytes / 128; ++b) {
+    const int c = cnt - b * SUB;
+    if (c <= 0) break;
+    uint8_t* blk = row + b * 128;
+    const bool f = first && b == 0;
+    if (c >= SUB) {
+      T v[SUB];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], blk + 16 * j, 16);
+#pragma unroll
+      for (int e = 0; e < SUB; ++e) {
+        acc = (e == 0 && f) ? v[0] : apply<T, OP>(acc, v[e]);
+        v[e] = acc;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) memcpy(blk + 16 * j, &v[j * PER16], 16);
+    } else {  // the row's last, short block: element by element in place
+      T* pv = reinterpret_cast<T*>(blk);
+      for (int e = 0; e < c; ++e) {
+        acc = (e == 0 && f) ? pv[0] : apply<T, OP>(acc, pv[e]);
+        pv[e] = acc;
+      }
+    }
+  }
+  return acc;
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kRowLanes + 32)
+    lane_running_rows(const T* __restrict__ x, T* __restrict__ out, int64_t alen, int64_t lanes,
+                      int64_t lstride, int64_t bstride, int rows_per_cta, uint32_t* err, Seed seed) {
+  constexpr int S = kRowStages;
+  const int stage_bytes = rows_per_cta * kRowPitch;
+  constexpr int SEG = kRowSegBytes / (int)sizeof(T);  // positions per stage
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 15) & ~uintptr_t(15));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)stage_bytes * S);
+  uint64_t* done = full + S;
+  __shared__ volatile int abort_flag;
+
+  const int t = threadIdx.x;
+  const int64_t l0 = (int64_t)blockIdx.x * rows_per_cta;
+  const int nrows = (int)((lanes - l0) < rows_per_cta ? (lanes - l0) : rows_per_cta);
+  const int64_t off0 = (int64_t)blockIdx.y * bstride + l0 * lstride;
+  const int64_t n_stages = (alen + SEG - 1) / SEG;
+  auto seg_bytes = [&](int64_t i) {
+    const int64_t left = alen - i * SEG;
+    return (uint32_t)((left < SEG ? left : SEG) * (int64_t)sizeof(T));
+  };
+
+  if (t == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&done[s], kRowLanes);
+    }
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+
+  if (t >= kRowLanes) {  // producer warp
+    const int lane = t - kRowLanes;
+    auto load = [&](int s, int64_t i) {
+      const uint32_t bytes = seg_bytes(i);
+      if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)nrows);
+      __syncwarp();
+      for (int r = lane; r < nrows; r += 32)
+        bulk_load(smem + (size_t)s * stage_bytes + r * kRowPitch, x + off0 + r * lstride + i * SEG, bytes,
+                  &full[s]);
+    };
+    int64_t issued = 0;
+    for (; issued < S && issued < n_stages; ++issued) load((int)issued, issued);
+    bool ok = true;
+    for (int64_t i = 0; i < n_stages; ++i) {
+      const int s = (int)(i % S);
+      const bool got = !abort_flag && mbar_wait_bounded(&done[s], (uint32_t)((i / S) & 1), NRS_WAIT_LIMIT);
+      if (!__all_sync(0xffffffffu, got)) {
+        ok = false;
+        break;
+      }
+      const uint32_t bytes = seg_bytes(i);
+      for (int r = lane; r < nrows; r += 32)
+        bulk_store(out + off0 + r * lstride + i * SEG, smem + (size_t)s * stage_bytes + r * kRowPitch, bytes);
+      bulk_commit();
+      const int64_t q = i - kStoreLag;  // its stores have now finished reading
+      if (q >= 0 && q + S < n_stages) {
+        bulk_wait_read<kStoreLag>();
+        __syncwarp();
+        load((int)(q % S), q + S);
+        issued = q + S + 1;
+      }
+    }
+    if (!ok) {
+      if (lane == 0) {
+        abort_flag = 1;
+        atomicOr(err, NRS_DEVERR_REDUCE_TMA | (7u << 8));
+      }
+      // Loads issued into the ring: steps issued - S .. issued - 1.
+      for (int64_t j = (issued > S ? issued - S : 0); j < issued; ++j)
+        mbar_wait_bounded(&full[j % S], (uint32_t)((j / S) & 1), NRS_WAIT_LIMIT);
+    }
+    bulk_wait<0>();
+    return;
+  }
+
+  // consumers: every thread takes every step (rows past the array only
+  // arrive), so each phase of done[] counts exactly one arrival per thread
+  T acc = seed.get<T>();
+  uint8_t* myrow = smem + t * kRowPitch;
+  for (int64_t i = 0; i < n_stages; ++i) {
+    const int s = (int)(i % S);
+    if (abort_flag || !mbar_wait_bounded(&full[s], (uint32_t)((i / S) & 1), NRS_WAIT_LIMIT)) {
+      abort_flag = 1;
+      return;
+    }
+    if (t < nrows) {
+      const int cnt = (int)((alen - i * SEG) < SEG ? (alen - i * SEG) : SEG);
+      acc = fold_seg<T, OP>(myrow + (size_t)s * stage_bytes, cnt, i == 0 && seed.first, acc);
+    }
+    fence_proxy_async_smem();
+    mbar_arrive(&done[s]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Flat scans (order-free ops)
 // ---------------------------------------------------------------------------
@@ -631,6 +790,42 @@ int launch_lane_tma(nrs_handle* h, const LaneProblem& p) {
   const bool cols = (lstride == 1 && p.xastride > 1);
   const bool rows = (p.xastride == 1 && lstride > 1);
   if (!cols && !rows) return NRS_ERR_UNSUPPORTED;
+  // 4-byte rows: bulk-copy ring. 8-byte rows stay on the tiled ring, which
+  // keeps twice the rows per SM in flight (their folds were slower with
+  // fewer, longer segments: 2.2-2.7 against 3.6 TB/s at 11586^2 f64).
+  if (RUNNING && rows && es == 4 && ((uintptr_t)p.x & 15) == 0 && ((uintptr_t)p.out & 15) == 0 &&
+      (lstride * es) % 16 == 0 && (bstride * es) % 16 == 0 && (p.alen * es) % 16 == 0) {
+    auto kern = lane_running_rows<T, OP>;
+    // CTAs resident per SM for each row count (depends only on the kernel).
+    static int per_sm[kRowLanes + 1];
+    static std::once_flag once;
+    std::call_once(once, [&] {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem(kRowLanes));
+      for (int r = kRowLanes / 2; r <= kRowLanes; ++r)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[r], kern, kRowLanes + 32, row_smem(r)) !=
+            cudaSuccess)
+          per_sm[r] = 0;
+    });
+    // Rows per CTA: the count whose CTAs best fill whole waves (ties: more
+    // rows); within one wave, the count that reaches the most SMs.
+    int rows = kRowLanes;
+    double best = -1.0;
+    for (int r = kRowLanes; r >= kRowLanes / 2; --r) {
+      if (per_sm[r] < 1) continue;
+      const double ctas = (double)((lanes + r - 1) / r) * (double)batch;
+      const double q = ctas / ((double)per_sm[r] * h->num_sms);
+      const double eff = q <= 1.0 ? 0.999 * std::fmin(ctas, (double)h->num_sms) / h->num_sms : q / std::ceil(q);
+      if (eff > best + 1e-9) {
+        best = eff;
+        rows = r;
+      }
+    }
+    if (best < 0) return NRS_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)((lanes + rows - 1) / rows), (unsigned)batch);
+    kern<<<grid, kRowLanes + 32, row_smem(rows), h->stream>>>((const T*)p.x, (T*)p.out, p.alen, lanes, lstride,
+                                                              bstride, rows, h->dev_error, p.seed);
+    return nrs_after_launch(h, "lane_running_rows");
+  }
   uint64_t dims[3], strides[2];
   uint32_t box[3];
   if (cols) {
