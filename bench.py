@@ -554,6 +554,7 @@ def main():
         avg_b = sum(bytes_of[cls]) / len(bytes_of[cls])
         gbs = avg_b / (avg_ms / 1e3) / 1e9
         kernels[cls] = {"launches_per_step": len(bytes_of[cls]), "avg_ms": round(avg_ms, 4),
+                        "median_ms": round(statistics.median(ts), 4), "timed_launches": len(ts),
                         "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
                         "share": round(sum(ts) / sum(sum(v) for v in per_class.values()), 4)}
     dom = max(kernels, key=lambda c: kernels[c]["share"])
