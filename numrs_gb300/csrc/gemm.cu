@@ -12,6 +12,7 @@
 // Overwrite contract: C is written, never read, unless ACCUMULATE is set, in
 // which case C += (A*B) with the product rounded first (matmul_to computes a
 // temporary and adds it, src/array/operations_optimized.rs:385).
+#include <cmath>
 #include <type_traits>
 
 #include "gemm_tiles.cuh"
@@ -20,17 +21,80 @@ using namespace nrs_tiles;
 
 namespace {
 
+// blockIdx.z takes k-values [z*kc, min(k, (z+1)*kc)). With one chunk the
+// tile goes to C; with several, chunk z writes its product to the partial
+// slab P + z*m*n (row pitch n) and splitk_finish adds the slabs.
 template <int BM, int BN, int WM, int WN>
 __global__ void __launch_bounds__(WM * WN * 32)
-    dmma_gemm(int64_t m, int64_t n, int64_t k, const double* __restrict__ A, int64_t rsa,
+    dmma_gemm(int64_t m, int64_t n, int64_t k, int64_t kc, const double* __restrict__ A, int64_t rsa,
               int64_t csa, const double* __restrict__ B, int64_t rsb, int64_t csb,
-              double* __restrict__ C, int64_t ldc, int accumulate) {
+              double* __restrict__ C, int64_t ldc, int accumulate, double* __restrict__ P) {
   using Tile = Dmma<BM, BN, WM, WN>;
   __shared__ __align__(16) uint8_t smem[Tile::kSmem];
   Tile t;
   const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-  t.run(A, rsa, csa, B, rsb, csb, m, n, m0, n0, 0, k, smem);
-  tile_store<double>(t, C, ldc, m, n, m0, n0, accumulate != 0);
+  const int64_t k0 = (int64_t)blockIdx.z * kc, k1 = (k0 + kc < k) ? k0 + kc : k;
+  t.run(A, rsa, csa, B, rsb, csb, m, n, m0, n0, k0, k1, smem);
+  if (gridDim.z == 1)
+    tile_store<double>(t, C, ldc, m, n, m0, n0, accumulate != 0);
+  else
+    tile_store<double>(t, P + (int64_t)blockIdx.z * m * n, n, m, n, m0, n0, false);
+}
+
+// C := p_0 + p_1 + ... + p_{S-1} (slab order), or C += that sum: the product
+// is rounded before it meets C, as without the split.
+__global__ void splitk_finish(const double* __restrict__ P, int splits, int64_t m, int64_t n,
+                              double* __restrict__ C, int64_t ldc, int accumulate) {
+  const int64_t mn = m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double v = P[e];
+    for (int z = 1; z < splits; ++z) v += P[z * mn + e];
+    double* c = C + (e / n) * ldc + (e % n);
+    *c = accumulate ? *c + v : v;
+  }
+}
+
+// DMMA tiling for an m x n x k product on `sms` SMs: 32x32 or 64x64 tiles and
+// the number of k chunks (multiples of 16, at least 64 values each when split)
+// that minimise the busiest SM's share of the work, ceil(ctas / sms) x the
+// work of one CTA, a split charged 1% (its partial slabs and the finish).
+// Measured at 256^3-2048^3: per flop the two tiles run within 4% of each
+// other (32x32 ahead), and the CTAs' pipeline fill overlaps across the many
+// CTAs an SM holds, so whole-wave balance is what decides.
+struct DmmaPlan {
+  int tile;
+  int splits;
+  int64_t kc;
+};
+DmmaPlan plan_dmma(int64_t m, int64_t n, int64_t k, int sms) {
+#if defined(NRS_DMMA_TILE) && defined(NRS_DMMA_SPLITS)  // fixed plan, for measuring the model
+  {
+    int64_t kc = (k + NRS_DMMA_SPLITS - 1) / NRS_DMMA_SPLITS;
+    kc = (kc + 15) / 16 * 16;
+    return DmmaPlan{NRS_DMMA_TILE, (int)((k + kc - 1) / kc), kc};
+  }
+#endif
+  DmmaPlan best{32, 1, k};
+  double best_cost = 1e300;
+  for (int tile : {32, 64}) {
+    const double ntiles = (double)((m + tile - 1) / tile) * (double)((n + tile - 1) / tile);
+    const double w = tile == 64 ? 4.0 : 1.0;
+    for (int s = 1; s <= 16; ++s) {
+      int64_t kc = (k + s - 1) / s;
+      kc = (kc + 15) / 16 * 16;
+      if (s > 1 && kc < 64) break;
+      const int splits = (int)((k + kc - 1) / kc);
+      if (splits != s) continue;
+      if (splits > 1 && (double)splits * (double)m * (double)n * 8.0 > 256.0 * (1 << 20)) break;
+      const double cost = std::ceil(ntiles * splits / sms) * w * ((double)kc / (double)k) * (splits > 1 ? 1.01 : 1.0);
+      if (cost < best_cost - 1e-12) {
+        best_cost = cost;
+        best = DmmaPlan{tile, splits, kc};
+      }
+    }
+  }
+  return best;
 }
 
 template <typename T, int BM, int BN, int BK, int TM, int TN>
@@ -108,13 +172,25 @@ int nrs_plain_gemm_launch(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_
     else variant = NRS_GEMM_GENERIC;
   }
   if (variant == NRS_GEMM_DMMA && dtype == NRS_F64) {
-    // 64x64 tiles when they fill the GPU, else 32x32.
-    if (((m + 63) / 64) * ((n + 63) / 64) >= h->num_sms) {
-      dmma_gemm<64, 64, 2, 4><<<tiles(m, n, 64, 64), 256, 0, s>>>(
-          m, n, k, (const double*)A, rsa, csa, (const double*)B, rsb, csb, (double*)C, ldc, acc);
-    } else {
-      dmma_gemm<32, 32, 2, 2><<<tiles(m, n, 32, 32), 128, 0, s>>>(
-          m, n, k, (const double*)A, rsa, csa, (const double*)B, rsb, csb, (double*)C, ldc, acc);
+    const DmmaPlan pl = plan_dmma(m, n, k, h->num_sms);
+    double* P = nullptr;
+    if (pl.splits > 1) {
+      int st;
+      P = (double*)nrs_workspace(h, (size_t)pl.splits * (size_t)(m * n) * sizeof(double), &st);
+      if (!P) return st;
+    }
+    dim3 g = tiles(m, n, pl.tile, pl.tile);
+    g.z = (unsigned)pl.splits;
+    if (pl.tile == 64)
+      dmma_gemm<64, 64, 2, 4><<<g, 256, 0, s>>>(m, n, k, pl.kc, (const double*)A, rsa, csa, (const double*)B,
+                                                rsb, csb, (double*)C, ldc, acc, P);
+    else
+      dmma_gemm<32, 32, 2, 2><<<g, 128, 0, s>>>(m, n, k, pl.kc, (const double*)A, rsa, csa, (const double*)B,
+                                                rsb, csb, (double*)C, ldc, acc, P);
+    if (pl.splits > 1) {
+      const int64_t blocks = (m * n + 255) / 256;
+      const int grid = (int)(blocks < (int64_t)h->num_sms * 8 ? blocks : (int64_t)h->num_sms * 8);
+      splitk_finish<<<grid, 256, 0, s>>>(P, pl.splits, m, n, (double*)C, ldc, acc);
     }
     return nrs_after_launch(h, "dmma_gemm");
   }
