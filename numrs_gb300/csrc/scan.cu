@@ -703,6 +703,185 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Flat scans over 16-byte-aligned arrays, as three streaming passes over
+// G <= 2 x SMs contiguous segments (each a whole number of CTA tiles):
+// seg_totals folds each segment, seg_carries folds the G totals into each
+// segment's carry, seg_scan rescans each segment from its carry. A CTA tile
+// is kSegWarps warp sub-tiles of kSegRounds rounds of 32 lanes x 16 bytes;
+// lane l of round r holds V = 16 / sizeof(T) consecutive elements, scanned in
+// the lane, then across the warp (shuffles), then across rounds and warps in
+// order. Every combine keeps the earlier operand on the left.
+constexpr int kSegWarps = 8;
+constexpr int kSegRounds = 8;
+template <typename T>
+constexpr int64_t seg_tile() { return (int64_t)kSegWarps * kSegRounds * 32 * (16 / (int)sizeof(T)); }
+
+// Loads elements [e, e + V) (identity past `hi`) / stores them (none past `hi`).
+template <typename T, int OP>
+NRS_DEV void seg_load(const T* __restrict__ x, int64_t e, int64_t hi, T (&v)[16 / sizeof(T)]) {
+  constexpr int V = 16 / (int)sizeof(T);
+  if (e + V <= hi) {
+    const uint4 u = *reinterpret_cast<const uint4*>(x + e);
+    memcpy(v, &u, 16);
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j) v[j] = (e + j < hi) ? x[e + j] : identity<T, OP>();
+  }
+}
+
+// Segment totals in index order: warp w folds a contiguous run of 512-byte
+// rounds (each round: lanes' V elements in order, then an ordered tree over
+// the lanes), the warps' totals fold in order. Index order matters for float
+// maximum / minimum, whose ties keep the later operand (+0.0 vs -0.0).
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    seg_totals(const T* __restrict__ x, int64_t n, int64_t seg, T* __restrict__ totals) {
+  constexpr int V = 16 / (int)sizeof(T);
+  constexpr int64_t ROUND = 32 * V;
+  __shared__ T wt[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t lo = (int64_t)blockIdx.x * seg;
+  const int64_t hi = (lo + seg < n) ? lo + seg : n;
+  const int64_t nr = (hi - lo + ROUND - 1) / ROUND;
+  const int64_t per = (nr + 7) / 8;
+  const int64_t r0 = w * per, r1 = (r0 + per < nr) ? r0 + per : nr;
+  constexpr int U = 8;  // rounds loaded before any is folded
+  T acc = identity<T, OP>();
+  for (int64_t r = r0; r < r1; r += U) {
+    T v[U][V];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (r + u < r1) {
+        seg_load<T, OP>(x, lo + (r + u) * ROUND + lane * V, hi, v[u]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) v[u][j] = identity<T, OP>();
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      T s = v[u][0];
+#pragma unroll
+      for (int j = 1; j < V; ++j) s = apply<T, OP>(s, v[u][j]);
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const T o = __shfl_down_sync(0xffffffffu, s, off);
+        if ((lane & (2 * off - 1)) == 0) s = apply<T, OP>(s, o);
+      }
+      acc = apply<T, OP>(acc, __shfl_sync(0xffffffffu, s, 0));
+    }
+  }
+  if (lane == 0) wt[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T r = wt[0];
+    for (int i = 1; i < 8; ++i) r = apply<T, OP>(r, wt[i]);
+    totals[blockIdx.x] = r;
+  }
+}
+
+// carries[g] = seed (op) totals[0] (op) ... (op) totals[g - 1] (identity in
+// place of an absent seed); with `final_out`, seed (op) all totals there. One
+// warp, g <= 1024: lane l folds the run [l*per, (l+1)*per) in order, an
+// ordered warp scan gives each run's carry, then lane l writes its run's.
+template <typename T, int OP>
+__global__ void __launch_bounds__(32)
+    seg_carries(const T* __restrict__ totals, int g, int has_seed, Seed seed,
+                T* __restrict__ carries, T* __restrict__ final_out) {
+  __shared__ T tot[1024];
+  const int lane = threadIdx.x;
+  for (int i = lane; i < g; i += 32) tot[i] = totals[i];
+  __syncwarp();
+  const int per = (g + 31) / 32;
+  const int a = lane * per, b = (a + per < g) ? a + per : g;
+  T run = identity<T, OP>();
+  for (int i = a; i < b; ++i) run = apply<T, OP>(run, tot[i]);
+  T inc = run;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const T o = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc = apply<T, OP>(o, inc);
+  }
+  const T s0 = has_seed ? seed.get<T>() : identity<T, OP>();
+  const T ex = __shfl_up_sync(0xffffffffu, inc, 1);
+  T c = lane == 0 ? s0 : apply<T, OP>(s0, ex);
+  if (final_out) {
+    if (lane == 31) *final_out = apply<T, OP>(s0, inc);
+    return;
+  }
+  for (int i = a; i < b; ++i) {
+    carries[i] = c;
+    c = apply<T, OP>(c, tot[i]);
+  }
+}
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kSegWarps * 32)
+    seg_scan(const T* __restrict__ x, int64_t n, int64_t seg, const T* __restrict__ carries,
+             T* __restrict__ out) {
+  constexpr int V = 16 / (int)sizeof(T);
+  constexpr int R = kSegRounds;
+  constexpr int64_t TILE = seg_tile<T>();
+  constexpr int64_t SUB = (int64_t)R * 32 * V;  // elements per warp sub-tile
+  __shared__ T wt[2][kSegWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t lo = (int64_t)blockIdx.x * seg;
+  const int64_t hi = (lo + seg < n) ? lo + seg : n;
+  T carry = carries[blockIdx.x];
+  int par = 0;
+  for (int64_t base = lo; base < hi; base += TILE, par ^= 1) {
+    const int64_t sb = base + w * SUB;
+    T v[R][V];
+#pragma unroll
+    for (int r = 0; r < R; ++r) seg_load<T, OP>(x, sb + (int64_t)r * 32 * V + lane * V, hi, v[r]);
+    // in-lane prefixes, then the lanes' exclusive prefix and each round's total
+    T ex[R], rt[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+#pragma unroll
+      for (int j = 1; j < V; ++j) v[r][j] = apply<T, OP>(v[r][j - 1], v[r][j]);
+      T inc = v[r][V - 1];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const T o = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc = apply<T, OP>(o, inc);
+      }
+      rt[r] = __shfl_sync(0xffffffffu, inc, 31);
+      const T e = __shfl_up_sync(0xffffffffu, inc, 1);
+      ex[r] = lane == 0 ? identity<T, OP>() : e;
+    }
+    T sub = rt[0];
+#pragma unroll
+    for (int r = 1; r < R; ++r) sub = apply<T, OP>(sub, rt[r]);
+    if (lane == 0) wt[par][w] = sub;
+    __syncthreads();
+    T run = carry;
+    for (int i = 0; i < w; ++i) run = apply<T, OP>(run, wt[par][i]);
+    T next = carry;
+#pragma unroll
+    for (int i = 0; i < kSegWarps; ++i) next = apply<T, OP>(next, wt[par][i]);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const T b = lane == 0 ? run : apply<T, OP>(run, ex[r]);
+      T o[V];
+#pragma unroll
+      for (int j = 0; j < V; ++j) o[j] = apply<T, OP>(b, v[r][j]);
+      const int64_t e = sb + (int64_t)r * 32 * V + lane * V;
+      if (e + V <= hi) {
+        uint4 u;
+        memcpy(&u, o, 16);
+        *reinterpret_cast<uint4*>(out + e) = u;
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j)
+          if (e + j < hi) out[e + j] = o[j];
+      }
+      run = apply<T, OP>(run, rt[r]);
+    }
+    carry = next;
+  }
+}
+
 template <typename T, int OP>
 __global__ void seed_combine(T* out, Seed seed) {
   out[0] = apply<T, OP>(seed.get<T>(), out[0]);
@@ -910,6 +1089,17 @@ int flat_scan_t(nrs_handle* h, const T* x, int64_t n, int has_seed, Seed seed, T
   if (!ws) return st;
   T* totals = ws;
   T* carries = ws + nchunks + 1;
+  if ((reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    // Segments: a whole number of tiles each, at most two per SM.
+    const int64_t tiles = (n + seg_tile<T>() - 1) / seg_tile<T>();
+    const int64_t gmax = (int64_t)h->num_sms * 2 < 1024 ? (int64_t)h->num_sms * 2 : 1024;
+    const int64_t seg = ((tiles + gmax - 1) / gmax) * seg_tile<T>();
+    const int g = (int)((n + seg - 1) / seg);
+    seg_totals<T, OP><<<g, 256, 0, h->stream>>>(x, n, seg, totals);
+    seg_carries<T, OP><<<1, 32, 0, h->stream>>>(totals, g, has_seed, seed, carries, final_out);
+    if (!final_out) seg_scan<T, OP><<<g, kSegWarps * 32, 0, h->stream>>>(x, n, seg, carries, out);
+    return nrs_after_launch(h, "flat scan");
+  }
   const int grid = (int)(nchunks < (int64_t)h->num_sms * 8 ? nchunks : (int64_t)h->num_sms * 8);
   flat_chunk_totals<T, OP><<<grid, 256, 0, h->stream>>>(x, n, totals);
   flat_chunk_carries<T, OP><<<1, 1024, 0, h->stream>>>(totals, nchunks, has_seed, seed, carries, final_out);
