@@ -74,6 +74,25 @@ def test_argmax_reference_examples_and_nan(K, ora):
     assert int(to_np(K.argmin(_dev(x)))[0]) == ora.axis_arg(x, None, False)[0]
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_argmax_axis_nan_and_zero_ties(K, ora, dtype):
+    """Lane pipelines (axis length >= 256, >= 64 lanes): NaNs are skipped
+    unless a lane starts with one, an all-NaN lane gives 0, and among equal
+    extremes (+0.0 / -0.0 included) the first index wins."""
+    r = np.random.default_rng(11)
+    x = r.choice(np.array([-0.0, 0.0, -1.0, -2.0], dtype=dtype), (300, 4100))
+    x[r.random(x.shape) < 0.01] = np.nan
+    x[5, 0] = np.nan            # lane 5 along axis 1 starts with NaN
+    x[:, 7] = np.nan            # column 7: an all-NaN lane along axis 0
+    x[9, :] = np.nan            # row 9: an all-NaN lane along axis 1
+    x[0, 3] = np.nan            # column 3 starts with NaN along axis 0
+    xd = _dev(x)
+    for want_max, fn in ((True, K.argmax), (False, K.argmin)):
+        for axis in (0, 1):
+            np.testing.assert_array_equal(to_np(fn(xd, axis=axis)), ora.axis_arg(x, axis, want_max))
+            np.testing.assert_array_equal(to_np(fn(xd.t(), axis=axis)), ora.axis_arg(x.T, axis, want_max))
+
+
 def test_argmax_large_flat(K, ora):
     x = np.random.default_rng(9).integers(-1000, 1000, 5_000_001).astype(np.int64)
     xd = _dev(x)
