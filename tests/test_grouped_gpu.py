@@ -65,7 +65,10 @@ def test_grouped_matches_individual_and_oracle(K, ora):
             Cdd, ab = ora.gemm_dd(to_np(a).astype(np.float64), to_np(b).astype(np.float64))
             err = np.max(np.abs(to_np(got).astype(np.float64) - Cdd) / ab)
             assert err <= 1e-5
-        if k < 8 * max(m, n):  # unsplit variants: identical tile arithmetic
+        # Unsplit f32 tiles: identical arithmetic to the plain SIMT GEMM. (The
+        # plain f64 DMMA GEMM may split k to fill the GPU, so f64 is held to
+        # the double-double bound above.)
+        if a.dtype == torch.float32 and k < 8 * max(m, n):
             assert torch.equal(got.view(torch.int64 if a.dtype == torch.float64 else torch.int32),
                                ref.view(torch.int64 if a.dtype == torch.float64 else torch.int32))
     for x, op, out in reds:
