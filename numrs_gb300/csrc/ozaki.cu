@@ -41,6 +41,7 @@
 // data ~29% of its time and for the epilogue ~8%.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
 // word, drains its own copies and MMAs (bounded), frees TMEM and returns.
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -550,10 +551,12 @@ __device__ __forceinline__ unsigned __int128 digit_offset(int S, int b) {
   for (int t = 0; t < S; ++t) c += (unsigned __int128)(1u << (b - 1)) << (kTopOf(b) - b * t);
   return c;
 }
-__device__ __forceinline__ int digit_at(unsigned __int128 Z, int t, int b) {
-  const int p = kTopOf(b) - b * t;
+// B is a template argument so that every digit position is a constant shift.
+template <int B>
+__device__ __forceinline__ int digit_at(unsigned __int128 Z, int t) {
+  const int p = kTopOf(B) - B * t;
   const int f = (int)(uint32_t)(uint64_t)(Z >> p);
-  return (t == 0 ? f : (f & ((1 << b) - 1))) - (1 << (b - 1));
+  return (t == 0 ? f : (f & ((1 << B) - 1))) - (1 << (B - 1));
 }
 
 __device__ __forceinline__ uint32_t bf16_of_int(int v) {
@@ -562,11 +565,12 @@ __device__ __forceinline__ uint32_t bf16_of_int(int v) {
 }
 
 // A (m x k) -> slices [S][m][kpad], K-major; zero beyond k. A thread takes 8
-// consecutive k of one row (kpad is a multiple of 8) and writes one 16-byte
-// vector per slice.
+// consecutive k of one row (kpad is a multiple of 8; four 16-byte loads when
+// aligned) and writes one 16-byte vector per slice.
+template <int b, bool VEC>
 __global__ void __launch_bounds__(256)
     slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda, int64_t kpad,
-               const int* __restrict__ ea, int S, int b, uint16_t* __restrict__ out) {
+               const int* __restrict__ ea, int S, uint16_t* __restrict__ out) {
   const int64_t gpr = kpad / 8;
   const int64_t total = m * gpr;
   const unsigned __int128 C = digit_offset(S, b);
@@ -577,13 +581,25 @@ __global__ void __launch_bounds__(256)
     uint32_t pk[OZ_MAX_SLICES][4];
 #pragma unroll
     for (int t = 0; t < OZ_MAX_SLICES; ++t) pk[t][0] = pk[t][1] = pk[t][2] = pk[t][3] = 0;
+    double x[8];
+    const double* row = A + i * lda + j0;
+    if (VEC && j0 + 8 <= k) {  // four 16-byte loads
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double2 d2 = reinterpret_cast<const double2*>(row)[q];
+        x[2 * q] = d2.x;
+        x[2 * q + 1] = d2.y;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) x[q] = j0 + q < k ? row[q] : 0.0;
+    }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const int64_t j = j0 + q;
-      const unsigned __int128 Z = (unsigned __int128)(j < k ? fixed126(A[i * lda + j], e) : (__int128)0) + C;
+      const unsigned __int128 Z = (unsigned __int128)fixed126(x[q], e) + C;
 #pragma unroll
       for (int t = 0; t < OZ_MAX_SLICES; ++t)
-        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at(Z, t, b)) << (16 * (q & 1));
+        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at<b>(Z, t)) << (16 * (q & 1));
     }
     uint16_t* o = out + i * kpad + j0;
 #pragma unroll
@@ -599,9 +615,10 @@ __global__ void __launch_bounds__(256)
 // words] (the pad word keeps both phases free of bank conflicts), then every
 // thread writes one 16-byte vector (8 k of one n row) per slice.
 constexpr int kSliceColK = 64, kSliceColN = 32, kSliceColPitch = kSliceColK / 2 + 1;
+template <int b>
 __global__ void __launch_bounds__(256)
     slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb, int64_t kpad,
-               const int* __restrict__ eb, int S, int b, uint16_t* __restrict__ out) {
+               const int* __restrict__ eb, int S, uint16_t* __restrict__ out) {
   extern __shared__ uint32_t tile[];  // [S][32][33]
   const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -617,9 +634,11 @@ __global__ void __launch_bounds__(256)
           (unsigned __int128)(kk < k && nn < n ? fixed126(B[kk * ldb + nn], e) : (__int128)0) + C;
       const unsigned __int128 Z1 =
           (unsigned __int128)(kk + 1 < k && nn < n ? fixed126(B[(kk + 1) * ldb + nn], e) : (__int128)0) + C;
-      for (int t = 0; t < S; ++t)
-        tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
-            bf16_of_int(digit_at(Z0, t, b)) | (bf16_of_int(digit_at(Z1, t, b)) << 16);
+#pragma unroll
+      for (int t = 0; t < OZ_MAX_SLICES; ++t)
+        if (t < S)
+          tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+              bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
     }
   }
   __syncthreads();
@@ -718,16 +737,21 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   exponents_from_bits<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(colmax, n, eb);
   const int64_t groups = m * (kpad / 8);
   const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
-  slice_rows<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, b, sa);
+  // 16-byte row loads when every row start is 16-byte aligned.
+  const bool vec = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && (lda % 2 == 0);
+  auto rows_kern = vec ? (b == 8 ? slice_rows<8, true> : b == 7 ? slice_rows<7, true> : slice_rows<6, true>)
+                       : (b == 8 ? slice_rows<8, false> : b == 7 ? slice_rows<7, false> : slice_rows<6, false>);
+  auto cols_kern = b == 8 ? slice_cols<8> : b == 7 ? slice_cols<7> : slice_cols<6>;
+  rows_kern<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
   const size_t col_smem = (size_t)S * kSliceColN * kSliceColPitch * 4;
-  static bool col_attr = false;
-  if (!col_attr) {
-    cudaFuncSetAttribute(slice_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)((size_t)OZ_MAX_SLICES * kSliceColN * kSliceColPitch * 4));
-    col_attr = true;
-  }
+  static std::once_flag col_attr;
+  std::call_once(col_attr, [] {
+    for (auto kern : {slice_cols<8>, slice_cols<7>, slice_cols<6>})
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((size_t)OZ_MAX_SLICES * kSliceColN * kSliceColPitch * 4));
+  });
   dim3 g2((unsigned)((n + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
-  slice_cols<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, b, sb);
+  cols_kern<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, sb);
   if ((st = nrs_after_launch(h, "ozaki slicing"))) return st;
 
   CUtensorMap mapA, mapB;
