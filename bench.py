@@ -37,6 +37,7 @@ F32_SEED, I64_SEED = 3, 4
 A_SCALE, B_SHIFT = 0.5, -0.25
 
 
+E2E_BLOCKS = 4  # row blocks of the i64 upload in the end-to-end step
 CONFIG = {"workload": "16384x16384 f32 N(0,1) + i64 U[-2^20,2^20): axis-0/1 sum/mean/max (f32), "
                       "sum/max (i64), row-major and transposed-stride views, + fused exp(0.5x-0.25); "
                       "one step = 21 launches",
@@ -585,47 +586,106 @@ def main():
         # Two extra handles on their own non-blocking streams carry the bulk
         # copies (H2D and D2H use separate copy engines); CUDA events order
         # them against the compute on the current stream, so the i64 upload
-        # and the ufunc download overlap the f32 reductions.
+        # and the ufunc download overlap the f32 reductions. The i64 array
+        # lands in E2E_BLOCKS row blocks and each block is reduced as soon as
+        # it is in: reductions whose lanes are rows write their block's slice
+        # of the result, the others a per-block partial that one more
+        # nrs_reduce folds over the blocks (integer sum and max: exact in any
+        # grouping), so only the last block's reductions trail the link.
         h_in, h_out = C.c_void_p(), C.c_void_p()
         L.check(lib.nrs_create(local, C.byref(h_in)))
         L.check(lib.nrs_create(local, C.byref(h_out)))
         s_in = torch.cuda.ExternalStream(lib.nrs_get_stream(h_in))
         s_out = torch.cuda.ExternalStream(lib.nrs_get_stream(h_out))
-        ev32, ev64, evy = (torch.cuda.Event() for _ in range(3))
+        ev32, evy = torch.cuda.Event(), torch.cuda.Event()
+        ev64 = [torch.cuda.Event() for _ in range(E2E_BLOCKS)]
         cur = torch.cuda.current_stream()
         f32_ops = [fn for cls, _, fn in ops if cls.endswith("/f32") and not cls.startswith("exp")]
-        i64_ops = [fn for cls, _, fn in ops if cls.endswith("/i64")]
+        rb = R // E2E_BLOCKS
+        blk = rb * C_ * 8
+        # (view, op, axis, lanes are x64 rows) for the eight i64 reductions
+        i64_red = [(vn, code, axis, axis == (1 if vn == "rm" else 0))
+                   for vn in ("rm", "tr") for code in (L.SUM, L.MAX) for axis in (0, 1)]
+        i64_res = [torch.empty(C_, dtype=torch.int64, device=x64.device) for _ in i64_red]
+        i64_part = [None if rows else torch.empty((E2E_BLOCKS, C_), dtype=torch.int64, device=x64.device)
+                    for (_, _, _, rows) in i64_red]
+
+        # Three more handles on their own streams: a block's eight reductions
+        # run on four streams at once (the lanes-along-rows ones use few CTAs
+        # on a quarter of the rows, so alone they would not fill the GPU).
+        hx = [h]
+        for _ in range(3):
+            hh = C.c_void_p()
+            L.check(lib.nrs_create(local, C.byref(hh)))
+            hx.append(hh)
+        sx = [cur] + [torch.cuda.ExternalStream(lib.nrs_get_stream(hh)) for hh in hx[1:]]
+        evx = [torch.cuda.Event() for _ in sx]
+        ev_done = torch.cuda.Event()
+
+        def reduce_into(hh, view, code, axis, out):
+            L.check(lib.nrs_reduce(hh, L.I64, code, view.dim(), L.i64_array(view.shape),
+                                   L.i64_array(view.stride()), axis, 0, C.c_void_p(view.data_ptr()),
+                                   C.c_void_p(out.data_ptr())), hh)
+
+        def i64_block(b):
+            xb = x64[b * rb:(b + 1) * rb]
+            for k in range(len(sx)):
+                sx[k].wait_event(ev64[b])
+            for j, (vn, code, axis, rows) in enumerate(i64_red):
+                v = xb if vn == "rm" else xb.t()
+                reduce_into(hx[j % len(hx)], v, code, axis,
+                            i64_res[j][b * rb:(b + 1) * rb] if rows else i64_part[j][b])
+
         res_host = {}
 
         def d2h_small(r, key):
+            # result reads go on the download stream, after ev_done
             nbytes = r.numel() * r.element_size()
             if key not in res_host:
                 res_host[key] = torch.empty(r.shape, dtype=r.dtype, pin_memory=True)
-            L.check(lib.nrs_memcpy_d2h(h, C.c_void_p(res_host[key].data_ptr()), C.c_void_p(r.data_ptr()),
-                                       nbytes), h)
+            L.check(lib.nrs_memcpy_d2h(h_out, C.c_void_p(res_host[key].data_ptr()), C.c_void_p(r.data_ptr()),
+                                       nbytes), h_out)
             return nbytes
 
         def e2e_step():
             L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x32.data_ptr()), hp32, nb32), h_in)
             ev32.record(s_in)
-            L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x64.data_ptr()), hp64, nb64), h_in)
-            ev64.record(s_in)
+            for b in range(E2E_BLOCKS):
+                L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x64.data_ptr() + b * blk),
+                                           C.c_void_p(hp64.value + b * blk), blk), h_in)
+                ev64[b].record(s_in)
             cur.wait_event(ev32)
             K.exp_affine(x32, A_SCALE, B_SHIFT, out=y)
             evy.record(cur)
             s_out.wait_event(evy)
             L.check(lib.nrs_memcpy_d2h(h_out, hy, C.c_void_p(y.data_ptr()), nb32), h_out)
             d2h = nb32
-            for i, fn in enumerate(f32_ops):
-                d2h += d2h_small(fn(), ("f32", i))
-            cur.wait_event(ev64)
-            for i, fn in enumerate(i64_ops):
-                d2h += d2h_small(fn(), ("i64", i))
-            for hh in (h_in, h_out, h):
+            f32_res = [fn() for fn in f32_ops]
+            for b in range(E2E_BLOCKS):
+                i64_block(b)
+            for k in range(1, len(sx)):
+                evx[k].record(sx[k])
+                cur.wait_event(evx[k])
+            for j, (_, code, _, rows) in enumerate(i64_red):
+                if not rows:
+                    reduce_into(h, i64_part[j], code, 0, i64_res[j])
+            ev_done.record(cur)
+            s_out.wait_event(ev_done)
+            for i, r in enumerate(f32_res):
+                d2h += d2h_small(r, ("f32", i))
+            for j, r in enumerate(i64_res):
+                d2h += d2h_small(r, ("i64", j))
+            for hh in (h_in, h_out, *hx):
                 L.check(lib.nrs_synchronize(hh), hh)
             return d2h
 
         e2e_step()
+        # the blocked i64 reductions give the whole-array results bit for bit
+        for j, (vn, code, axis, _) in enumerate(i64_red):
+            want = K.reduce(x64 if vn == "rm" else x64.t(), code, axis)
+            if not torch.equal(want, i64_res[j]):
+                raise RuntimeError(f"blocked i64 reduction {j} differs from the whole-array one")
+        e2e_step()  # a second untimed step: the first after the check ran long once
         barrier()
         t0 = time.perf_counter()
         e_steps = max(2, min(args.steps, 5))
@@ -638,8 +698,8 @@ def main():
                       "ms_per_step": round(dt * 1e3, 3)}
         for p in (hp32, hp64, hy):
             lib.nrs_host_free(h, p)
-        lib.nrs_destroy(h_in)
-        lib.nrs_destroy(h_out)
+        for hh in (h_in, h_out, *hx[1:]):
+            lib.nrs_destroy(hh)
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
