@@ -89,6 +89,7 @@ LANE_CASES = [
     ((200, 300), 1, "t"),      # transposed view: column pipeline
     ((3, 260, 136), 1, None),  # batched columns
     ((3, 40, 300), 2, None),   # collapsed batch rows
+    ((1000, 260), 1, None),    # many rows: rows per CTA chosen at launch, partial last CTA
     ((3, 40, 300), 0, None),   # short axis: generic
     ((50, 400), 1, "s"),       # strided columns: generic
     ((1000,), 0, None),        # one lane
@@ -133,9 +134,10 @@ def test_axis_nan_and_signed_zero(K, ora, dtype):
             _same(to_np(K.ufunc_reduce(op, _dev(x), axis)).ravel(), ora.ufunc_reduce(OPS[op], x, axis))
 
 
+@pytest.mark.parametrize("offset", [0, 1])  # 1: a view one element in (not 16-byte aligned)
 @pytest.mark.parametrize("n", [1, 5, 63, 64, 4095, 4096, 4097, 8191, 8192, 8193, 100003, (1 << 22) + 5])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int64])
-def test_flat_accumulate(K, ora, n, dtype):
+def test_flat_accumulate(K, ora, n, dtype, offset):
     r = np.random.default_rng(n)
     for op in OPS:
         if op == "divide" and dtype == np.int64:
@@ -147,7 +149,8 @@ def test_flat_accumulate(K, ora, n, dtype):
             x[r.random(n) < 1e-3] = np.nan
             x[r.random(n) < 1e-3] = -0.0
             x[r.random(n) < 1e-3] = 0.0
-        got = to_np(K.ufunc_accumulate(op, _dev(x)))
+        xd = _dev(np.concatenate([np.zeros(offset, dtype), x]))[offset:]
+        got = to_np(K.ufunc_accumulate(op, xd))
         ref = ora.accumulate(OPS[op], x)
         reassoc = np.dtype(dtype).kind == "f" and op in ("add", "multiply") and n >= 64
         if not reassoc:
@@ -163,9 +166,10 @@ def test_flat_accumulate(K, ora, n, dtype):
             assert np.all(np.abs(got.astype(np.float64) - exact) <= tol + np.finfo(dtype).tiny)
 
 
+@pytest.mark.parametrize("offset", [0, 1])
 @pytest.mark.parametrize("n", [1, 7, 5000, 65537, (1 << 22) + 3])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int64])
-def test_flat_reduce(K, ora, n, dtype):
+def test_flat_reduce(K, ora, n, dtype, offset):
     r = np.random.default_rng(7 + n)
     for op in OPS:
         if op == "divide" and dtype == np.int64:
@@ -177,7 +181,8 @@ def test_flat_reduce(K, ora, n, dtype):
             x[r.integers(0, n, 3)] = -0.0
             x[r.integers(0, n, 3)] = 0.0
         for init in (None, 2 if dtype == np.int64 else 0.5):
-            got = to_np(K.ufunc_reduce(op, _dev(x), None, initial=init))
+            xd = _dev(np.concatenate([np.zeros(offset, dtype), x]))[offset:]
+            got = to_np(K.ufunc_reduce(op, xd, None, initial=init))
             ref = ora.ufunc_reduce(OPS[op], x, None, init)
             if np.dtype(dtype).kind == "f" and op in ("add", "multiply"):
                 # seed (op) the tiered flat sum / product: within the flat
