@@ -122,9 +122,11 @@ __device__ __forceinline__ bool arg_better(T v, int64_t i, T w, int64_t j) {
   return v == w && i < j;
 }
 
-// One candidate per 8192-element chunk, one warp per chunk with eight
-// consecutive elements per thread and step (the flat_partials layout below).
-// arg_better is a strict preference, so the scan and combine order are free.
+// One warp per 8192-element chunk with eight consecutive elements per thread
+// and step (the flat_partials layout below); each warp keeps the best of all
+// its chunks and writes one candidate, part[global warp index] (idx -1: the
+// warp had no chunk). arg_better is a strict preference, so the scan and
+// combine order are free.
 template <typename T, bool MAX, bool VEC>
 __global__ void __launch_bounds__(256, 4)
     arg_partials(const T* __restrict__ x, int64_t n, ArgCand<T>* __restrict__ part) {
@@ -133,7 +135,10 @@ __global__ void __launch_bounds__(256, 4)
   const int64_t nchunks = (n + kChunk - 1) / kChunk;
   const int t = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  T wbv = T(0);
+  int64_t wgi = -1;
+  for (int64_t c = wid; c < nchunks; c += nwarps) {
     const int64_t lo = c * kChunk;
     const int64_t len = (n - lo) < kChunk ? (n - lo) : kChunk;
     const T* p = x + lo + LPT * t;
@@ -185,8 +190,12 @@ __global__ void __launch_bounds__(256, 4)
         gi = oi;
       }
     }
-    if (t == 0) part[c] = ArgCand<T>{bv, gi};
+    if (gi >= 0 && arg_better<T, MAX>(bv, gi, wbv, wgi)) {
+      wbv = bv;
+      wgi = gi;
+    }
   }
+  if (t == 0) part[wid] = ArgCand<T>{wbv, wgi};
 }
 
 // Combines the chunk candidates. arg_better is a strict preference (better
@@ -587,6 +596,7 @@ __global__ void __launch_bounds__(256, kFlatBlocksPerSM)
 // Blocks of 256 threads for one warp per chunk: about the same number of
 // chunks per warp, on a grid that is resident at once.
 inline int flat_warp_grid(int64_t nchunks, int sms) {
+  if (nchunks < 1) return 1;
   const int64_t cap = (int64_t)sms * kFlatBlocksPerSM * 8;  // resident warps
   const int64_t per = (nchunks + cap - 1) / cap;
   const int64_t warps = (nchunks + per - 1) / per;
@@ -959,14 +969,15 @@ template <typename T, bool MAX>
 int flat_arg(nrs_handle* h, int64_t n, const void* x, void* out) {
   const int64_t nchunks = (n + kChunk - 1) / kChunk;
   int st;
-  ArgCand<T>* part = (ArgCand<T>*)nrs_workspace(h, (size_t)(nchunks + 1) * sizeof(ArgCand<T>), &st);
-  if (!part) return st;
   const int grid = flat_warp_grid(nchunks, h->num_sms);
+  const int64_t ncand = (int64_t)grid * 8;  // one candidate per warp
+  ArgCand<T>* part = (ArgCand<T>*)nrs_workspace(h, (size_t)(ncand + 1) * sizeof(ArgCand<T>), &st);
+  if (!part) return st;
   if ((reinterpret_cast<uintptr_t>(x) & 15) == 0)
     arg_partials<T, MAX, true><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
   else
     arg_partials<T, MAX, false><<<grid, 256, 0, h->stream>>>((const T*)x, n, part);
-  arg_finish<T, MAX><<<1, 1024, 0, h->stream>>>((const T*)x, part, nchunks, (int64_t*)out);
+  arg_finish<T, MAX><<<1, 1024, 0, h->stream>>>((const T*)x, part, ncand, (int64_t*)out);
   return nrs_after_launch(h, "flat argmax/argmin");
 }
 

@@ -23,6 +23,9 @@ CASES = {
     "fold_cols_i64_sum": ("i64", L.SUM, 0),
     "fold_cols_i64_max": ("i64", L.MAX, 0),
     "fold_rows_i64_sum": ("i64", L.SUM, 1),
+    "flat_sum_f32": ("f32", L.SUM, None),
+    "flat_max_f32": ("f32", L.MAX, None),
+    "flat_argmax_f32": ("f32", L.ARGMAX, None),
     "exp_affine_f32": ("f32", None, None),
     "ozaki_f64": ("f64", None, None),
     "dmma_f64": ("f64", None, None),
@@ -44,7 +47,7 @@ def main():
     a = ap.parse_args()
     dt, op, axis = CASES[a.case]
     n = a.n
-    if a.case.startswith("fold"):
+    if a.case.startswith("fold") or a.case.startswith("flat"):
         if dt == "f32":
             x = torch.empty((n, n), dtype=torch.float32, device="cuda")
             K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
