@@ -461,10 +461,33 @@ NRS_DEV T fold_seg(uint8_t* row, int cnt, bool first, T acc) {
       T v[SUB];
 #pragma unroll
       for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], blk + 16 * j, 16);
+      if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN)) {
+        // apply's result, with a shorter dependent chain: a sticky flag
+        // records that a NaN has been seen (from then on every prefix is the
+        // canonical NaN), so the value chain is one compare and select (ties
+        // keep the later operand, as apply does). A seeding first element
+        // keeps its own bits, as in the general path.
+        bool nanf = acc != acc;
+        T a = acc;
 #pragma unroll
-      for (int e = 0; e < SUB; ++e) {
-        acc = (e == 0 && f) ? v[0] : apply<T, OP>(acc, v[e]);
-        v[e] = acc;
+        for (int e = 0; e < SUB; ++e) {
+          const T xe = v[e];
+          if (e == 0 && f) {
+            a = xe;
+            nanf = xe != xe;
+          } else {
+            nanf |= xe != xe;
+            a = (OP == NRS_OP_MAX ? (a > xe) : (a < xe)) ? a : xe;
+            v[e] = nanf ? qnan<T>() : a;
+          }
+        }
+        acc = nanf ? qnan<T>() : a;
+      } else {
+#pragma unroll
+        for (int e = 0; e < SUB; ++e) {
+          acc = (e == 0 && f) ? v[0] : apply<T, OP>(acc, v[e]);
+          v[e] = acc;
+        }
       }
 #pragma unroll
       for (int j = 0; j < 8; ++j) memcpy(blk + 16 * j, &v[j * PER16], 16);
