@@ -38,7 +38,7 @@ F32_SEED, I64_SEED = 3, 4
 A_SCALE, B_SHIFT = 0.5, -0.25
 
 
-E2E_BLOCKS = 4  # row blocks of the i64 upload in the end-to-end step
+E2E_BLOCKS = 8  # row blocks of the i64 upload in the end-to-end step
 CONFIG = {"workload": "16384x16384 f32 N(0,1) + i64 U[-2^20,2^20): axis-0/1 sum/mean/max (f32), "
                       "sum/max (i64), row-major and transposed-stride views, + fused exp(0.5x-0.25); "
                       "one step = 21 launches",
@@ -615,7 +615,7 @@ def main():
 
         # Three more handles on their own streams: a block's eight reductions
         # run on four streams at once (the lanes-along-rows ones use few CTAs
-        # on a quarter of the rows, so alone they would not fill the GPU).
+        # on a block's rows, so alone they would not fill the GPU).
         hx = [h]
         for _ in range(3):
             hh = C.c_void_p()
