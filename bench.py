@@ -338,10 +338,10 @@ def reductions_extra_section(K, L):
 
 
 def scan_section(K, L):
-    """Running folds on 16384x16384 f32 N(0,1) (seed 3): cumsum along axis 0
-    (column pipeline), axis 1 (row pipeline) and over the flattened array
-    (chunked parallel scan), each one call; algorithmic bytes = read + write
-    of the array (8 B/elem)."""
+    """Running folds on 16384x16384 f32 N(0,1) (seed 3): cumsum and
+    maximum.accumulate along axis 0 (column pipeline), axis 1 (row pipeline)
+    and over the flattened array (segmented parallel scan), each one call;
+    algorithmic bytes = read + write of the array (8 B/elem)."""
     import torch
     n = R * C_
     stream = torch.cuda.current_stream()
@@ -350,7 +350,9 @@ def scan_section(K, L):
     cases = {"cumsum_axis0": lambda: K.cumsum(x, 0),
              "cumsum_axis1": lambda: K.cumsum(x, 1),
              "cumsum_flat": lambda: K.cumsum(x),
-             "maximum_accumulate_axis1": lambda: K.ufunc_accumulate("maximum", x, 1)}
+             "maximum_accumulate_axis1": lambda: K.ufunc_accumulate("maximum", x, 1),
+             "maximum_accumulate_axis0": lambda: K.ufunc_accumulate("maximum", x, 0),
+             "maximum_accumulate_flat": lambda: K.ufunc_accumulate("maximum", x, None)}
     out = {}
     for name, fn in cases.items():
         ms = _time_ms(fn, 5, stream)

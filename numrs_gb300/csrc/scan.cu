@@ -160,6 +160,40 @@ NRS_DEV int swz(int r, int j) { return r * 128 + ((j ^ (r & 7)) << 4); }
 // Folds one staged column (cols) / row (rows) of a tile into `acc`; with
 // WRITE the prefix values replace the staged ones. `first` seeds the lane
 // from its first element (the tile's element 0).
+// Running fold of N staged values in place (v[e] becomes the prefix through
+// e); `first` seeds the lane from v[0], which keeps its own bits. Float
+// maximum / minimum give apply's result with a shorter dependent chain: a
+// sticky flag records that a NaN has been seen (every later prefix is then
+// the canonical NaN), so the value chain is one compare and select (ties keep
+// the later operand, as apply does).
+template <typename T, int OP, int N>
+NRS_DEV T run_block(T (&v)[N], bool first, T acc) {
+  if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN)) {
+    bool nanf = acc != acc;
+    T a = acc;
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+      const T xe = v[e];
+      if (e == 0 && first) {
+        a = xe;
+        nanf = xe != xe;
+      } else {
+        nanf |= xe != xe;
+        a = (OP == NRS_OP_MAX ? (a > xe) : (a < xe)) ? a : xe;
+        v[e] = nanf ? qnan<T>() : a;
+      }
+    }
+    return nanf ? qnan<T>() : a;
+  } else {
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+      acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
+      v[e] = acc;
+    }
+    return acc;
+  }
+}
+
 template <typename T, int OP, bool WRITE>
 NRS_DEV T fold_col(T* tile, int t, int cnt, bool first, T acc) {
   constexpr int RB = col_rows<T>();
@@ -168,11 +202,7 @@ NRS_DEV T fold_col(T* tile, int t, int cnt, bool first, T acc) {
     T v[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) v[r] = tile[r * LW + t];
-#pragma unroll
-    for (int r = 0; r < RB; ++r) {
-      acc = (r == 0 && first) ? v[0] : apply<T, OP>(acc, v[r]);
-      v[r] = acc;
-    }
+    acc = run_block<T, OP, RB>(v, first, acc);
     if (WRITE) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) tile[r * LW + t] = v[r];
@@ -194,11 +224,7 @@ NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], tile + swz(t, j), 16);
   if (cnt == XB) {
-#pragma unroll
-    for (int e = 0; e < XB; ++e) {
-      acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
-      v[e] = acc;
-    }
+    acc = run_block<T, OP, XB>(v, first, acc);
   } else {
     for (int e = 0; e < cnt; ++e) {
       acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
@@ -461,34 +487,7 @@ NRS_DEV T fold_seg(uint8_t* row, int cnt, bool first, T acc) {
       T v[SUB];
 #pragma unroll
       for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], blk + 16 * j, 16);
-      if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN)) {
-        // apply's result, with a shorter dependent chain: a sticky flag
-        // records that a NaN has been seen (from then on every prefix is the
-        // canonical NaN), so the value chain is one compare and select (ties
-        // keep the later operand, as apply does). A seeding first element
-        // keeps its own bits, as in the general path.
-        bool nanf = acc != acc;
-        T a = acc;
-#pragma unroll
-        for (int e = 0; e < SUB; ++e) {
-          const T xe = v[e];
-          if (e == 0 && f) {
-            a = xe;
-            nanf = xe != xe;
-          } else {
-            nanf |= xe != xe;
-            a = (OP == NRS_OP_MAX ? (a > xe) : (a < xe)) ? a : xe;
-            v[e] = nanf ? qnan<T>() : a;
-          }
-        }
-        acc = nanf ? qnan<T>() : a;
-      } else {
-#pragma unroll
-        for (int e = 0; e < SUB; ++e) {
-          acc = (e == 0 && f) ? v[0] : apply<T, OP>(acc, v[e]);
-          v[e] = acc;
-        }
-      }
+      acc = run_block<T, OP, SUB>(v, f, acc);
 #pragma unroll
       for (int j = 0; j < 8; ++j) memcpy(blk + 16 * j, &v[j * PER16], 16);
     } else {  // the row's last, short block: element by element in place
