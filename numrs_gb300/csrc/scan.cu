@@ -751,6 +751,21 @@ NRS_DEV void seg_load(const T* __restrict__ x, int64_t e, int64_t hi, T (&v)[16 
   }
 }
 
+// Float maximum / minimum in the segmented scans: values combine without
+// NaN checks (ties keep the later operand, as apply does) and a separate
+// flag, ORed along the same order, marks every prefix at or after a NaN;
+// flagged results are the canonical NaN. Without a NaN this is apply bit for
+// bit, and the flag makes the NaN cases so as well. Other ops use apply.
+template <typename T, int OP>
+constexpr bool seg_flagged() {
+  return std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN);
+}
+template <typename T, int OP>
+NRS_DEV T seg_comb(T a, T b) {
+  if constexpr (seg_flagged<T, OP>()) return (OP == NRS_OP_MAX ? (a > b) : (a < b)) ? a : b;
+  else return apply<T, OP>(a, b);
+}
+
 // Segment totals in index order: warp w folds a contiguous run of 512-byte
 // rounds (each round: lanes' V elements in order, then an ordered tree over
 // the lanes), the warps' totals fold in order. Index order matters for float
@@ -769,6 +784,7 @@ __global__ void __launch_bounds__(256)
   const int64_t r0 = w * per, r1 = (r0 + per < nr) ? r0 + per : nr;
   constexpr int U = 8;  // rounds loaded before any is folded
   T acc = identity<T, OP>();
+  bool nanf = false;
   for (int64_t r = r0; r < r1; r += U) {
     T v[U][V];
 #pragma unroll
@@ -782,22 +798,29 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
+      if constexpr (seg_flagged<T, OP>()) {
+#pragma unroll
+        for (int j = 0; j < V; ++j) nanf |= v[u][j] != v[u][j];
+      }
       T s = v[u][0];
 #pragma unroll
-      for (int j = 1; j < V; ++j) s = apply<T, OP>(s, v[u][j]);
+      for (int j = 1; j < V; ++j) s = seg_comb<T, OP>(s, v[u][j]);
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
         const T o = __shfl_down_sync(0xffffffffu, s, off);
-        if ((lane & (2 * off - 1)) == 0) s = apply<T, OP>(s, o);
+        if ((lane & (2 * off - 1)) == 0) s = seg_comb<T, OP>(s, o);
       }
-      acc = apply<T, OP>(acc, __shfl_sync(0xffffffffu, s, 0));
+      acc = seg_comb<T, OP>(acc, __shfl_sync(0xffffffffu, s, 0));
     }
   }
   if (lane == 0) wt[w] = acc;
-  __syncthreads();
+  const int anynan = __syncthreads_or(nanf);
   if (threadIdx.x == 0) {
     T r = wt[0];
-    for (int i = 1; i < 8; ++i) r = apply<T, OP>(r, wt[i]);
+    for (int i = 1; i < 8; ++i) r = seg_comb<T, OP>(r, wt[i]);
+    if constexpr (seg_flagged<T, OP>()) {
+      if (anynan) r = qnan<T>();
+    }
     totals[blockIdx.x] = r;
   }
 }
@@ -846,6 +869,7 @@ __global__ void __launch_bounds__(kSegWarps * 32)
   constexpr int64_t TILE = seg_tile<T>();
   constexpr int64_t SUB = (int64_t)R * 32 * V;  // elements per warp sub-tile
   __shared__ T wt[2][kSegWarps];
+  __shared__ int wtf[2][kSegWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t lo = (int64_t)blockIdx.x * seg;
   const int64_t hi = (lo + seg < n) ? lo + seg : n;
@@ -856,17 +880,33 @@ __global__ void __launch_bounds__(kSegWarps * 32)
     T v[R][V];
 #pragma unroll
     for (int r = 0; r < R; ++r) seg_load<T, OP>(x, sb + (int64_t)r * 32 * V + lane * V, hi, v[r]);
-    // in-lane prefixes, then the lanes' exclusive prefix and each round's total
+    // in-lane prefixes, then the lanes' exclusive prefix and each round's
+    // total; with flags (float max / min): a per-element NaN-prefix bit in
+    // `lf`, the lanes' exclusive NaN bit and each round's NaN bit
+    constexpr bool FL = seg_flagged<T, OP>();
     T ex[R], rt[R];
+    uint32_t lf[R], exf = 0, rtf = 0;  // bit j of lf[r]: a NaN at or before element j of the lane
 #pragma unroll
     for (int r = 0; r < R; ++r) {
+      lf[r] = 0;
+      if constexpr (FL) {
+        bool f = false;
 #pragma unroll
-      for (int j = 1; j < V; ++j) v[r][j] = apply<T, OP>(v[r][j - 1], v[r][j]);
+        for (int j = 0; j < V; ++j) {
+          f |= v[r][j] != v[r][j];
+          lf[r] |= (uint32_t)f << j;
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, f);
+        exf |= (uint32_t)((m & ((1u << lane) - 1u)) != 0) << r;
+        rtf |= (uint32_t)(m != 0) << r;
+      }
+#pragma unroll
+      for (int j = 1; j < V; ++j) v[r][j] = seg_comb<T, OP>(v[r][j - 1], v[r][j]);
       T inc = v[r][V - 1];
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
         const T o = __shfl_up_sync(0xffffffffu, inc, off);
-        if (lane >= off) inc = apply<T, OP>(o, inc);
+        if (lane >= off) inc = seg_comb<T, OP>(o, inc);
       }
       rt[r] = __shfl_sync(0xffffffffu, inc, 31);
       const T e = __shfl_up_sync(0xffffffffu, inc, 1);
@@ -874,20 +914,38 @@ __global__ void __launch_bounds__(kSegWarps * 32)
     }
     T sub = rt[0];
 #pragma unroll
-    for (int r = 1; r < R; ++r) sub = apply<T, OP>(sub, rt[r]);
-    if (lane == 0) wt[par][w] = sub;
+    for (int r = 1; r < R; ++r) sub = seg_comb<T, OP>(sub, rt[r]);
+    if (lane == 0) {
+      wt[par][w] = sub;
+      wtf[par][w] = rtf != 0;
+    }
     __syncthreads();
+    const bool cf = FL && carry != carry;  // the carry is the canonical NaN once flagged
     T run = carry;
-    for (int i = 0; i < w; ++i) run = apply<T, OP>(run, wt[par][i]);
+    bool runf = cf;
+    for (int i = 0; i < w; ++i) {
+      run = seg_comb<T, OP>(run, wt[par][i]);
+      runf |= wtf[par][i] != 0;
+    }
     T next = carry;
+    bool nextf = cf;
 #pragma unroll
-    for (int i = 0; i < kSegWarps; ++i) next = apply<T, OP>(next, wt[par][i]);
+    for (int i = 0; i < kSegWarps; ++i) {
+      next = seg_comb<T, OP>(next, wt[par][i]);
+      nextf |= wtf[par][i] != 0;
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const T b = lane == 0 ? run : apply<T, OP>(run, ex[r]);
+      const T b = lane == 0 ? run : seg_comb<T, OP>(run, ex[r]);
+      const bool bf = runf || ((exf >> r) & 1u);
       T o[V];
 #pragma unroll
-      for (int j = 0; j < V; ++j) o[j] = apply<T, OP>(b, v[r][j]);
+      for (int j = 0; j < V; ++j) {
+        o[j] = seg_comb<T, OP>(b, v[r][j]);
+        if constexpr (FL) {
+          if (bf || ((lf[r] >> j) & 1u)) o[j] = qnan<T>();
+        }
+      }
       const int64_t e = sb + (int64_t)r * 32 * V + lane * V;
       if (e + V <= hi) {
         uint4 u;
@@ -898,9 +956,13 @@ __global__ void __launch_bounds__(kSegWarps * 32)
         for (int j = 0; j < V; ++j)
           if (e + j < hi) out[e + j] = o[j];
       }
-      run = apply<T, OP>(run, rt[r]);
+      run = seg_comb<T, OP>(run, rt[r]);
+      runf = runf || ((rtf >> r) & 1u);
     }
     carry = next;
+    if constexpr (FL) {
+      if (nextf) carry = qnan<T>();
+    }
   }
 }
 
