@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(64)
   if (t == 0)
     for (int s = 0; s < STAGES && s < n_tiles; ++s) load(s, s);
   T best = T(0);
-  int64_t bi = 0;
+  int bt = 0, be = 0;  // tile and position of the best so far (32-bit selects)
   const int sw = t & 7;
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
@@ -474,10 +474,10 @@ __global__ void __launch_bounds__(64)
       if (e < cnt) {
         if (it == 0 && e == 0) {
           best = v[0];
-          bi = 0;
         } else if (MAX ? (v[e] > best) : (v[e] < best)) {
           best = v[e];
-          bi = j0 + e;
+          bt = (int)it;
+          be = e;
         }
       }
     }
@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(64)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = bi;
+  if (lane < lanes) out[(int64_t)batch * lanes + lane] = (int64_t)bt * TB + be;
 }
 
 constexpr int kStages = 8;
