@@ -469,6 +469,7 @@ __global__ void __launch_bounds__(64)
     }
     // Unrolled over the tile with constant indices (v stays in registers);
     // positions past the end of the axis are skipped.
+    int bet = -1;  // position of this tile's improvement, if any
 #pragma unroll
     for (int e = 0; e < TB; ++e) {
       if (e < cnt) {
@@ -476,10 +477,13 @@ __global__ void __launch_bounds__(64)
           best = v[0];
         } else if (MAX ? (v[e] > best) : (v[e] < best)) {
           best = v[e];
-          bt = (int)it;
-          be = e;
+          bet = e;
         }
       }
+    }
+    if (bet >= 0) {
+      bt = (int)it;
+      be = bet;
     }
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + STAGES < n_tiles) load(s, it + STAGES);
