@@ -578,9 +578,6 @@ __global__ void __launch_bounds__(256)
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = g / gpr, j0 = (g - i * gpr) * 8;
     const int e = ea[i];
-    uint32_t pk[OZ_MAX_SLICES][4];
-#pragma unroll
-    for (int t = 0; t < OZ_MAX_SLICES; ++t) pk[t][0] = pk[t][1] = pk[t][2] = pk[t][3] = 0;
     double x[8];
     const double* row = A + i * lda + j0;
     if (VEC && j0 + 8 <= k) {  // four 16-byte loads
@@ -594,18 +591,22 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int q = 0; q < 8; ++q) x[q] = j0 + q < k ? row[q] : 0.0;
     }
+    // The eight offset values, then one slice at a time (one 16-byte store
+    // each), so only the current slice's packed words are live.
+    unsigned __int128 Z[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const unsigned __int128 Z = (unsigned __int128)fixed126(x[q], e) + C;
-#pragma unroll
-      for (int t = 0; t < OZ_MAX_SLICES; ++t)
-        if (t < S) pk[t][q >> 1] |= bf16_of_int(digit_at<b>(Z, t)) << (16 * (q & 1));
-    }
+    for (int q = 0; q < 8; ++q) Z[q] = (unsigned __int128)fixed126(x[q], e) + C;
     uint16_t* o = out + i * kpad + j0;
 #pragma unroll
-    for (int t = 0; t < OZ_MAX_SLICES; ++t)
-      if (t < S)
-        *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+    for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+      if (t < S) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+          pk[h] = bf16_of_int(digit_at<b>(Z[2 * h], t)) | (bf16_of_int(digit_at<b>(Z[2 * h + 1], t)) << 16);
+        *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
   }
 }
 
