@@ -24,9 +24,10 @@
 //                    views).
 //
 // Flat reductions (kernels::reduce, src/kernels/reduce.rs:204-444) keep the
-// reference's 8192-element chunking: each chunk is summed by a lane-striped
-// tree, chunk partials go to workspace, and a single CTA folds them in chunk
-// order.
+// reference's 8192-element chunking: one warp sums a chunk with a
+// lane-striped tree (256 lanes, eight per thread, 16-byte loads), chunk
+// partials go to workspace, and a single CTA folds them (in chunk order up to
+// 1024 chunks, else as 1024 interleaved runs folded in order).
 #include <cfloat>
 #include <type_traits>
 #include <climits>

@@ -11,12 +11,13 @@
 // left-to-right fold, so results are bit-identical; lanes run in parallel
 // through the same TMA pipelines as the axis reductions. A running fold
 // (accumulate) rewrites each staged tile in shared memory with its prefix
-// values and stores it back with a TMA store: HBM traffic is one read and one
-// write of the array.
+// values and stores it back (a TMA store; per-row bulk copies for rows of
+// 4-byte types): HBM traffic is one read and one write of the array.
 //
 // Over the flattened array (axis = None) the order-free cases use a
-// reduce-then-scan over 8192-element chunks whose combine always keeps the
-// earlier operand on the left. maximum/minimum are associative under the
+// reduce-then-scan over contiguous segments (8192-element chunks for
+// unaligned arrays) whose combine always keeps the earlier operand on the
+// left. maximum/minimum are associative under the
 // reference's apply (NaN absorbs, ties take the right operand), so the
 // parallel scan is exact; integer add/multiply wrap and are exact in any
 // order; float add/multiply reassociate (tolerance-based, as the flat
