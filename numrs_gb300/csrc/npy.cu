@@ -28,9 +28,13 @@
 
 #include "nrs_internal.cuh"
 
+// Pinned staging ring of a handle, allocated on its first NPY transfer.
+// 64 MB slots: each slot's file I/O starts up to 8 threads, so larger slots
+// spend less of the transfer starting them (32 MB slots loaded 39-45 GB/s,
+// 64 MB slots 56 GB/s, a 1 GiB array through the page cache).
 struct nrs_host_stage {
   static constexpr int kSlots = 4;
-  static constexpr size_t kSlotBytes = size_t(32) << 20;
+  static constexpr size_t kSlotBytes = size_t(64) << 20;
   uint8_t* buf = nullptr;  // kSlots * kSlotBytes, pinned
   cudaEvent_t ev[kSlots] = {};
   bool pending[kSlots] = {};
