@@ -470,13 +470,23 @@ __global__ void __launch_bounds__(64)
     }
     // Unrolled over the tile with constant indices (v stays in registers);
     // positions past the end of the axis are skipped.
+    // The lane's first element starts it (comparing it with itself then
+    // changes nothing, NaN included), so full tiles need no per-element
+    // checks beyond the compare.
+    if (it == 0) best = v[0];
     int bet = -1;  // position of this tile's improvement, if any
+    if (cnt == TB) {
 #pragma unroll
-    for (int e = 0; e < TB; ++e) {
-      if (e < cnt) {
-        if (it == 0 && e == 0) {
-          best = v[0];
-        } else if (MAX ? (v[e] > best) : (v[e] < best)) {
+      for (int e = 0; e < TB; ++e) {
+        if (MAX ? (v[e] > best) : (v[e] < best)) {
+          best = v[e];
+          bet = e;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < TB; ++e) {
+        if (e < cnt && (MAX ? (v[e] > best) : (v[e] < best))) {
           best = v[e];
           bet = e;
         }
