@@ -82,6 +82,15 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+def _bf16_peak():
+    """Dense BF16 burst rate (TFLOP/s) of MEASURED_PEAKS.json, else the
+    fallback figure."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["bf16_tflops"])
+    return 1900.0
+
+
 class Clocks:
     """nvidia-smi sampler over the timed region."""
 
@@ -192,31 +201,39 @@ def cpu_sample(steps: int | None, min_seconds: float, x32_np, x64_np):
             break
         if steps is None and time.perf_counter() - t_start >= min_seconds:
             break
-    return nbytes, times, ora.num_threads(), f"{rows}x{x32_np.shape[1]} row slab of both arrays, all 21 ops"
+    shape = f"{rows}x{x32_np.shape[1]}"
+    what = "the full arrays" if rows == R else f"a {shape} row slab of both arrays"
+    return nbytes, times, ora.num_threads(), f"{what}, all 21 ops, numrs2 kernels restated in C (OpenMP)"
+
+
+def reference_inputs():
+    """The step's two arrays on the host, from the same SplitMix64 streams as
+    the device generator (seed 3: f32 N(0,1); seed 4: i64 U[-2^20, 2^20))."""
+    from oracle import Oracle
+    ora = Oracle()
+    x32 = ora.gen_normal_f32(F32_SEED, R * C_).reshape(R, C_)
+    x64 = ora.gen_i64(I64_SEED, R * C_).reshape(R, C_)
+    return x32, x64
 
 
 def run_reference(args):
-    """`--impl reference`: the CPU restatement of numrs2's kernels, all host threads."""
-    import numpy as np
-    from numrs_gb300 import rng
+    """`--impl reference`: the CPU restatement of numrs2's kernels (the
+    reference is Rust and cannot be built here) on the full step, all host
+    threads, the same config as the GPU arm."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    rows = args.cpu_rows
-    n = rows * C_
-    x64 = rng.int_range(I64_SEED, n).reshape(rows, C_)
-    x32 = np.random.default_rng(F32_SEED).standard_normal(n).astype(np.float32).reshape(rows, C_)
+    x32, x64 = reference_inputs()
     nbytes, times, cores, sample = cpu_sample(args.warmup + args.steps, 0, x32, x64)
     t = sum(times[args.warmup:])
     val = nbytes * args.steps / t / 1e9
     line = {"impl": "reference", "metric": "reduce GB/s", "value": round(val, 2), "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": dict(CONFIG, sample=f"each step: the same 21 operations on a {rows}x16384 "
-                                          "row slab of both arrays (CPU)"),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (SplitMix64, seeds 3/4)",
+            "config": dict(CONFIG, bytes_per_step=nbytes, parallelism=f"replicas x{args.gpus}"),
             "cpu_baseline": {"value": round(val, 2), "unit": "GB/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample + f"; each of the {args.steps} timed steps is the whole step"},
             "e2e": {"value": round(val, 2), "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -235,49 +252,135 @@ def _time_ms(fn, reps, stream):
     return e0.elapsed_time(e1) / reps
 
 
-def gemm_section(K, L, quick: bool):
-    """Plain f64 GEMM 512^3 (DMMA) and the 8192^3 split-precision GEMM beside
-    the native FP64 DMMA GEMM, errors measured on the GPU against the FP64
-    result as max |C - C_fp64| / (|A||B|)_ij."""
+def _flush_l2(buf):
+    """Overwrite a buffer larger than the 129 MB L2 between timed launches."""
+    buf.add_(1)
+
+
+def _event_median_ms(fn, reps, stream, flush=None):
+    """Median of individually event-timed calls (L2 flushed before each)."""
     import torch
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        if flush is not None:
+            flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def _gemm_peaks(K, L):
+    """FP64 DMMA and FP32 FMA pipe rates measured on this GPU now."""
+    return {"fp64_dmma_tflops": round(K.probe_peak(L.PEAK_FP64_DMMA), 4),
+            "fp32_fma_tflops": round(K.probe_peak(L.PEAK_FP32_FMA), 3),
+            "kind": "measured (nrs_probe_peak: register-resident mma.sync f64 / fp32 FMA chains on every SM)"}
+
+
+def _cpu_gemm_tflops(n: int, seconds: float):
+    """The oracle's restated gemm_2d (f64, all host threads) at n^3."""
+    from oracle import Oracle
+    ora = Oracle()
+    A = ora.gen_uniform_pm1(1, n * n).reshape(n, n)
+    B = ora.gen_uniform_pm1(2, n * n).reshape(n, n)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while not times or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        ora.gemm(A, B)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": round(2.0 * n ** 3 / t / 1e12, 5), "unit": "TFLOP/s", "cores": ora.num_threads(),
+            "kind": "port", "sample": f"f64 {n}^3 gemm_2d restatement (i-k-j, KC=256, row split), "
+                                     f"median of {len(times)} runs"}
+
+
+def gemm_section(K, L, quick: bool, cpu: bool = True):
+    """C1: plain f64 GEMM 512^3 (DMMA), against the FP64 pipe rate and the
+    CPU restatement. C3: the 8192^3 split-precision GEMM with the automatic
+    slice count beside the native FP64 DMMA GEMM for phi in {0, 1, 4};
+    errors of both against 4096 double-double entries (i, j uniform) as
+    max |C - C_dd| / (|A||B|)_ij."""
+    import numpy as np
+    import torch
+    from oracle import Oracle
+    ora = Oracle()
     stream = torch.cuda.current_stream()
-    out = {}
-    A = torch.empty((512, 512), dtype=torch.float64, device="cuda")
+    out = {"peaks": _gemm_peaks(K, L)}
+    fp64_peak = out["peaks"]["fp64_dmma_tflops"]
+    flush_buf = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    n1 = 512
+    A = torch.empty((n1, n1), dtype=torch.float64, device="cuda")
     B = torch.empty_like(A)
     K.fill_random(A, L.RNG_UNIFORM, 1, -1.0, 1.0)
     K.fill_random(B, L.RNG_UNIFORM, 2, -1.0, 1.0)
     C = torch.empty_like(A)
-    ms = _time_ms(lambda: K.gemm_2d(512, 512, 512, A, B, C, variant=L.GEMM_DMMA), 20, stream)
-    out["f64_512_dmma"] = {"ms": round(ms, 4), "tflops": round(2 * 512 ** 3 / ms / 1e9, 3)}
+    ms = _event_median_ms(lambda: K.gemm_2d(n1, n1, n1, A, B, C, variant=L.GEMM_DMMA), 20, stream,
+                          flush=lambda: _flush_l2(flush_buf))
+    tf = 2 * n1 ** 3 / ms / 1e9
+    Cdd, ab = ora.gemm_dd(A.cpu().numpy(), B.cpu().numpy())
+    c1 = {"workload": "f64 C=A*B 512^3, U(-1,1) SplitMix64 seeds 1/2, row-major", "ms": round(ms, 4),
+          "tflops": round(tf, 4), "l2": "flushed before each timed call",
+          "max_err_vs_dd": float(np.max(np.abs(C.cpu().numpy() - Cdd) / ab)),
+          "roofline": {"bound": "fp64 dmma", "kernel": "dmma_gemm", "achieved": round(tf, 4),
+                       "peak": fp64_peak, "unit": "TFLOP/s", "frac": round(tf / fp64_peak, 4)}}
+    if cpu:
+        c1["cpu_baseline"] = _cpu_gemm_tflops(n1, 3.0)
+    out["c1_f64_512_dmma"] = c1
+    del A, B, C
     n = 2048 if quick else 8192
     A = torch.empty((n, n), dtype=torch.float64, device="cuda")
     B = torch.empty_like(A)
     Cd = torch.empty_like(A)
     Co = torch.empty_like(A)
-    Aa = torch.empty_like(A)
-    Ba = torch.empty_like(A)
-    AB = torch.empty_like(A)
     flops = 2.0 * n ** 3
+    r = np.random.default_rng(11)
+    rows, cols = r.integers(0, n, 4096), r.integers(0, n, 4096)
     res = {}
-    # the library's default slice count (equal error with FP64 for phi = 0)
-    z = torch.zeros((8, 8), dtype=torch.float64, device="cuda")
-    s0 = K.gemm_ozaki(z, z)[1]["slices"]
+    bf16_peak = _bf16_peak()
     for phi in (0.0, 1.0, 4.0):
         K.fill_random(A, L.RNG_OZAKI, 5, phi, 0.0)
         K.fill_random(B, L.RNG_OZAKI, 6, phi, 0.0)
-        ms_d = _time_ms(lambda: K.gemm_2d(n, n, n, A, B, Cd, variant=L.GEMM_DMMA), 1, stream)
-        torch.abs(A, out=Aa)
-        torch.abs(B, out=Ba)
-        K.gemm_2d(n, n, n, Aa, Ba, AB, variant=L.GEMM_DMMA)
-        entry = {"dmma_ms": round(ms_d, 2), "dmma_tflops": round(flops / ms_d / 1e9, 3), "ozaki": []}
-        for s in ((s0 - 1, s0, s0 + 2) if phi == 0.0 else (s0, s0 + 3, s0 + 5, min(s0 + 7, 16))):
-            ms_o = _time_ms(lambda: K.gemm_ozaki(A, B, slices=s, out=Co), 2, stream)
-            err = float(((Co - Cd).abs() / AB.clamp_min(1e-300)).max())
-            entry["ozaki"].append({"slices": s, "ms": round(ms_o, 2), "tflops": round(flops / ms_o / 1e9, 2),
-                                   "max_err_vs_fp64": err})
+        ms_d = _event_median_ms(lambda: K.gemm_2d(n, n, n, A, B, Cd, variant=L.GEMM_DMMA), 1, stream)
+        # automatic slice count: spread estimate (one host read-back) + slices
+        # + tensor-core products, timed as the whole call
+        ms_o = _event_median_ms(lambda: K.gemm_ozaki(A, B, out=Co), 3, stream)
+        info = K.gemm_ozaki(A, B, out=Co)[1]
+        ref, ab = ora.gemm_dd_sampled(A.cpu().numpy(), B.cpu().numpy(), rows, cols)
+        e_d = float(np.max(np.abs(Cd.cpu().numpy()[rows, cols] - ref) / ab))
+        e_o = float(np.max(np.abs(Co.cpu().numpy()[rows, cols] - ref) / ab))
+        entry = {"dmma_ms": round(ms_d, 2), "dmma_tflops": round(flops / ms_d / 1e9, 4),
+                 "dmma_frac_of_fp64_peak": round(flops / ms_d / 1e9 / fp64_peak, 4),
+                 "dmma_max_err_vs_dd": e_d,
+                 "ozaki_auto": {"ms": round(ms_o, 2), "tflops_f64_equiv": round(flops / ms_o / 1e9, 2),
+                                "slices": info["slices"], "slice_bits": info["slice_bits"],
+                                "products": info["products"], "spread": info["spread"],
+                                "est_rel_error": info["est_rel_error"], "max_err_vs_dd": e_o,
+                                "speedup_vs_dmma": round(ms_d / ms_o, 2),
+                                "error_within_dmma_or_1e-14": e_o <= max(e_d, 1e-14)}}
+        if info["slices"] > 0:
+            # the same slices without the estimate: the tensor-core kernel's
+            # BF16 rate (slice-pair flops; slicing's ~3% of the time included)
+            S = info["slices"]
+            ms_x = _event_median_ms(lambda: K.gemm_ozaki(A, B, slices=S, out=Co), 3, stream)
+            bf = 2.0 * n ** 3 * S * (S + 1) / 2
+            entry["ozaki_auto"]["explicit_count_ms"] = round(ms_x, 2)
+            entry["ozaki_auto"]["estimate_ms"] = round(ms_o - ms_x, 2)
+            entry["ozaki_auto"]["roofline"] = {
+                "bound": "tensor (bf16)", "kernel": "ozaki_tc_kernel + slicing",
+                "achieved": round(bf / ms_x / 1e9, 1), "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": round(bf / ms_x / 1e9 / bf16_peak, 4)}
         res[f"phi={phi:g}"] = entry
-    out[f"f64_{n}_split_vs_dmma"] = res
-    del A, B, Cd, Co, Aa, Ba, AB
+    out[f"c3_f64_{n}_split_vs_dmma"] = res
+    if cpu:
+        out[f"c3_cpu_baseline"] = dict(_cpu_gemm_tflops(2048, 2.0),
+                                       note="C3's 8192^3 is ~1 min on the host; the 2048^3 rate stands for it")
+    del A, B, Cd, Co, flush_buf
     torch.cuda.empty_cache()
     return out
 
@@ -476,7 +579,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=1024)
+    ap.add_argument("--cpu-rows", type=int, default=R, help="rows of the CPU baseline's sample (default: all)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -717,10 +820,12 @@ def main():
 
     # ---- CPU baseline (rank 0, N = 1 only) ------------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:
+        # the device arrays themselves, copied to the host: the same inputs
         rows = args.cpu_rows
         x32n = x32[:rows].cpu().numpy()
         x64n = x64[:rows].cpu().numpy()
         nbytes, times, cores, sample = cpu_sample(None, args.cpu_seconds, x32n, x64n)
+        del x32n, x64n
         t = sum(times)
         out["cpu_baseline"] = {"value": round(nbytes * len(times) / t / 1e9, 2), "unit": "GB/s",
                                "cores": cores, "kind": "port", "sample": sample,
@@ -729,7 +834,7 @@ def main():
         del x32, x64, y
         ops = None
         torch.cuda.empty_cache()
-        out["gemm"] = gemm_section(K, L, quick=args.quick_gemm)
+        out["gemm"] = gemm_section(K, L, quick=args.quick_gemm, cpu=not args.no_cpu)
     if rank == 0 and not args.no_elementwise:
         out["elementwise"] = elementwise_section(K, L)
     if rank == 0 and not args.no_extra:

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define NRS_ABI_VERSION 1
+#define NRS_ABI_VERSION 2
 
 typedef struct nrs_handle nrs_handle;
 
@@ -73,6 +73,13 @@ int nrs_set_stream(nrs_handle* h, void* cuda_stream);
 /* Enqueue on the handle's own non-blocking stream (the state after create). */
 int nrs_use_own_stream(nrs_handle* h);
 void* nrs_get_stream(nrs_handle* h);
+/* Sizes the handle's grids for at most `sms` SMs (0 = all of the device's),
+ * for sharing the GPU with concurrent work. No reference counterpart. Results
+ * do not depend on it: every plan that decides a rounding order (a GEMM's k
+ * split, a flattened scan's segments, chunk groupings) is fixed by the
+ * problem's sizes alone, as the reference's results are independent of its
+ * thread count (src/kernels/gemm.rs:364-381). */
+int nrs_set_sm_budget(nrs_handle* h, int sms);
 /* Waits for the stream, then reports any device-side error flag. */
 int nrs_synchronize(nrs_handle* h);
 /* Message of the last failing call on this handle ("" if none). */
@@ -153,8 +160,11 @@ int nrs_reduce(nrs_handle* h, int dtype, int op, int ndim, const int64_t* shape,
  *   - Limit: n <= 67,108,864 (8192 chunks of 8192); larger n returns
  *     NRS_ERR_TOO_LARGE before anything is launched.
  *   - The first call on a device looks the array's address up (and the SM
- *     count) with that device current and caches them; make that first call
+ *     count) with that device current and caches them with the current
+ *     context; a call in another context of the device (for instance after
+ *     cudaDeviceReset) looks them up again. Make the first call in a context
  *     before any stream capture.
+ *   - `cuda_stream` must belong to the current device.
  *   - All calls share the one array and it keeps the last call's contents;
  *     every call rewrites each partial it reads, so nothing has to start at
  *     zero. Calls whose work overlaps on the GPU (different streams, no
@@ -336,26 +346,55 @@ int nrs_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, const vo
              int64_t lda, const void* B, int64_t ldb, void* C, int64_t ldc, unsigned flags,
              int variant);
 
+/* Measures a compute pipe's rate on the handle's device (TFLOP/s, best of
+ * three timed launches after a warm-up, CUDA events on the handle's stream;
+ * returns after synchronising). No reference counterpart: the denominators
+ * of the GEMM rooflines. NRS_PEAK_FP64_DMMA: register-resident chains of
+ * mma.sync m8n8k4 f64 (512 flops each) on every SM; NRS_PEAK_FP32_FMA:
+ * chains of fp32 FMA (2 flops each). */
+typedef enum nrs_peak_kind { NRS_PEAK_FP64_DMMA = 0, NRS_PEAK_FP32_FMA = 1 } nrs_peak_kind;
+int nrs_probe_peak(nrs_handle* h, int kind, double* tflops);
+
 /* ---------------------------------------------------------------------- */
 /* f64-accurate split GEMM (Ozaki scheme on BF16 tcgen05 tensor cores)      */
 /* ---------------------------------------------------------------------- */
 typedef struct nrs_ozaki_info {
-  int32_t slices;        /* slices per operand actually used                 */
-  int32_t products;      /* slice-pair GEMMs executed                        */
+  int32_t slices;        /* slices per operand used; 0 = the call ran the native
+                            FP64 (DMMA) GEMM instead (see below)              */
+  int32_t products;      /* slice-pair GEMM work units executed              */
   int32_t slice_bits;    /* bits carried by each slice after the first       */
   int32_t k_chunk;       /* K block inside which fp32 accumulation is exact  */
-  double est_rel_error;  /* a-priori bound on |C - AB| / (rowmax|A| colmax|B| k) */
+  double est_rel_error;  /* slices = 0 (auto): estimated max_ij |C - AB|_ij /
+                            (|A||B|)_ij; explicit count: a-priori bound on
+                            |C - AB| / (rowmax|A| colmax|B| k)               */
+  double spread;         /* auto: max_ij R_ij measured (below); else 0       */
 } nrs_ozaki_info;
 
-/* C := A*B in f64 accuracy from BF16 slice products on tcgen05 tensor cores
- * with per-row (A) / per-column (B) power-of-two scaling and exact fp32
- * accumulation inside K blocks, int32 cross-block accumulation and f64
- * cross-slice accumulation. `slices` = 0 picks the count from the operands'
- * exponent spread. No reference counterpart: replaces the f64 tier of
- * gemm_2d (src/kernels/gemm.rs:290) for large problems. Row-major, no
- * flags. `info` may be NULL. */
+/* C := A*B (or C += A*B with NRS_GEMM_ACCUMULATE) in f64 accuracy from BF16
+ * slice products on tcgen05 tensor cores with per-row (A) / per-column (B)
+ * power-of-two scaling, exact fp32 accumulation inside K blocks, exact int32
+ * cross-block and int128 cross-slice accumulation, one conversion to f64.
+ * No reference counterpart: replaces the f64 tier of gemm_2d
+ * (src/kernels/gemm.rs:290) for large problems. Operands as in nrs_gemm
+ * (row-major, NRS_GEMM_TRANS_A / _TRANS_B for transposed views); operands
+ * must be finite unless slices = 0.
+ *
+ * slices = 0 (automatic) measures how far apart the magnitudes that meet in
+ * each dot product are: with A' and B' the operands scaled by their row and
+ * column exponents, R_ij = sum_k (|a'_ik| + |b'_kj|) / (|A'||B'|)_ij (a BF16
+ * tensor-core product of |A'| and |B'| and the row / column sums; if some
+ * (|A'||B'|)_ij is 0, a second pass counts only the k where the other factor
+ * is nonzero). Each operand is then carried to 53 + log2(max R) bits, which
+ * keeps max_ij |C - AB|_ij / (|A||B|)_ij at about 2^-53. If no count within
+ * the limits (16 slices, 126 bits, exact int32 sums for this K) reaches
+ * that, or an operand holds Inf or NaN, the call runs the native FP64 DMMA
+ * GEMM and reports slices = 0. The automatic mode reads the measured spread
+ * back to the host: one synchronisation of the handle's stream, so it
+ * cannot be captured in a CUDA graph; pass the count a previous call
+ * reported to capture.
+ * slices = 1..16 uses that count as given. `info` may be NULL. */
 int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, const double* A, int64_t lda,
-                   const double* B, int64_t ldb, double* C, int64_t ldc, int slices,
+                   const double* B, int64_t ldb, double* C, int64_t ldc, unsigned flags, int slices,
                    nrs_ozaki_info* info);
 
 /* ---------------------------------------------------------------------- */

@@ -24,6 +24,7 @@ OP_INPUT, OP_SCALAR, OP_ADD, OP_SUB, OP_MUL, OP_DIV = 0, 1, 2, 3, 4, 5
 OP_NEG, OP_ABS, OP_SQRT, OP_EXP, OP_LN, OP_MAX, OP_MIN = 6, 7, 8, 9, 10, 11, 12
 GEMM_ACCUMULATE, GEMM_TRANS_A, GEMM_TRANS_B = 1, 2, 4
 GEMM_AUTO, GEMM_DMMA, GEMM_SIMT, GEMM_GENERIC, GEMM_SIMT_SMALL = 0, 1, 2, 3, 4
+PEAK_FP64_DMMA, PEAK_FP32_FMA = 0, 1
 RNG_UNIFORM, RNG_NORMAL, RNG_INT, RNG_OZAKI = 0, 1, 2, 3
 TILE_VARIANTS = 6
 
@@ -41,7 +42,7 @@ class UfuncOp(C.Structure):
 
 class OzakiInfo(C.Structure):
     _fields_ = [("slices", C.c_int32), ("products", C.c_int32), ("slice_bits", C.c_int32),
-                ("k_chunk", C.c_int32), ("est_rel_error", C.c_double)]
+                ("k_chunk", C.c_int32), ("est_rel_error", C.c_double), ("spread", C.c_double)]
 
 
 class GemmDesc(C.Structure):
@@ -61,6 +62,7 @@ _lib = None
 # (name, restype, argtypes) for every exported function.
 _vp, _i, _i64, _u64, _d, _f, _sz, _u = (C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double,
                                         C.c_float, C.c_size_t, C.c_uint)
+_u32 = C.c_uint32
 _P64 = C.POINTER(C.c_int64)
 SIGNATURES = {
     "nrs_abi_version": (_i, []),
@@ -90,7 +92,9 @@ SIGNATURES = {
     "nrs_npy_write": (_i, [_vp, C.c_char_p, _i, _i, _P64, _vp]),
     "nrs_accumulate": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _P64]),
     "nrs_gemm": (_i, [_vp, _i, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u, _i]),
-    "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i,
+    "nrs_set_sm_budget": (_i, [_vp, _i]),
+    "nrs_probe_peak": (_i, [_vp, _i, C.POINTER(C.c_double)]),
+    "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u32, _i,
                             C.POINTER(OzakiInfo)]),
     "nrs_plan_create": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
                              C.POINTER(_vp)]),

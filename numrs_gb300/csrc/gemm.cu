@@ -172,7 +172,8 @@ int nrs_plain_gemm_launch(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_
     else variant = NRS_GEMM_GENERIC;
   }
   if (variant == NRS_GEMM_DMMA && dtype == NRS_F64) {
-    const DmmaPlan pl = plan_dmma(m, n, k, h->num_sms);
+    // The k split decides the rounding: plan for a fixed SM count.
+    const DmmaPlan pl = plan_dmma(m, n, k, NRS_PLAN_SMS);
     double* P = nullptr;
     if (pl.splits > 1) {
       int st;
@@ -270,4 +271,87 @@ extern "C" int nrs_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t 
   const int64_t rsb = tb ? 1 : ldb, csb = tb ? ldb : 1;
   return nrs_plain_gemm_launch(h, dtype, m, k, n, A, rsa, csa, B, rsb, csb, C, ldc, accumulate,
                                variant);
+}
+
+// ---------------------------------------------------------------------------
+// Pipe-rate probes: the denominators for the GEMM rooflines on this device.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Every warp issues `iters` rounds of 8 independent m8n8k4 DMMA chains
+// (8 x 512 flops per round) from registers; the operands change with the
+// thread so nothing folds at compile time, and the result is stored only if
+// it is NaN (never) so the chains stay live.
+__global__ void __launch_bounds__(256) dmma_rate(int64_t iters, double seed, double* sink) {
+  double a = seed + threadIdx.x * 1e-3, b = 1.0 - a * 1e-3;
+  double d[8][2];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) d[c][0] = d[c][1] = 0.0;
+  for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dmma_m8n8k4(d[c][0], d[c][1], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += d[c][0] + d[c][1];
+  if (s != s) sink[threadIdx.x] = s;
+}
+
+// FP32 FMA rate: 8 independent FMA chains per thread.
+__global__ void __launch_bounds__(256) ffma_rate(int64_t iters, float seed, float* sink) {
+  float x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = seed + (float)(threadIdx.x + c) * 1e-3f;
+  const float a = 0.999f, b = 1e-4f;
+  for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = fmaf(x[c], a, b);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  if (s != s) sink[threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int nrs_probe_peak(nrs_handle* h, int kind, double* tflops) {
+  if (!h || !tflops) return NRS_ERR_INVALID;
+  if (kind != NRS_PEAK_FP64_DMMA && kind != NRS_PEAK_FP32_FMA)
+    return nrs_fail(h, NRS_ERR_INVALID, "unknown probe kind");
+  h->last_error.clear();
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  void* sink = nrs_workspace(h, 4096, &st);
+  if (!sink) return st;
+  // 32 warps per SM; long enough (tens of ms) that launch overhead is noise.
+  const int blocks = h->num_sms * 4;
+  const int64_t iters = kind == NRS_PEAK_FP64_DMMA ? 4096 : (1 << 20);
+  cudaEvent_t e0, e1;
+  if ((st = nrs_cuda_check(h, cudaEventCreate(&e0), "cudaEventCreate"))) return st;
+  if ((st = nrs_cuda_check(h, cudaEventCreate(&e1), "cudaEventCreate"))) {
+    cudaEventDestroy(e0);
+    return st;
+  }
+  float best_ms = 1e30f;
+  for (int rep = 0; rep < 4 && st == NRS_OK; ++rep) {  // first launch is a warm-up
+    cudaEventRecord(e0, h->stream);
+    if (kind == NRS_PEAK_FP64_DMMA)
+      dmma_rate<<<blocks, 256, 0, h->stream>>>(iters, 0.5, (double*)sink);
+    else
+      ffma_rate<<<blocks, 256, 0, h->stream>>>(iters, 0.5f, (float*)sink);
+    cudaEventRecord(e1, h->stream);
+    st = nrs_cuda_check(h, cudaEventSynchronize(e1), "probe");
+    float ms = 0.0f;
+    if (st == NRS_OK) st = nrs_cuda_check(h, cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    if (st == NRS_OK && rep > 0 && ms < best_ms) best_ms = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  const double warps = (double)blocks * 8.0;
+  const double flops = kind == NRS_PEAK_FP64_DMMA ? warps * (double)iters * 8.0 * 512.0
+                                                  : warps * 32.0 * (double)iters * 8.0 * 2.0;
+  *tflops = flops / (best_ms * 1e-3) / 1e12;
+  return NRS_OK;
 }

@@ -24,9 +24,16 @@ enum : uint32_t {
 struct nrs_tuner_table;
 struct nrs_host_stage;  // pinned staging slots for file I/O (npy.cu)
 
+// SM count that every result-affecting plan is computed for (a GEMM's k
+// split, a flattened scan's segments): GB300's 152. Grids are sized from
+// the handle's num_sms, plans from this constant, so results do not depend
+// on the device or on the handle's SM budget.
+constexpr int NRS_PLAN_SMS = 152;
+
 struct nrs_handle {
   int device = 0;
-  int num_sms = 0;
+  int num_sms = 0;   // SMs grids are sized for (the budget, nrs_set_sm_budget)
+  int hw_sms = 0;    // the device's SM count
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   // Grow-only device workspace for kernels that need scratch memory.

@@ -196,7 +196,14 @@ struct OzParams {
   int final_shift; // 2 - 2b - b(S-1) for b-bit digits
   int digit_bits;  // b
   int kchunk;      // exact FP32 K chunk, 2^(26-2b)
+  int accumulate;  // C += result instead of C = result
   uint32_t* err;
+  // Spread estimate only (EST kernel): row sums of |A'| and column sums of
+  // |B'| (operands scaled by their row / column exponents), and the word
+  // that collects max_ij of the ratio as float bits.
+  const float* ra;
+  const float* cb;
+  uint32_t* est;
 };
 
 // Pair order within a tile: diagonals from the least significant (d = S-1)
@@ -226,6 +233,14 @@ __device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm
   tn = r / gm;
 }
 
+// EST = false: the slice-pair GEMM described in the file header.
+// EST = true : the same pipeline on the spread-estimate operands (one K chunk
+//              covering all of K): pass 1 (slices = 1) runs the one product
+//              D = |A'| |B'|^T; pass 2 (slices = 2) also runs the two cross
+//              products N = |A'| 1_B^T + 1_A |B'|^T of slices 0 and 1 (|x'|
+//              and the nonzero indicator). The epilogue folds
+//              max_ij (numerator_ij / D_ij) into P.est instead of writing C.
+template <bool EST>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                     OzParams P) {
@@ -347,6 +362,86 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       tc_commit(drain);
       mbar_wait_bounded(drain, 0, 1u << 20);
     }
+  } else if (EST) {
+    // ---------------- spread-estimate epilogue (warps 2..9) ----------------
+    // Same TMEM geometry as below. Units of a tile: pass 1: (0,0) = D;
+    // pass 2: (0,1), (1,0) summed in fp32 into columns 256..511 = N, then
+    // (0,0) = D. Per element r = numerator / D (pass 1: numerator =
+    // (ra_i + cb_j) 2^96, the operands' 2^48 scale factors); D = 0 gives
+    // +inf unless the numerator is 0 too (every product then has a zero
+    // factor and the result is exact). The running max is float bits.
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int row_in_tile = q * 32 + lane;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + half * (OZ_BN / 2);
+    const uint32_t acc_t = lane_base;
+    const uint32_t dsum_t = lane_base + OZ_BN;
+    uint32_t ai = 0;
+    float rmax = 0.0f;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+      int tm, tn;
+      tile_coords(tile, P, tm, tn);
+      const int64_t row = (int64_t)tm * OZ_BM + row_in_tile;
+      const bool row_ok = row < P.m;
+      const int64_t col0 = (int64_t)tn * OZ_BN + half * (OZ_BN / 2);
+      const float ra = row_ok ? P.ra[row] : 0.0f;
+      for (int u = 0; u < P.n_pairs; ++u, ++ai) {
+        const PairOf pr = pair_of(u, P.slices, 1);
+        if (!bounded(&accf[0], ai & 1, 4)) { ok = false; break; }
+        tc_fence_after();
+        uint32_t v[OZ_BN / 2];
+#pragma unroll
+        for (int c = 0; c < OZ_BN / 32; ++c) tmem_ld16_nowait(acc_t + c * 16, v + c * 16);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[0]);
+        if (pr.s + pr.t == 1) {
+#pragma unroll
+          for (int c = 0; c < OZ_BN / 32; ++c) {
+            uint32_t w[16];
+            if (pr.s == 1) {
+              tmem_ld16(dsum_t + c * 16, w);
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                w[e] = __float_as_uint(__uint_as_float(w[e]) + __uint_as_float(v[c * 16 + e]));
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) w[e] = v[c * 16 + e];
+            }
+            tmem_st16(dsum_t + c * 16, w);
+          }
+          tmem_wait_st();
+          tc_fence_before();
+          __syncwarp();
+          continue;
+        }
+#pragma unroll 1
+        for (int c = 0; c < OZ_BN / 32; ++c) {
+          uint32_t w[16];
+          if (P.slices == 2) tmem_ld16(dsum_t + c * 16, w);  // warp-uniform
+          if (!row_ok) continue;
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int64_t col = col0 + c * 16 + e;
+            if (col >= P.n) continue;
+            const float D = __uint_as_float(v[c * 16 + e]);
+            const float num = P.slices == 2 ? __uint_as_float(w[e]) : ra + P.cb[col];
+            float r;
+            if (D > 0.0f) {
+              r = num / D;
+              if (P.slices != 2) r *= 0x1p96f;
+            } else {
+              r = num > 0.0f ? __uint_as_float(0x7f800000u) : 0.0f;
+            }
+            rmax = fmaxf(rmax, r);
+          }
+        }
+      }
+    }
+    for (int off = 16; off; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+    if (lane == 0 && ok) atomicMax(P.est, __float_as_uint(rmax));
   } else {
     // ---------------- epilogue (warps 2..9) ----------------
     // Warp w reads TMEM lane quarter w % 4 (one tile row per thread) and
@@ -443,7 +538,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
               const uint64_t top = (uint64_t)(mag >> sh);
               double val = (double)top;
               val = ldexp(val, sh + ecol_base + P.eb[col]);
-              P.C[row * P.ldc + col] = neg ? -val : val;
+              double* cp = P.C + row * P.ldc + col;
+              const double r = neg ? -val : val;
+              *cp = P.accumulate ? *cp + r : r;
             }
           }
         }
@@ -462,8 +559,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 // Scaling exponents and slicing
 // ---------------------------------------------------------------------------
 // frexp-style exponent of max |x| over a row (one warp per row).
+// `flag` (may be null) gets bit 0 set when a row holds an Inf or a NaN.
 __global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda,
-                              int* __restrict__ ea) {
+                              int* __restrict__ ea, uint32_t* __restrict__ flag) {
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (row >= m) return;
@@ -480,6 +578,7 @@ __global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k
     int e = (int)(mx >> 52) - 1022;  // |max| < 2^e
     if ((mx >> 52) == 0) e = -1021;  // zero or subnormal
     ea[row] = e;
+    if (flag && (mx >> 52) == 0x7FF) atomicOr(flag, 1u);
   }
 }
 
@@ -504,11 +603,12 @@ __global__ void col_max_bits(const double* __restrict__ B, int64_t k, int64_t n,
 
 // frexp-style exponent from a max-magnitude bit pattern.
 __global__ void exponents_from_bits(const unsigned long long* __restrict__ mx, int64_t n,
-                                    int* __restrict__ e) {
+                                    int* __restrict__ e, uint32_t* __restrict__ flag) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const unsigned long long b = mx[i];
   e[i] = ((b >> 52) == 0) ? -1021 : (int)(b >> 52) - 1022;
+  if (flag && (b >> 52) == 0x7FF) atomicOr(flag, 1u);
 }
 
 // X = round(x * 2^(126 - e)) as a signed 128-bit integer (|x| < 2^e).
@@ -654,6 +754,119 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Spread estimate operands
+// ---------------------------------------------------------------------------
+// For the automatic slice count the operands are also written as two BF16
+// "slices": slice 0 = |x'| 2^48 (x' = x 2^-e, so |x'| < 1; rounded to
+// nearest) and slice 1 = 2^48 where x != 0, else 0. The 2^48 factors keep
+// products of small |x'| above FP32's underflow threshold while every sum
+// over K stays below 2^96 * 2^31 < 2^128. Row sums of |x'| (fp32, fixed
+// order) give the pass-1 numerator.
+__device__ __forceinline__ uint32_t bf16_rn_bits(float f) {
+  // round to nearest even on the bit pattern (f is finite and >= 0)
+  const uint32_t u = __float_as_uint(f);
+  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+constexpr uint32_t kBf16Two48 = 0x5780u;  // 2^48 in BF16
+constexpr float kTwo48 = 281474976710656.0f;
+
+// X (rows x k, row pitch ld, contiguous along k) -> out [2][rows][kpad],
+// sums[row] = sum_k |x'|. One warp per row, 8 consecutive k per lane step.
+template <bool VEC>
+__global__ void __launch_bounds__(256)
+    est_rows(const double* __restrict__ X, int64_t rows, int64_t k, int64_t ld, int64_t kpad,
+             const int* __restrict__ e, uint16_t* __restrict__ out, float* __restrict__ sums) {
+  const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const double sc = ldexp(1.0, -e[row]);
+  const double* xr = X + row * ld;
+  float s = 0.0f;
+  for (int64_t j0 = (int64_t)lane * 8; j0 < kpad; j0 += 256) {
+    double x[8];
+    if (VEC && j0 + 8 <= k) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double2 d2 = reinterpret_cast<const double2*>(xr + j0)[q];
+        x[2 * q] = d2.x;
+        x[2 * q + 1] = d2.y;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) x[q] = j0 + q < k ? xr[j0 + q] : 0.0;
+    }
+    uint32_t pa[4], pi[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const float f0 = (float)(fabs(x[2 * h]) * sc), f1 = (float)(fabs(x[2 * h + 1]) * sc);
+      s += f0;
+      s += f1;
+      pa[h] = bf16_rn_bits(f0 * kTwo48) | (bf16_rn_bits(f1 * kTwo48) << 16);
+      pi[h] = (x[2 * h] != 0.0 ? kBf16Two48 : 0u) | ((x[2 * h + 1] != 0.0 ? kBf16Two48 : 0u) << 16);
+    }
+    uint16_t* o = out + row * kpad + j0;
+    *reinterpret_cast<uint4*>(o) = make_uint4(pa[0], pa[1], pa[2], pa[3]);
+    *reinterpret_cast<uint4*>(o + rows * kpad) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
+  }
+  for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) sums[row] = s;
+}
+
+// X (k x cols row-major) -> out [2][cols][kpad] (transposed through shared
+// memory like slice_cols), part[strip][col] = sum of |x'| over the block's
+// 64 k; est_strip_sums adds the strips in order (deterministic).
+__global__ void __launch_bounds__(256)
+    est_cols(const double* __restrict__ X, int64_t k, int64_t cols, int64_t ld, int64_t kpad,
+             const int* __restrict__ e, uint16_t* __restrict__ out, float* __restrict__ part) {
+  __shared__ uint32_t tile[2][kSliceColN][kSliceColPitch];
+  __shared__ float csum[8][kSliceColN];
+  const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t nn = n0 + tx;
+  const double sc = nn < cols ? ldexp(1.0, -e[nn]) : 0.0;
+  float s = 0.0f;
+#pragma unroll
+  for (int r = 0; r < kSliceColK / 16; ++r) {
+    const int w = ty + 8 * r;
+    const int64_t kk = k0 + 2 * w;
+    const double x0 = kk < k && nn < cols ? X[kk * ld + nn] : 0.0;
+    const double x1 = kk + 1 < k && nn < cols ? X[(kk + 1) * ld + nn] : 0.0;
+    const float f0 = (float)(fabs(x0) * sc), f1 = (float)(fabs(x1) * sc);
+    s += f0;
+    s += f1;
+    tile[0][tx][w] = bf16_rn_bits(f0 * kTwo48) | (bf16_rn_bits(f1 * kTwo48) << 16);
+    tile[1][tx][w] = (x0 != 0.0 ? kBf16Two48 : 0u) | ((x1 != 0.0 ? kBf16Two48 : 0u) << 16);
+  }
+  csum[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && nn < cols) {
+    float t = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t += csum[q][tx];
+    part[(int64_t)blockIdx.y * cols + nn] = t;
+  }
+  const int r = threadIdx.x >> 3, c = threadIdx.x & 7;
+  const int64_t n2 = n0 + r, k2 = k0 + c * 8;
+  if (n2 < cols && k2 < kpad) {
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const uint32_t* src = &tile[t][r][c * 4];
+      *reinterpret_cast<uint4*>(out + (int64_t)t * cols * kpad + n2 * kpad + k2) =
+          make_uint4(src[0], src[1], src[2], src[3]);
+    }
+  }
+}
+
+__global__ void est_strip_sums(const float* __restrict__ part, int64_t strips, int64_t cols,
+                               float* __restrict__ sums) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float t = 0.0f;
+  for (int64_t s = 0; s < strips; ++s) t += part[s * cols + c];
+  sums[c] = t;
+}
+
 bool make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t rows, int S,
                     uint32_t box_rows) {
   auto enc = nrs_get_encode_tiled();
@@ -667,58 +880,206 @@ bool make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t ro
              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-}  // namespace
 
-extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, const double* A,
-                              int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
-                              int slices, nrs_ozaki_info* info) {
-  if (!h) return NRS_ERR_INVALID;
-  h->last_error.clear();
-  if (m < 0 || k < 0 || n < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative GEMM dimension");
-  if (lda < (k > 0 ? k : 1) || ldb < (n > 0 ? n : 1) || ldc < (n > 0 ? n : 1))
-    return nrs_fail(h, NRS_ERR_SHAPE, "leading dimension too small");
-  if (slices < 0 || slices > OZ_MAX_SLICES)
-    return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
-  // Widest digits whose int32 diagonal sums stay exact for this K and S:
-  // a diagonal sums at most kchunks * S chunk sums of magnitude <= 2^24.
-  const int64_t kpad = ((k + 7) / 8) * 8;
-  int b = 0, S = 0, kchunks = 0;
-  for (int cand = 8; cand >= 6 && !b; --cand) {
-    const int s_c = slices == 0 ? (54 + cand - 1) / cand : slices;
-    const int kc = (int)((kpad + kChunkOf(cand) - 1) / kChunkOf(cand));
-    // ... and every digit position (127 - b - b t, t < S) lies inside X's
-    // 126 fraction bits: b * S <= 126.
-    if ((int64_t)(kc > 0 ? kc : 1) * s_c < 128 && cand * s_c <= 126) {
-      b = cand;
-      S = s_c;
-      kchunks = kc;
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+// One operand as the kernels see it: `rows` output rows (m for A, n for B)
+// along K. rows_contig: element (r, kk) at p[r * ld + kk] (A as given, or B
+// passed transposed); otherwise at p[kk * ld + r] (B as given, or A passed
+// transposed), which the column kernels read coalesced and transpose.
+struct OzOperand {
+  const double* p;
+  int64_t ld;
+  int64_t rows;
+  bool rows_contig;
+};
+
+int launch_exponents(nrs_handle* h, const OzOperand& o, int64_t k, int* e,
+                     unsigned long long* colmax, uint32_t* flag) {
+  cudaStream_t s = h->stream;
+  if (o.rows_contig) {
+    row_exponents<<<(unsigned)((o.rows + 7) / 8), 256, 0, s>>>(o.p, o.rows, k, o.ld, e, flag);
+  } else {
+    int st = nrs_cuda_check(h, cudaMemsetAsync(colmax, 0, (size_t)o.rows * 8, s), "cudaMemsetAsync");
+    if (st) return st;
+    col_max_bits<<<dim3((unsigned)((o.rows + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip)), 256,
+                   0, s>>>(o.p, k, o.rows, o.ld, colmax);
+    exponents_from_bits<<<(unsigned)((o.rows + 255) / 256), 256, 0, s>>>(colmax, o.rows, e, flag);
+  }
+  return nrs_after_launch(h, "ozaki exponents");
+}
+
+template <int b>
+int launch_slices_b(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int S,
+                    uint16_t* out) {
+  cudaStream_t s = h->stream;
+  if (o.rows_contig) {
+    const int64_t groups = o.rows * (kpad / 8);
+    const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
+    // 16-byte row loads when every row start is 16-byte aligned.
+    if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
+      slice_rows<b, true><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, S, out);
+    else
+      slice_rows<b, false><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, S, out);
+  } else {
+    const int smem = (int)((size_t)S * kSliceColN * kSliceColPitch * 4);
+    int st = nrs_cuda_check(h, cudaFuncSetAttribute(slice_cols<b>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    smem),
+                            "cudaFuncSetAttribute(slice_cols)");
+    if (st) return st;
+    dim3 g((unsigned)((o.rows + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
+    slice_cols<b><<<g, 256, smem, s>>>(o.p, k, o.rows, o.ld, kpad, e, S, out);
+  }
+  return nrs_after_launch(h, "ozaki slicing");
+}
+
+int launch_slices(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int b, int S,
+                  uint16_t* out) {
+  return b == 8 ? launch_slices_b<8>(h, o, k, kpad, e, S, out)
+                : b == 7 ? launch_slices_b<7>(h, o, k, kpad, e, S, out)
+                         : launch_slices_b<6>(h, o, k, kpad, e, S, out);
+}
+
+int launch_est_operand(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e,
+                       uint16_t* out, float* sums, float* part) {
+  cudaStream_t s = h->stream;
+  if (o.rows_contig) {
+    const unsigned grid = (unsigned)((o.rows + 7) / 8);
+    if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
+      est_rows<true><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, out, sums);
+    else
+      est_rows<false><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, out, sums);
+  } else {
+    const int64_t strips = (kpad + kSliceColK - 1) / kSliceColK;
+    dim3 g((unsigned)((o.rows + kSliceColN - 1) / kSliceColN), (unsigned)strips);
+    est_cols<<<g, 256, 0, s>>>(o.p, k, o.rows, o.ld, kpad, e, out, part);
+    est_strip_sums<<<(unsigned)((o.rows + 255) / 256), 256, 0, s>>>(part, strips, o.rows, sums);
+  }
+  return nrs_after_launch(h, "ozaki spread operands");
+}
+
+template <bool EST>
+int launch_tc(nrs_handle* h, const void* sa, const void* sb, int S, const OzParams& P) {
+  CUtensorMap mapA, mapB;
+  if (!make_slice_map(&mapA, sa, P.kpad, P.m, S, OZ_BM) || !make_slice_map(&mapB, sb, P.kpad, P.n, S, OZ_BN))
+    return nrs_fail(h, NRS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the slices");
+  // Set on every call: the attribute belongs to the current device's context.
+  int st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel<EST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  OZ_SMEM),
+                          "cudaFuncSetAttribute(ozaki)");
+  if (st) return st;
+  const int n_tiles = P.tiles_m * P.tiles_n;
+  const int ctas = n_tiles < h->num_sms ? n_tiles : h->num_sms;
+  ozaki_tc_kernel<EST><<<ctas, OZ_THREADS, OZ_SMEM, h->stream>>>(mapA, mapB, P);
+  return nrs_after_launch(h, EST ? "ozaki_tc_kernel<est>" : "ozaki_tc_kernel");
+}
+
+OzParams base_params(nrs_handle* h, int64_t m, int64_t n, int64_t k, int64_t kpad) {
+  OzParams P{};
+  P.m = m;
+  P.n = n;
+  P.k = k;
+  P.kpad = kpad;
+  P.tiles_m = (int)((m + OZ_BM - 1) / OZ_BM);
+  P.tiles_n = (int)((n + OZ_BN - 1) / OZ_BN);
+  P.group_m = 12;
+  P.err = h->dev_error;
+  return P;
+}
+
+// Digit width and count for `bits` bits of each operand's fixed-point value:
+// the widest b (8, 7, 6) with S = ceil(bits / b) <= 16, every digit inside
+// the 126 fraction bits (b S <= 126) and int32-exact diagonal sums
+// (ceil(kpad / 2^(26-2b)) S < 128). false if no width qualifies.
+bool choose_digits(int64_t kpad, double bits, int* b, int* S, int* kchunks) {
+  for (int cand = 8; cand >= 6; --cand) {
+    int s_c = (int)std::ceil(bits / cand - 1e-9);
+    if (s_c < 1) s_c = 1;
+    const int64_t kc = (kpad + kChunkOf(cand) - 1) / kChunkOf(cand);
+    if (s_c <= OZ_MAX_SLICES && cand * s_c <= 126 && (kc > 0 ? kc : 1) * s_c < 128) {
+      *b = cand;
+      *S = s_c;
+      *kchunks = (int)kc;
+      return true;
     }
   }
-  if (!b)
-    return nrs_fail(h, NRS_ERR_TOO_LARGE,
-                    "k too large for this slice count (ceil(k / 16384) * S must be < 128)");
-  const int n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
-  if (info) {
-    info->slices = S;
-    info->products = n_pairs;
-    info->slice_bits = b;
-    info->k_chunk = kChunkOf(b);
-    // each operand is rounded at 2^-(bS) of its row (column) maximum
-    info->est_rel_error = std::ldexp(2.0, -b * S);
-  }
-  if (m == 0 || n == 0) return NRS_OK;
-  if (k == 0) return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
-  if (!A || !B || !C) return nrs_fail(h, NRS_ERR_INVALID, "null operand");
-  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
-  if (st) return st;
-  if (m > (1LL << 31) || n > (1LL << 31) || kpad > (1LL << 31))
-    return nrs_fail(h, NRS_ERR_TOO_LARGE, "dimension beyond 2^31");
+  return false;
+}
 
-  // Workspace: exponents | A slices | B slices | int128 accumulators.
+// Bits of the fixed-point operands that keep the slicing error at FP64's
+// unit roundoff relative to (|A||B|)_ij: each operand element is rounded at
+// 2^-(bS) (scaled units), so |C - AB|_ij <~ 2^-(bS) (sum_k |a'_ik| + |b'_kj|)
+// = 2^-(bS) R_ij (|A'||B'|)_ij, and bS >= 53 + log2 max_ij R_ij.
+constexpr double kTargetBits = 53.0;
+
+struct SpreadResult {
+  float rmax;
+  uint32_t flags;  // bit 0: an operand holds Inf or NaN
+};
+
+// Runs the spread estimate: exponents, estimate operands and one (pass 1) or
+// three (pass 2) BF16 products, then reads max_ij R_ij back (one stream
+// synchronisation).
+int spread_estimate(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m, int64_t n, int64_t k,
+                    int64_t kpad, int pass, SpreadResult* res) {
   auto al = [](size_t v) { return (v + 1023) & ~size_t(1023); };
+  const int64_t strips = (kpad + kSliceColK - 1) / kSliceColK;
+  const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4), ra_b = al((size_t)m * 4),
+               cb_b = al((size_t)n * 4), cm_b = al((size_t)std::max(m, n) * 8),
+               part_b = al((size_t)strips * std::max(m, n) * 4), sa_b = al((size_t)2 * m * kpad * 2),
+               sb_b = al((size_t)2 * n * kpad * 2), word_b = 1024;
+  int st;
+  uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + ra_b + cb_b + cm_b + part_b + sa_b + sb_b + word_b, &st);
+  if (!ws) return st;
+  int* ea = (int*)ws;
+  int* eb = (int*)(ws + ea_b);
+  float* ra = (float*)(ws + ea_b + eb_b);
+  float* cb = (float*)(ws + ea_b + eb_b + ra_b);
+  unsigned long long* colmax = (unsigned long long*)(ws + ea_b + eb_b + ra_b + cb_b);
+  float* part = (float*)(ws + ea_b + eb_b + ra_b + cb_b + cm_b);
+  uint16_t* sa = (uint16_t*)(ws + ea_b + eb_b + ra_b + cb_b + cm_b + part_b);
+  uint16_t* sb = (uint16_t*)((uint8_t*)sa + sa_b);
+  uint32_t* word = (uint32_t*)((uint8_t*)sb + sb_b);  // [0] max R bits, [1] flags
+  cudaStream_t s = h->stream;
+  if ((st = nrs_cuda_check(h, cudaMemsetAsync(word, 0, 8, s), "cudaMemsetAsync"))) return st;
+  if ((st = launch_exponents(h, a, k, ea, colmax, word + 1))) return st;
+  if ((st = launch_exponents(h, bT, k, eb, colmax, word + 1))) return st;
+  if ((st = launch_est_operand(h, a, k, kpad, ea, sa, ra, part))) return st;
+  if ((st = launch_est_operand(h, bT, k, kpad, eb, sb, cb, part))) return st;
+  OzParams P = base_params(h, m, n, k, kpad);
+  P.slices = pass;
+  P.kchunks = 1;
+  P.n_pairs = pass == 1 ? 1 : 3;
+  P.kchunk = (int)(((kpad + OZ_BK - 1) / OZ_BK) * OZ_BK);
+  P.ra = ra;
+  P.cb = cb;
+  P.est = word;
+  if ((st = launch_tc<true>(h, sa, sb, 2, P))) return st;
+  uint32_t host[2] = {0, 0};
+  if ((st = nrs_cuda_check(h, cudaMemcpyAsync(host, word, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync")))
+    return st;
+  if ((st = nrs_cuda_check(h, cudaStreamSynchronize(s), "cudaStreamSynchronize"))) return st;
+  uint32_t derr = 0;
+  if ((st = nrs_cuda_check(h, cudaMemcpy(&derr, h->dev_error, 4, cudaMemcpyDeviceToHost), "cudaMemcpy")))
+    return st;
+  if (derr) return nrs_fail(h, NRS_ERR_TIMEOUT, "ozaki spread estimate: a device-side bounded wait gave up");
+  float r;
+  std::memcpy(&r, &host[0], 4);
+  res->rmax = r;
+  res->flags = host[1];
+  return NRS_OK;
+}
+
+int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m, int64_t n, int64_t k,
+              int64_t kpad, int b, int S, int kchunks, double* C, int64_t ldc, bool accumulate) {
+  auto al = [](size_t v) { return (v + 1023) & ~size_t(1023); };
+  // Workspace: exponents | A slices | B slices | int128 accumulators (the
+  // column maxima of a column-major operand go through the accumulators).
   const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4);
   const size_t sa_b = al((size_t)S * m * kpad * 2), sb_b = al((size_t)S * n * kpad * 2);
-  const size_t acc_b = al((size_t)m * n * 16);
+  const size_t acc_b = al(std::max((size_t)m * n * 16, (size_t)std::max(m, n) * 8));
+  int st;
   uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + sa_b + sb_b + acc_b, &st);
   if (!ws) return st;
   int* ea = (int*)ws;
@@ -726,50 +1087,15 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   uint16_t* sa = (uint16_t*)(ws + ea_b + eb_b);
   uint16_t* sb = (uint16_t*)(ws + ea_b + eb_b + sa_b);
   __int128* acc = (__int128*)(ws + ea_b + eb_b + sa_b + sb_b);
-  cudaStream_t s = h->stream;
-
-  row_exponents<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(A, m, k, lda, ea);
-  // Column maxima go through the (not yet used) accumulator region.
   unsigned long long* colmax = reinterpret_cast<unsigned long long*>(acc);
-  if ((st = nrs_cuda_check(h, cudaMemsetAsync(colmax, 0, (size_t)n * 8, s), "cudaMemsetAsync")))
-    return st;
-  col_max_bits<<<dim3((unsigned)((n + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip)), 256, 0,
-                 s>>>(B, k, n, ldb, colmax);
-  exponents_from_bits<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(colmax, n, eb);
-  const int64_t groups = m * (kpad / 8);
-  const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
-  // 16-byte row loads when every row start is 16-byte aligned.
-  const bool vec = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && (lda % 2 == 0);
-  auto rows_kern = vec ? (b == 8 ? slice_rows<8, true> : b == 7 ? slice_rows<7, true> : slice_rows<6, true>)
-                       : (b == 8 ? slice_rows<8, false> : b == 7 ? slice_rows<7, false> : slice_rows<6, false>);
-  auto cols_kern = b == 8 ? slice_cols<8> : b == 7 ? slice_cols<7> : slice_cols<6>;
-  rows_kern<<<grid, 256, 0, s>>>(A, m, k, lda, kpad, ea, S, sa);
-  const size_t col_smem = (size_t)S * kSliceColN * kSliceColPitch * 4;
-  static std::once_flag col_attr;
-  std::call_once(col_attr, [] {
-    for (auto kern : {slice_cols<8>, slice_cols<7>, slice_cols<6>})
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((size_t)OZ_MAX_SLICES * kSliceColN * kSliceColPitch * 4));
-  });
-  dim3 g2((unsigned)((n + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
-  cols_kern<<<g2, 256, col_smem, s>>>(B, k, n, ldb, kpad, eb, S, sb);
-  if ((st = nrs_after_launch(h, "ozaki slicing"))) return st;
-
-  CUtensorMap mapA, mapB;
-  if (!make_slice_map(&mapA, sa, kpad, m, S, OZ_BM) || !make_slice_map(&mapB, sb, kpad, n, S, OZ_BN))
-    return nrs_fail(h, NRS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the slices");
-
-  OzParams P{};
-  P.m = m;
-  P.n = n;
-  P.k = k;
-  P.kpad = kpad;
+  if ((st = launch_exponents(h, a, k, ea, colmax, nullptr))) return st;
+  if ((st = launch_exponents(h, bT, k, eb, colmax, nullptr))) return st;
+  if ((st = launch_slices(h, a, k, kpad, ea, b, S, sa))) return st;
+  if ((st = launch_slices(h, bT, k, kpad, eb, b, S, sb))) return st;
+  OzParams P = base_params(h, m, n, k, kpad);
   P.slices = S;
   P.kchunks = kchunks;
-  P.n_pairs = n_pairs;
-  P.tiles_m = (int)((m + OZ_BM - 1) / OZ_BM);
-  P.tiles_n = (int)((n + OZ_BN - 1) / OZ_BN);
-  P.group_m = 12;
+  P.n_pairs = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
   P.ea = ea;
   P.eb = eb;
   P.acc = acc;
@@ -778,18 +1104,96 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
   P.final_shift = 2 - 2 * b - b * (S - 1);
   P.digit_bits = b;
   P.kchunk = kChunkOf(b);
-  P.err = h->dev_error;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if ((st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     OZ_SMEM),
-                             "cudaFuncSetAttribute(ozaki)")))
-      return st;
-    attr_set = true;
+  P.accumulate = accumulate ? 1 : 0;
+  return launch_tc<false>(h, sa, sb, S, P);
+}
+
+}  // namespace
+
+extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, const double* A,
+                              int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
+                              unsigned flags, int slices, nrs_ozaki_info* info) {
+  if (!h) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  if (m < 0 || k < 0 || n < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative GEMM dimension");
+  if (flags & ~(NRS_GEMM_ACCUMULATE | NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B))
+    return nrs_fail(h, NRS_ERR_INVALID, "unknown GEMM flag");
+  const bool ta = flags & NRS_GEMM_TRANS_A, tb = flags & NRS_GEMM_TRANS_B;
+  const bool accumulate = flags & NRS_GEMM_ACCUMULATE;
+  if (ldc < (n > 0 ? n : 1)) return nrs_fail(h, NRS_ERR_SHAPE, "ldc < n");
+  if (lda < ((ta ? m : k) > 0 ? (ta ? m : k) : 1)) return nrs_fail(h, NRS_ERR_SHAPE, "lda too small");
+  if (ldb < ((tb ? k : n) > 0 ? (tb ? k : n) : 1)) return nrs_fail(h, NRS_ERR_SHAPE, "ldb too small");
+  if (slices < 0 || slices > OZ_MAX_SLICES)
+    return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
+  const int64_t kpad = ((k + 7) / 8) * 8;
+  if (info) std::memset(info, 0, sizeof(*info));
+  int b = 0, S = 0, kchunks = 0;
+  if (slices > 0) {
+    // Widest digits whose int32 diagonal sums stay exact for this K and S.
+    for (int cand = 8; cand >= 6 && !b; --cand) {
+      const int kc = (int)((kpad + kChunkOf(cand) - 1) / kChunkOf(cand));
+      if ((int64_t)(kc > 0 ? kc : 1) * slices < 128 && cand * slices <= 126) {
+        b = cand;
+        S = slices;
+        kchunks = kc;
+      }
+    }
+    if (!b)
+      return nrs_fail(h, NRS_ERR_TOO_LARGE,
+                      "k too large for this slice count (ceil(k / 16384) * S must be < 128)");
   }
-  const int n_tiles = P.tiles_m * P.tiles_n;
-  const int ctas = n_tiles < h->num_sms ? n_tiles : h->num_sms;
-  ozaki_tc_kernel<<<ctas, OZ_THREADS, OZ_SMEM, s>>>(mapA, mapB, P);
-  return nrs_after_launch(h, "ozaki_tc_kernel");
+  if (m == 0 || n == 0) return NRS_OK;
+  if (k == 0) {
+    if (accumulate) return NRS_OK;
+    return nrs_gemm(h, NRS_F64, m, 0, n, A, lda, B, ldb, C, ldc, 0, NRS_GEMM_GENERIC);
+  }
+  if (!A || !B || !C) return nrs_fail(h, NRS_ERR_INVALID, "null operand");
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  if (m > (1LL << 31) || n > (1LL << 31) || kpad > (1LL << 31))
+    return nrs_fail(h, NRS_ERR_TOO_LARGE, "dimension beyond 2^31");
+  const OzOperand a{A, lda, m, !ta};
+  const OzOperand bT{B, ldb, n, tb};
+
+  auto fallback = [&](const char*) {
+    // Native FP64 (DMMA) GEMM: non-finite operands, or a spread that no
+    // slice count within the limits covers.
+    if (info) {
+      info->slices = 0;
+      info->products = 0;
+      info->est_rel_error = 0.0;
+    }
+    return nrs_gemm(h, NRS_F64, m, k, n, A, lda, B, ldb, C, ldc, flags, NRS_GEMM_DMMA);
+  };
+
+  double spread = 0.0;
+  if (slices == 0) {
+    SpreadResult r{};
+    if ((st = spread_estimate(h, a, bT, m, n, k, kpad, 1, &r))) return st;
+    if (r.flags & 1u) return fallback("non-finite operand");
+    double need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+    if (!(std::isfinite((double)r.rmax) && choose_digits(kpad, need, &b, &S, &kchunks))) {
+      // The pass-1 numerator counts every k; pass 2 counts only the k where
+      // the other operand is nonzero (sparse and structured operands).
+      if ((st = spread_estimate(h, a, bT, m, n, k, kpad, 2, &r))) return st;
+      need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+      if (!(std::isfinite((double)r.rmax) && choose_digits(kpad, need, &b, &S, &kchunks))) {
+        if (info) info->spread = std::isfinite((double)r.rmax) ? (double)r.rmax : HUGE_VAL;
+        return fallback("spread beyond the slice limits");
+      }
+    }
+    spread = r.rmax;
+  }
+  if (info) {
+    info->slices = S;
+    info->products = S * (S + 1) / 2 * (kchunks > 0 ? kchunks : 1);
+    info->slice_bits = b;
+    info->k_chunk = kChunkOf(b);
+    info->spread = spread;
+    // auto: 2^-(bS) R_max (+ the final rounding); explicit: relative to
+    // rowmax|A| colmax|B| k, as no spread was measured
+    info->est_rel_error = slices == 0 ? std::ldexp(std::max(spread, 1.0), -b * S) + std::ldexp(1.0, -53)
+                                      : std::ldexp(2.0, -b * S);
+  }
+  return ozaki_run(h, a, bT, m, n, k, kpad, b, S, kchunks, C, ldc, accumulate);
 }

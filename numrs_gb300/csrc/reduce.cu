@@ -1213,6 +1213,28 @@ namespace {
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
 int g_noalloc_sms[kNoAllocMaxDevices] = {0};
+// The context the cached address belongs to: after cudaDeviceReset (or with
+// another context current) the module, and with it the array, can live at a
+// new address, so a different current context repeats the lookup.
+void* g_noalloc_ctx[kNoAllocMaxDevices] = {nullptr};
+
+typedef int (*ctx_get_current_fn)(void**);
+void* current_context() {
+  static ctx_get_current_fn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<ctx_get_current_fn>(p);
+    else
+      cudaGetLastError();
+  });
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 template <typename T>
 int noalloc_flat(cudaStream_t s, int op, int64_t n, const T* x, void* out, void* scratch, int sms) {
@@ -1249,6 +1271,9 @@ extern "C" int nrs_reduce_flat_noalloc(void* cuda_stream, int dtype, int op, int
   if (op != NRS_SUM && op != NRS_MEAN && op != NRS_MAX && op != NRS_MIN) return NRS_ERR_INVALID;
   if (n < 0 || !out || (n > 0 && !x)) return NRS_ERR_INVALID;
   if (n > kNoAllocMaxElems) return NRS_ERR_TOO_LARGE;
+  // An error left by earlier, unrelated work must not be reported as this
+  // call's launch failure: clear it before the first launch.
+  cudaGetLastError();
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
     cudaGetLastError();
@@ -1257,10 +1282,13 @@ extern "C" int nrs_reduce_flat_noalloc(void* cuda_stream, int dtype, int op, int
   void* scratch;
   int sms;
   {
-    // First call on a device: look up the array's device address with this
-    // device current, and its SM count. Later calls reuse both.
+    // First call on a device (or in a new context of it): look up the
+    // array's device address with this device current, and its SM count.
+    // Later calls in the same context reuse both.
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    void* ctx = current_context();
+    if (!g_noalloc_ptr[dev] || ctx != g_noalloc_ctx[dev]) {
+      g_noalloc_ptr[dev] = nullptr;
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) {
         cudaGetLastError();
@@ -1273,6 +1301,7 @@ extern "C" int nrs_reduce_flat_noalloc(void* cuda_stream, int dtype, int op, int
       }
       g_noalloc_sms[dev] = count;
       g_noalloc_ptr[dev] = p;
+      g_noalloc_ctx[dev] = ctx;
     }
     scratch = g_noalloc_ptr[dev];
     sms = g_noalloc_sms[dev];

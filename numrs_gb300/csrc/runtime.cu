@@ -113,8 +113,15 @@ extern "C" int nrs_create(int device, nrs_handle** out) {
     delete h;
     return st;
   }
+  h->hw_sms = h->num_sms;
   h->stream = h->own_stream;
   *out = h;
+  return NRS_OK;
+}
+
+extern "C" int nrs_set_sm_budget(nrs_handle* h, int sms) {
+  if (!h || sms < 0) return NRS_ERR_INVALID;
+  h->num_sms = (sms == 0 || sms > h->hw_sms) ? h->hw_sms : sms;
   return NRS_OK;
 }
 

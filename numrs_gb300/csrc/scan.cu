@@ -1175,9 +1175,11 @@ int flat_scan_t(nrs_handle* h, const T* x, int64_t n, int has_seed, Seed seed, T
   T* totals = ws;
   T* carries = ws + nchunks + 1;
   if ((reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
-    // Segments: a whole number of tiles each, at most two per SM.
+    // Segments: a whole number of tiles each, at most two per SM of the
+    // planning SM count (the segments decide the float rounding, so they do
+    // not follow the device or the handle's SM budget).
     const int64_t tiles = (n + seg_tile<T>() - 1) / seg_tile<T>();
-    const int64_t gmax = (int64_t)h->num_sms * 2 < 1024 ? (int64_t)h->num_sms * 2 : 1024;
+    const int64_t gmax = (int64_t)NRS_PLAN_SMS * 2 < 1024 ? (int64_t)NRS_PLAN_SMS * 2 : 1024;
     const int64_t seg = ((tiles + gmax - 1) / gmax) * seg_tile<T>();
     const int g = (int)((n + seg - 1) / seg);
     seg_totals<T, OP><<<g, 256, 0, h->stream>>>(x, n, seg, totals);

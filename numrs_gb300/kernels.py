@@ -324,18 +324,32 @@ def gemm_2d(m: int, k: int, n: int, a: torch.Tensor, b: torch.Tensor, c: torch.T
     L.check(st, h)
 
 
+def _logical_copy(t: torch.Tensor) -> torch.Tensor:
+    """A row-major copy of a view in logical order, made by the library's
+    ufunc kernel (kernels::borrow::operand copies non-contiguous operands the
+    same way, src/kernels/borrow.rs:59)."""
+    return run_program([(L.OP_INPUT, 0, 0.0)], [t])
+
+
+def _gemm_operands(a, b):
+    """(a, (ld, transposed)) and (b, ...) for the GEMM entry points: row- or
+    column-contiguous views go as they are, any other view is copied."""
+    sa, sb = _mat_strides(a), _mat_strides(b)
+    if sa is None:
+        a = _logical_copy(a)
+        sa = _mat_strides(a)
+    if sb is None:
+        b = _logical_copy(b)
+        sb = _mat_strides(b)
+    return a, sa, b, sb
+
+
 def _gemm_views(a, b, c, accumulate, variant):
     lib = L.load()
     h = handle(c.device.index)
     m, k = a.shape
     n = b.shape[1]
-    sa, sb = _mat_strides(a), _mat_strides(b)
-    if sa is None:
-        a = a.contiguous()
-        sa = _mat_strides(a)
-    if sb is None:
-        b = b.contiguous()
-        sb = _mat_strides(b)
+    a, sa, b, sb = _gemm_operands(a, b)
     flags = (L.GEMM_ACCUMULATE if accumulate else 0) | (L.GEMM_TRANS_A if sa[1] else 0) | (
         L.GEMM_TRANS_B if sb[1] else 0)
     ldc = c.stride(0) if m > 1 else _bi.max(n, 1)
@@ -345,49 +359,58 @@ def _gemm_views(a, b, c, accumulate, variant):
 
 
 def matmul(a: torch.Tensor, b: torch.Tensor, variant: int = L.GEMM_AUTO) -> torch.Tensor:
-    """Array::matmul: 2-D product, 1-D promotion, N-D batched with broadcast
-    batch dimensions (src/array/linalg.rs:153-266)."""
+    """Array::matmul (src/array/linalg.rs:153-266): two 2-D operands are one
+    GEMM; otherwise a 1-D operand becomes [1, k] (left) or [k, 1] (right) and
+    stays so in the result (the reference does not squeeze it), the batch
+    axes broadcast by NumPy's rules, and every panel is one GEMM of the batch
+    (batched_gemm, :56-136; f32/f64 panels run as one grouped launch).
+    0-D operands raise DimensionMismatch; mismatched inner or batch
+    dimensions raise ShapeMismatch."""
     _need_cuda(a, b)
     if a.dtype != b.dtype:
         raise L.NumRs2Error(L.ERR_DTYPE, "matmul operands must share a dtype")
-    if a.dim() == 0 or b.dim() == 0:
-        raise L.ShapeMismatch(L.ERR_SHAPE, "matmul needs at least 1-D operands")
-    squeeze_a = a.dim() == 1
-    squeeze_b = b.dim() == 1
-    if squeeze_a:
+    if a.dim() == 2 and b.dim() == 2:
+        if a.shape[1] != b.shape[0]:
+            raise L.ShapeMismatch(L.ERR_SHAPE, f"matmul: {tuple(a.shape)} @ {tuple(b.shape)}")
+        out = torch.empty((a.shape[0], b.shape[1]), dtype=a.dtype, device=a.device)
+        _gemm_views(a, b, out, False, variant)
+        return out
+    if a.dim() == 1:
         a = a.unsqueeze(0)
-    if squeeze_b:
+    if b.dim() == 1:
         b = b.unsqueeze(1)
+    if a.dim() < 2 or b.dim() < 2:
+        raise L.DimensionMismatch(L.ERR_AXIS, "matmul requires operands with at least 1 dimension")
     if a.shape[-1] != b.shape[-2]:
         raise L.ShapeMismatch(L.ERR_SHAPE, f"matmul: {tuple(a.shape)} @ {tuple(b.shape)}")
     m, k, n = a.shape[-2], a.shape[-1], b.shape[-1]
-    batch = torch.broadcast_shapes(a.shape[:-2], b.shape[:-2])
+    try:
+        batch = torch.broadcast_shapes(a.shape[:-2], b.shape[:-2])
+    except RuntimeError:
+        raise L.ShapeMismatch(L.ERR_SHAPE, f"matmul batch axes: {tuple(a.shape)} @ {tuple(b.shape)}") from None
     out = torch.empty((*batch, m, n), dtype=a.dtype, device=a.device)
+    if len(batch) == 0:
+        _gemm_views(a, b, out, False, variant)
+        return out
+    # Broadcast operands are stride-0 views, not copies: each panel is a
+    # view of the original operand (the reference materialises them,
+    # Array::broadcast_to, before borrowing the flat panels).
     ab = a.expand(*batch, m, k)
     bb = b.expand(*batch, k, n)
-    if len(batch) == 0:
-        _gemm_views(ab, bb, out, False, variant)
+    panels = []
+    for idx in range(out[..., 0, 0].numel()):
+        bi = torch.unravel_index(torch.tensor(idx), batch)
+        bi = tuple(int(x) for x in bi)
+        panels.append((ab[bi], bb[bi], out[bi]))
+    grouped_ok = a.dtype in (torch.float32, torch.float64) and variant == L.GEMM_AUTO and all(
+        _mat_strides(p[0]) is not None and _mat_strides(p[1]) is not None for p in panels)
+    if grouped_ok and m > 0 and n > 0:
+        plan = Plan([(pa, pb, pc, False) for pa, pb, pc in panels])
+        plan.run(use_graph=False)
+        plan.close()
     else:
-        # batched_gemm (src/array/linalg.rs:56-136): every batch panel of the
-        # broadcast operands; f32/f64 panels run as one grouped launch.
-        panels = []
-        for idx in range(out[..., 0, 0].numel()):
-            bi = torch.unravel_index(torch.tensor(idx), batch)
-            bi = tuple(int(x) for x in bi)
-            panels.append((ab[bi], bb[bi], out[bi]))
-        grouped_ok = a.dtype in (torch.float32, torch.float64) and variant == L.GEMM_AUTO and all(
-            _mat_strides(p[0]) is not None and _mat_strides(p[1]) is not None for p in panels)
-        if grouped_ok and m > 0 and n > 0:
-            plan = Plan([(pa, pb, pc, False) for pa, pb, pc in panels])
-            plan.run(use_graph=False)
-            plan.close()
-        else:
-            for pa, pb, pc in panels:
-                _gemm_views(pa, pb, pc, False, variant)
-    if squeeze_a:
-        out = out.squeeze(-2)
-    if squeeze_b:
-        out = out.squeeze(-1)
+        for pa, pb, pc in panels:
+            _gemm_views(pa, pb, pc, False, variant)
     return out
 
 
@@ -553,30 +576,65 @@ class Expr:
         return run_program(prog, uniq)
 
 
-def gemm_ozaki(a: torch.Tensor, b: torch.Tensor, slices: int = 0, out: torch.Tensor | None = None):
-    """f64 C = a @ b from BF16 slice products on the tensor cores (Ozaki
-    scheme); returns (C, info dict). Row-major contiguous f64 operands."""
+def gemm_ozaki(a: torch.Tensor, b: torch.Tensor, slices: int = 0, out: torch.Tensor | None = None,
+               accumulate: bool = False):
+    """f64 C = a @ b (or out += a @ b with accumulate) from BF16 slice products
+    on the tensor cores (Ozaki scheme); returns (C, info dict). slices = 0
+    picks the count from the operands' measured spread (info["slices"] == 0:
+    the call ran the native FP64 GEMM). Row- or column-contiguous operands
+    go as they are (transposed views included); other views are copied."""
     _need_cuda(a, b)
     if a.dtype != torch.float64 or b.dtype != torch.float64:
         raise L.NumRs2Error(L.ERR_DTYPE, "gemm_ozaki takes f64 operands")
     if a.dim() != 2 or b.dim() != 2 or a.shape[1] != b.shape[0]:
         raise L.ShapeMismatch(L.ERR_SHAPE, "gemm_ozaki shape mismatch")
-    a = a if a.stride(1) == 1 else a.contiguous()
-    b = b if b.stride(1) == 1 else b.contiguous()
     m, k = a.shape
     n = b.shape[1]
-    c = torch.empty((m, n), dtype=torch.float64, device=a.device) if out is None else out
+    if out is None:
+        if accumulate:
+            raise L.NumRs2Error(L.ERR_INVALID, "accumulate needs out")
+        c = torch.empty((m, n), dtype=torch.float64, device=a.device)
+    else:
+        c = out
+        if c.shape != (m, n) or c.dtype != torch.float64 or (c.stride(1) != 1 and n > 1):
+            raise L.ShapeMismatch(L.ERR_SHAPE, "gemm_ozaki output must be a row-contiguous m x n f64 array")
+    a, sa, b, sb = _gemm_operands(a, b)
     lib = L.load()
     h = handle(a.device.index)
     info = L.OzakiInfo()
-    lda = a.stride(0) if m > 1 else _bi.max(k, 1)
-    ldb = b.stride(0) if k > 1 else _bi.max(n, 1)
+    flags = (L.GEMM_ACCUMULATE if accumulate else 0) | (L.GEMM_TRANS_A if sa[1] else 0) | (
+        L.GEMM_TRANS_B if sb[1] else 0)
     ldc = c.stride(0) if m > 1 else _bi.max(n, 1)
-    st = lib.nrs_gemm_ozaki(h, m, k, n, _ptr(a), lda, _ptr(b), ldb, _ptr(c), ldc, slices,
+    st = lib.nrs_gemm_ozaki(h, m, k, n, _ptr(a), sa[0], _ptr(b), sb[0], _ptr(c), ldc, flags, slices,
                             C.byref(info))
     L.check(st, h)
     return c, {"slices": info.slices, "products": info.products, "slice_bits": info.slice_bits,
-               "k_chunk": info.k_chunk, "est_rel_error": info.est_rel_error}
+               "k_chunk": info.k_chunk, "est_rel_error": info.est_rel_error, "spread": info.spread}
+
+
+class sm_budget:
+    """Context manager: size the device handle's grids for at most `sms` SMs
+    (nrs_set_sm_budget); results do not change."""
+
+    def __init__(self, sms: int, device: int | None = None):
+        self.sms, self.h = sms, handle(device)
+
+    def __enter__(self):
+        L.check(L.load().nrs_set_sm_budget(self.h, self.sms), self.h)
+        return self
+
+    def __exit__(self, *exc):
+        L.load().nrs_set_sm_budget(self.h, 0)
+
+
+def probe_peak(kind: int, device: int | None = None) -> float:
+    """TFLOP/s of a compute pipe on this device (nrs_probe_peak):
+    L.PEAK_FP64_DMMA or L.PEAK_FP32_FMA."""
+    lib = L.load()
+    h = handle(device)
+    v = C.c_double()
+    L.check(lib.nrs_probe_peak(h, kind, C.byref(v)), h)
+    return v.value
 
 
 # ---------------------------------------------------------------------------

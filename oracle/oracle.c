@@ -93,8 +93,24 @@ void orc_gen_uniform_pm1_f32(uint64_t seed, int64_t n, float* out) {
 
 /* i64 uniform in [-2^20, 2^20): the top 21 bits minus 2^20, (x >> 43) - 2^20. */
 void orc_gen_i64(uint64_t seed, int64_t n, int64_t* out) {
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i)
     out[i] = (int64_t)(orc_splitmix64_at(seed, (uint64_t)i) >> 43) - (int64_t)(1 << 20);
+}
+
+/* N(mu, sigma) as f32: the device generator's formula (Box-Muller, cosine
+ * branch, on draws 2i and 2i+1, in double, then rounded to float). Host libm's
+ * log/cos may differ from the device's in the last bits of the double, so in
+ * rare cases a float element differs by one ulp from the device array. */
+void orc_gen_normal_f32(uint64_t seed, int64_t n, double mu, double sigma, float* out) {
+  const double two_pi = 6.283185307179586476925286766559;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const double u1 = 1.0 - sm64_u01(seed, 2 * (uint64_t)i);
+    const double u2 = sm64_u01(seed, 2 * (uint64_t)i + 1);
+    const double z = sqrt(-2.0 * log(u1)) * cos(two_pi * u2);
+    out[i] = (float)(mu + sigma * z);
+  }
 }
 
 /* ------------------------------------------------------------------------ */

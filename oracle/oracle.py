@@ -84,6 +84,7 @@ def _declare(L):
     L.orc_gen_uniform_pm1_f64.argtypes, L.orc_gen_uniform_pm1_f64.restype = [u64, i64, vp], None
     L.orc_gen_uniform_pm1_f32.argtypes, L.orc_gen_uniform_pm1_f32.restype = [u64, i64, vp], None
     L.orc_gen_i64.argtypes, L.orc_gen_i64.restype = [u64, i64, vp], None
+    L.orc_gen_normal_f32.argtypes, L.orc_gen_normal_f32.restype = [u64, i64, f64, f64, vp], None
     L.orc_num_threads.argtypes, L.orc_num_threads.restype = [], i32
     L.orc_set_threads.argtypes, L.orc_set_threads.restype = [i32], None
     L.orc_mlp_forward_backward.argtypes = [i64, i64, i64, i64] + [vp] * 16
@@ -305,6 +306,52 @@ class Oracle:
         getattr(self.L, f"orc_gemm_{_SUF[A.dtype]}")(m, k, n, _p(A), k, _p(B), n, _p(Cm), n)
         return Cm
 
+    def matmul(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        """Array::matmul (src/array/linalg.rs:153-266) over batched_gemm
+        (:56-136): two 2-D operands go straight to gemm_2d; otherwise a 1-D
+        operand is promoted to [1, k] (left) or [k, 1] (right) and KEPT in
+        the output shape, the batch axes (all but the last two) broadcast by
+        NumPy's rules (Array::broadcast_shape, src/array/manipulation.rs:16),
+        and every panel of the row-major broadcast operands is one gemm_2d.
+        Errors: ValueError("dimension") for a 0-D operand (DimensionMismatch),
+        ValueError("shape") for mismatched inner or batch dimensions
+        (ShapeMismatch)."""
+        a = np.asarray(a)
+        b = np.asarray(b)
+        if a.ndim == 2 and b.ndim == 2:
+            if a.shape[1] != b.shape[0]:
+                raise ValueError("shape")
+            return self.gemm(a, b)
+        if a.ndim == 1:
+            a = a.reshape(1, a.shape[0])
+        if b.ndim == 1:
+            b = b.reshape(b.shape[0], 1)
+        if a.ndim < 2 or b.ndim < 2:
+            raise ValueError("dimension")
+        m, k = a.shape[-2:]
+        k2, n = b.shape[-2:]
+        if k != k2:
+            raise ValueError("shape")
+        ba, bb = a.shape[:-2], b.shape[:-2]
+        nd = max(len(ba), len(bb))
+        pa, pb = (1,) * (nd - len(ba)) + ba, (1,) * (nd - len(bb)) + bb
+        batch = []
+        for x, y in zip(pa, pb):
+            if x == y or y == 1:
+                batch.append(x)
+            elif x == 1:
+                batch.append(y)
+            else:
+                raise ValueError("shape")
+        batch = tuple(batch)
+        af = np.ascontiguousarray(np.broadcast_to(a, batch + (m, k))).reshape(-1, m, k)
+        bf = np.ascontiguousarray(np.broadcast_to(b, batch + (k, n))).reshape(-1, k, n)
+        out = np.zeros((af.shape[0], m, n), dtype=a.dtype)
+        for t in range(af.shape[0]):
+            if m and n:
+                out[t] = self.gemm(af[t], bf[t]) if k else 0
+        return out.reshape(batch + (m, n))
+
     def gemm_dd(self, A: np.ndarray, B: np.ndarray):
         """Double-double product rounded to f64, and (|A||B|)_ij."""
         A = np.ascontiguousarray(A, dtype=np.float64)
@@ -341,6 +388,11 @@ class Oracle:
     def gen_i64(self, seed: int, n: int) -> np.ndarray:
         out = np.empty(n, dtype=np.int64)
         self.L.orc_gen_i64(seed, n, _p(out))
+        return out
+
+    def gen_normal_f32(self, seed: int, n: int, mu: float = 0.0, sigma: float = 1.0) -> np.ndarray:
+        out = np.empty(n, dtype=np.float32)
+        self.L.orc_gen_normal_f32(seed, n, mu, sigma, _p(out))
         return out
 
     # -- MLP selector -------------------------------------------------------

@@ -96,14 +96,23 @@ def test_transposed_and_accumulate(K, ora):
     assert np.max(np.abs(to_np(out) - (Cdd + 1.0))) <= 1e-12
 
 
-def test_matmul_batched_and_promotion(K):
-    a = torch.randn(3, 1, 20, 30, dtype=torch.float64, device="cuda")
-    b = torch.randn(4, 30, 10, dtype=torch.float64, device="cuda")
-    c = K.matmul(a, b)
-    assert tuple(c.shape) == (3, 4, 20, 10)
-    assert torch.allclose(c, torch.matmul(a, b), rtol=1e-12, atol=1e-12)
-    v = torch.randn(30, dtype=torch.float64, device="cuda")
-    assert tuple(K.matmul(a[0, 0], v).shape) == (20,)
+def test_matmul_batched_and_promotion(K, ora):
+    """Broadcast batch axes and 1-D promotion against the oracle's
+    Array::matmul restatement (more of the reference's cases in
+    tests/test_matmul_nd.py)."""
+    r = np.random.default_rng(12)
+    a = r.uniform(-1, 1, (3, 1, 20, 30))
+    b = r.uniform(-1, 1, (4, 30, 10))
+    c = to_np(K.matmul(_dev(a), _dev(b)))
+    want = ora.matmul(a, b)
+    assert c.shape == want.shape == (3, 4, 20, 10)
+    for i in range(3):
+        for j in range(4):
+            Cdd, ab = ora.gemm_dd(a[i, 0], b[j])
+            assert _err(c[i, j], Cdd, ab) <= 1e-14
+    v = r.uniform(-1, 1, 30)
+    c = to_np(K.matmul(_dev(a[0, 0]), _dev(v)))
+    assert c.shape == ora.matmul(a[0, 0], v).shape == (20, 1)
 
 
 def test_gemm_errors(K):

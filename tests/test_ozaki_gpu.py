@@ -94,3 +94,107 @@ def test_ozaki_digit_width_follows_k(K, ora, k, bits):
     e_oz = _err(to_np(C), Cdd, ab)
     e_dmma = _err(to_np(K.matmul(_dev(A), _dev(B), variant=L.GEMM_DMMA)), Cdd, ab)
     assert e_oz <= 1e-14 and e_oz <= max(3 * e_dmma, 5e-16), (e_oz, e_dmma, info)
+
+
+# ---------------------------------------------------------------------------
+# Automatic slice count (slices = 0): the measured spread decides
+# ---------------------------------------------------------------------------
+def _ozaki_operands(K, m, k, n, phi, seeds=(5, 6)):
+    A = torch.empty((m, k), dtype=torch.float64, device="cuda")
+    B = torch.empty((k, n), dtype=torch.float64, device="cuda")
+    K.fill_random(A, L.RNG_OZAKI, seeds[0], phi, 0.0)
+    K.fill_random(B, L.RNG_OZAKI, seeds[1], phi, 0.0)
+    return A, B
+
+
+@pytest.mark.parametrize("phi", [0.0, 1.0, 4.0])
+def test_ozaki_auto_count_full_oracle(K, ora, phi):
+    """1024^3, entries U(-0.5,0.5)*exp(phi*N(0,1)): with the automatic count
+    the componentwise error against the double-double product is at most
+    1e-14 and no worse than the native FP64 GEMM's own."""
+    A, B = _ozaki_operands(K, 1024, 1024, 1024, phi)
+    C, info = K.gemm_ozaki(A, B)
+    assert info["slices"] > 0, info
+    Cdd, ab = ora.gemm_dd(to_np(A), to_np(B))
+    e_oz = _err(to_np(C), Cdd, ab)
+    e_dmma = _err(to_np(K.matmul(A, B, variant=L.GEMM_DMMA)), Cdd, ab)
+    assert e_oz <= 1e-14, (phi, e_oz, e_dmma, info)
+    assert e_oz <= max(e_dmma, 1e-15), (phi, e_oz, e_dmma, info)
+    assert e_oz <= 4 * info["est_rel_error"], (e_oz, info)
+    if phi == 0.0:
+        assert info["slices"] == 7 and info["slice_bits"] == 8, info  # the fast case stays fast
+    if phi == 4.0:
+        assert info["slices"] >= 10, info
+
+
+def test_ozaki_auto_count_sampled_4096(K, ora):
+    """phi = 4 at 4096^3: 4096 random entries against double-double dots."""
+    n = 4096
+    A, B = _ozaki_operands(K, n, n, n, 4.0, seeds=(15, 16))
+    C, info = K.gemm_ozaki(A, B)
+    Cd = K.matmul(A, B, variant=L.GEMM_DMMA)
+    r = np.random.default_rng(9)
+    rows, cols = r.integers(0, n, 4096), r.integers(0, n, 4096)
+    ref, ab = ora.gemm_dd_sampled(to_np(A), to_np(B), rows, cols)
+    e_oz = float(np.max(np.abs(to_np(C)[rows, cols] - ref) / ab))
+    e_dmma = float(np.max(np.abs(to_np(Cd)[rows, cols] - ref) / ab))
+    assert e_oz <= 1e-14 and e_oz <= max(e_dmma, 1e-15), (e_oz, e_dmma, info)
+
+
+def test_ozaki_auto_identity_second_pass(K):
+    """I * I: every off-diagonal |A'||B'| is 0 while the row sums are not,
+    so the second pass (counting only k with a nonzero partner) sets the
+    count; the product is exact and the tensor cores still run it."""
+    n = 300
+    eye = torch.eye(n, dtype=torch.float64, device="cuda")
+    C, info = K.gemm_ozaki(eye, eye)
+    assert info["slices"] > 0, info
+    assert torch.equal(C, eye)
+    # block-diagonal operands: the same structure with random blocks
+    A = torch.zeros((256, 256), dtype=torch.float64, device="cuda")
+    B = torch.zeros_like(A)
+    a = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, (128, 128))).cuda()
+    b = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, (128, 128))).cuda()
+    A[:128, :128] = a
+    A[128:, 128:] = a
+    B[:128, :128] = b
+    B[128:, 128:] = b
+    C, info = K.gemm_ozaki(A, B)
+    assert info["slices"] > 0, info
+    assert torch.all(C[:128, 128:] == 0) and torch.all(C[128:, :128] == 0)
+
+
+def test_ozaki_auto_falls_back_to_fp64(K):
+    """Operands whose magnitudes that meet in a dot product are ~2^660 apart,
+    or that hold Inf / NaN, run the native FP64 GEMM (slices = 0 reported),
+    bit for bit the DMMA result."""
+    A = torch.tensor([[1.0, 1e-200], [2.0, 3.0]], dtype=torch.float64, device="cuda")
+    B = torch.tensor([[1e-200, 0.5], [1.0, 0.25]], dtype=torch.float64, device="cuda")
+    C, info = K.gemm_ozaki(A, B)
+    assert info["slices"] == 0, info
+    assert torch.equal(C, K.matmul(A, B, variant=L.GEMM_DMMA))
+    A2 = torch.ones((64, 64), dtype=torch.float64, device="cuda")
+    A2[3, 5] = float("inf")
+    A2[7, 1] = float("nan")
+    C, info = K.gemm_ozaki(A2, A2)
+    assert info["slices"] == 0
+    Cd = K.matmul(A2, A2, variant=L.GEMM_DMMA)
+    assert torch.equal(torch.isnan(C), torch.isnan(Cd)) and torch.equal(C[~torch.isnan(C)], Cd[~torch.isnan(Cd)])
+
+
+def test_ozaki_transposed_views_and_accumulate(K, ora):
+    """Transposed operand views go through the column slicers without a
+    copy; NRS_GEMM_ACCUMULATE adds the rounded product to C."""
+    m, k, n = 200, 333, 150
+    At = torch.from_numpy(ora.gen_uniform_pm1(21, m * k).reshape(k, m)).cuda()  # A = At.T
+    Bt = torch.from_numpy(ora.gen_uniform_pm1(22, k * n).reshape(n, k)).cuda()  # B = Bt.T
+    A, B = At.t(), Bt.t()
+    Cdd, ab = ora.gemm_dd(to_np(A), to_np(B))
+    for a, b in ((A, B), (A.contiguous(), B), (A, B.contiguous())):
+        C, info = K.gemm_ozaki(a, b)
+        assert _err(to_np(C), Cdd, ab) <= 1e-15, info
+    C0 = torch.full((m, n), 1.0, dtype=torch.float64, device="cuda")
+    C, _ = K.gemm_ozaki(A, B, out=C0, accumulate=True)
+    assert C is C0
+    want = 1.0 + to_np(K.gemm_ozaki(A, B)[0])
+    np.testing.assert_array_equal(to_np(C0), want)

@@ -78,3 +78,29 @@ def test_noalloc_rejects_beyond_the_limit_and_bad_args(K):
     assert lib.nrs_reduce_flat_noalloc(s, L.F32, L.PROD, 4, C.c_void_p(x.data_ptr()),
                                        C.c_void_p(out.data_ptr())) == L.ERR_INVALID
     assert lib.nrs_reduce_flat_noalloc(s, L.F32, L.SUM, 4, None, C.c_void_p(out.data_ptr())) == L.ERR_INVALID
+
+
+def test_noalloc_unaligned_input_and_alternating_calls(K):
+    """A view one element in (x[1:], not 16-byte aligned: the scalar-load
+    path) gives nrs_reduce's bits; f64 MAX and f32 SUM calls alternating on
+    one stream, all sharing the one array, each give their own result."""
+    lib = L.load()
+    g = torch.Generator(device="cuda").manual_seed(77)
+    for dtype in (torch.float32, torch.float64):
+        base = torch.randn(1_000_003, dtype=dtype, device="cuda", generator=g)
+        x = base[1:]
+        assert x.data_ptr() % 16 != 0
+        for op in (L.SUM, L.MAX):
+            got = _noalloc(lib, x, op)
+            torch.cuda.synchronize()
+            assert torch.equal(_bits(got), _bits(K.reduce(x, op))), (dtype, op)
+    a64 = torch.randn(3_000_001, dtype=torch.float64, device="cuda", generator=g)
+    b32 = torch.randn(2_000_003, dtype=torch.float32, device="cuda", generator=g)
+    outs = []
+    for _ in range(3):  # queued back to back, no synchronisation in between
+        outs.append((_noalloc(lib, a64, L.MAX), _noalloc(lib, b32, L.SUM)))
+    want_max, want_sum = K.reduce(a64, L.MAX), K.reduce(b32, L.SUM)
+    torch.cuda.synchronize()
+    for mx, sm in outs:
+        assert torch.equal(_bits(mx), _bits(want_max))
+        assert torch.equal(_bits(sm), _bits(want_sum))
