@@ -61,17 +61,12 @@ def whole_job_gbs(step_bytes: int, world: int, ms_per_step: float) -> float:
 
 
 def profiled_traffic(kernel_class: str):
-    """DRAM bytes per full-size launch of `kernel_class` recorded from an ncu
-    capture in profiles/*.md as a line `traffic_per_launch_bytes[<class>] = N`."""
-    import glob
-    import re
-    pat = re.compile(r"traffic_per_launch_bytes\[([^\]]+)\]\s*=\s*([0-9]+)")
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        for line in open(path):
-            m = pat.search(line)
-            if m and m.group(1) == kernel_class:
-                return int(m.group(2))
-    return None
+    """DRAM bytes per full-size launch of `kernel_class` from the ncu capture
+    recorded in profiles/traffic_per_launch.json (None if not recorded)."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    if not os.path.exists(p):
+        return None
+    return json.load(open(p))["traffic_per_launch_bytes"].get(kernel_class)
 
 
 def _peaks():

@@ -82,6 +82,14 @@ void* nrs_get_stream(nrs_handle* h);
 int nrs_set_sm_budget(nrs_handle* h, int sms);
 /* Waits for the stream, then reports any device-side error flag. */
 int nrs_synchronize(nrs_handle* h);
+/* Test support for the bounded-wait path (no reference counterpart): the
+ * next axis reduction on this handle served by the column-fold TMA pipeline
+ * leaves its first CTA's first tile unloaded, so that CTA waits on a barrier
+ * nothing completes; the wait gives up after `probes` probes, the CTA sets
+ * the device error word and returns, and the next nrs_synchronize reports
+ * NRS_ERR_TIMEOUT. Nothing faults or hangs, and the handle stays usable
+ * (that launch's output for the first 64 lanes is not written). */
+int nrs_test_expire_next_wait(nrs_handle* h, uint32_t probes);
 /* Message of the last failing call on this handle ("" if none). */
 const char* nrs_last_error(nrs_handle* h);
 

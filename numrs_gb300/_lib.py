@@ -93,6 +93,7 @@ SIGNATURES = {
     "nrs_accumulate": (_i, [_vp, _i, _i, _i, _P64, _P64, _i64, _vp, _vp, _P64]),
     "nrs_gemm": (_i, [_vp, _i, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u, _i]),
     "nrs_set_sm_budget": (_i, [_vp, _i]),
+    "nrs_test_expire_next_wait": (_i, [_vp, _u32]),
     "nrs_probe_peak": (_i, [_vp, _i, C.POINTER(C.c_double)]),
     "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u32, _i,
                             C.POINTER(OzakiInfo)]),

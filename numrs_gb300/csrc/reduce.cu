@@ -271,16 +271,25 @@ __global__ void __launch_bounds__(kColLanes)
   const int64_t l0 = (int64_t)blockIdx.x * LW;
   const int32_t batch = blockIdx.y;
   const int64_t n_tiles = (alen + RB - 1) / RB;
+  // Wait-expiry test hook (nrs_test_expire_next_wait): err[1], when set,
+  // makes the first CTA leave stage 0 unloaded, so its first wait is on a
+  // barrier nothing completes, bounded to err[1] probes. Other CTAs and all
+  // later launches run normally.
+  __shared__ uint32_t wait_limit, skip_stage0;
 
   if (t == 0) {
     prefetch_tensormap(&map);
     for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
     fence_mbar_init();
     abort_flag = 0;
+    const uint32_t probes = (blockIdx.x == 0 && blockIdx.y == 0) ? atomicExch(&err[1], 0u) : 0u;
+    skip_stage0 = probes != 0;
+    wait_limit = probes != 0 ? probes : NRS_WAIT_LIMIT;
   }
   __syncthreads();
   if (t == 0) {
     for (int s = 0; s < STAGES && s < n_tiles; ++s) {
+      if (s == 0 && skip_stage0) continue;
       mbar_arrive_expect_tx(&full[s], TILE);
       tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
     }
@@ -291,7 +300,7 @@ __global__ void __launch_bounds__(kColLanes)
   for (; it < n_tiles; ++it) {
     const int s = (int)(it % STAGES);
     const uint32_t phase = (uint32_t)((it / STAGES) & 1);
-    if (!mbar_wait_bounded(&full[s], phase, NRS_WAIT_LIMIT)) abort_flag = 1;
+    if (!mbar_wait_bounded(&full[s], phase, wait_limit)) abort_flag = 1;
     __syncthreads();
     if (abort_flag) break;
     const T* tile = reinterpret_cast<const T*>(smem + s * TILE);
@@ -311,11 +320,14 @@ __global__ void __launch_bounds__(kColLanes)
     }
   }
   if (abort_flag) {
-    // Drain: wait (bounded) for every copy this CTA issued and has not consumed.
+    // Drain: wait (bounded) for every copy this CTA issued and has not
+    // consumed (the stage the test hook left unloaded was never issued).
     if (t == 0) {
       atomicOr(err, NRS_DEVERR_REDUCE_TMA | (1u << 8));
-      for (int64_t j = it; j < n_tiles && j < it + STAGES; ++j)
+      for (int64_t j = it; j < n_tiles && j < it + STAGES; ++j) {
+        if (j == 0 && skip_stage0) continue;
         mbar_wait_bounded(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), NRS_WAIT_LIMIT);
+      }
     }
     return;
   }

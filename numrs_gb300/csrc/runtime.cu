@@ -173,6 +173,16 @@ extern "C" int nrs_synchronize(nrs_handle* h) {
   return NRS_OK;
 }
 
+extern "C" int nrs_test_expire_next_wait(nrs_handle* h, uint32_t probes) {
+  if (!h || probes == 0) return NRS_ERR_INVALID;
+  // Word 1 of the error block is read (and cleared) by the next column-fold
+  // launch on this handle's stream.
+  return nrs_cuda_check(h, cudaMemcpyAsync(h->dev_error + 1, &probes, sizeof(probes),
+                                           cudaMemcpyHostToDevice, h->stream),
+                        "cudaMemcpyAsync(test hook)") ||
+         nrs_cuda_check(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+}
+
 extern "C" const char* nrs_last_error(nrs_handle* h) { return h ? h->last_error.c_str() : ""; }
 
 extern "C" int nrs_malloc(nrs_handle* h, size_t bytes, void** p) {

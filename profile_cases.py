@@ -1,6 +1,6 @@
 """Small, self-contained launch cases for profiling one kernel at a time.
 
-    python -m numrs_gb300.profile_cases --case fold_cols_f32_max [--n 8192] [--launches 3]
+    python profile_cases.py --case fold_cols_f32_max [--n 8192] [--launches 3]
 
 Each case allocates inputs larger than the 129 MB L2 but only a few GB in
 total, runs one warm-up launch and then `--launches` launches of the kernel
@@ -12,8 +12,8 @@ import argparse
 
 import torch
 
-from . import _lib as L
-from . import kernels as K
+from numrs_gb300 import _lib as L
+from numrs_gb300 import kernels as K
 
 CASES = {
     "fold_cols_f32_sum": ("f32", L.SUM, 0),

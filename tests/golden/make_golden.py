@@ -1,8 +1,8 @@
 """Regenerates tests/golden/reference_goldens.json from the numrs2 source tree.
 
-Run in a checkout that has the reference at REF (default /root/reference):
+Run with the path of a numrs2 0.4.1 source tree:
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py REF
 
 It copies, verbatim, the reference's own test data for this path:
   * the NumPy-generated goldens read by tests/test_array_operations_reference.rs
@@ -52,4 +52,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <numrs2 source tree>")
+    main(sys.argv[1])

@@ -190,7 +190,7 @@ def test_selector_training_reduces_loss(K):
 def test_learned_selector_vs_heuristic_on_held_out_shapes(K):
     """Trains the selector on autotuner timings and compares, on held-out
     shapes, its picks and the size heuristic's against exhaustive tuning."""
-    from numrs_gb300 import tune_selector as TS
+    import tune_selector as TS
     res, sel, rows, _ = TS.run(360, 120, seed=11, reps=1, epochs=200, hi=1024,
                                f64_max_flops=2e10, f32_max_flops=2e11)
     print("selector", res["selector"], "heuristic", res["heuristic"])

@@ -1,7 +1,7 @@
 """Learned tile selection: collect autotuner timings, train the MLP selector
 on the GPU, evaluate it against exhaustive tuning.
 
-    python -m numrs_gb300.tune_selector --shapes 6700 --holdout 2000 \
+    python tune_selector.py --shapes 6700 --holdout 2000 \
         --out selector_run.json [--csv timings.csv] [--weights weights.npy]
 
 Shapes are log-uniform in [1, 16384]^3 (dtype f32 or f64 with equal
@@ -30,8 +30,8 @@ import time
 import numpy as np
 import torch
 
-from . import _lib as L
-from . import kernels as K
+from numrs_gb300 import _lib as L
+from numrs_gb300 import kernels as K
 
 
 def heuristic(dtype: int, m: int, k: int, n: int) -> int:
