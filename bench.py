@@ -502,24 +502,34 @@ def io_section(K, L):
     return out
 
 
-def grouped_section(K, L, seed: int = 7):
-    """4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64) and
-    4096 row reductions (length log-uniform in [64, 65536]) in one persistent
-    launch replayed from a CUDA graph, against launching them one by one."""
+def grouped_section(K, L, seed: int = 7, cpu: bool = True, peaks=None):
+    """C4: 4096 GEMMs (M, N, K log-uniform in [16, 512], half f32 / half f64)
+    and 4096 row reductions (length log-uniform in [64, 65536]) in one
+    persistent launch replayed from a CUDA graph: untuned, with the f64
+    GEMMs on the tensor cores, as chosen by the plan-level autotuner
+    (nrs_plan_autotune), and launched one by one. Roofline: the time the
+    group needs at the measured rates (f64 flops at the DMMA rate, or as BF16
+    slice products at the BF16 rate when the plan puts them on the tensor
+    cores; f32 flops at the FMA rate; reduction bytes at the HBM copy rate)
+    over the measured time."""
     import numpy as np
     import torch
     r = np.random.default_rng(seed)
     lu = lambda lo, hi, n: np.exp(r.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)  # noqa: E731
     M, N, Kd = lu(16, 512, 4096), lu(16, 512, 4096), lu(16, 512, 4096)
     gemms = []
-    flops = 0.0
+    f32_flops = f64_flops = 0.0
     for i in range(4096):
         dt = torch.float32 if i % 2 == 0 else torch.float64
         a = torch.empty((int(M[i]), int(Kd[i])), dtype=dt, device="cuda").uniform_(-1, 1)
         b = torch.empty((int(Kd[i]), int(N[i])), dtype=dt, device="cuda").uniform_(-1, 1)
         c = torch.empty((int(M[i]), int(N[i])), dtype=dt, device="cuda")
         gemms.append((a, b, c, False))
-        flops += 2.0 * M[i] * N[i] * Kd[i]
+        if dt == torch.float32:
+            f32_flops += 2.0 * M[i] * N[i] * Kd[i]
+        else:
+            f64_flops += 2.0 * M[i] * N[i] * Kd[i]
+    flops = f32_flops + f64_flops
     lens = lu(64, 65536, 4096)
     reds = []
     rbytes = 0
@@ -528,28 +538,22 @@ def grouped_section(K, L, seed: int = 7):
         reds.append((x, L.SUM, torch.empty(1, device="cuda")))
         rbytes += int(lens[i]) * 4
     stream = torch.cuda.current_stream()
-    # Tile choice without tuning (the size heuristic) for comparison.
     K.tuner_clear()
     plan_h = K.Plan(gemms, reds)
-    ms_h = _time_ms(lambda: plan_h.run(use_graph=True), 5, stream)
+    ms_h = _event_median_ms(lambda: plan_h.run(use_graph=True), 5, stream)
     plan_h.close()
-    # Exhaustive autotuning per shape bucket (log2-rounded m, k, n and dtype),
-    # each bucket timed as a grouped launch of as many copies as it has
-    # problems in this batch (capped at 64).
-    buckets = {}
-    for a, b, c, _ in gemms:
-        key = (L.F32 if a.dtype == torch.float32 else L.F64,
-               *(int(round(np.log2(v))) for v in (a.shape[0], a.shape[1], b.shape[1])))
-        buckets.setdefault(key, []).append((a.shape[0], a.shape[1], b.shape[1]))
+    # f64 GEMMs on the tensor cores, slice count from each problem's spread
+    plan_o = K.Plan(gemms, reds, f64_mode=L.PLAN_F64_OZAKI)
+    n_tc, oz_s, _ = plan_o.f64_info()
+    ms_o = _event_median_ms(lambda: plan_o.run(use_graph=True), 5, stream)
+    plan_o.close()
     t_tune = time.perf_counter()
-    for (dt, *_), shapes in buckets.items():
-        m, k, n = shapes[len(shapes) // 2]
-        _, best = K.tune_gemm(dt, m, k, n, batch=min(len(shapes), 64), reps=2)
-        K.tuner_set(dt, m, k, n, best)
+    rep = K.autotune_plan(gemms, reds, max_trials=48, reps=3, f64_ozaki=True)
     tune_s = time.perf_counter() - t_tune
-    plan = K.Plan(gemms, reds)
+    plan = K.Plan(gemms, reds, **rep["plan_kwargs"])
     st = plan.stats()
-    ms_g = _time_ms(lambda: plan.run(use_graph=True), 5, stream)
+    n_tc_final, s_final, b_final = plan.f64_info()
+    ms_g = _event_median_ms(lambda: plan.run(use_graph=True), 5, stream)
     K.tuner_clear()
 
     def one_by_one():
@@ -559,13 +563,71 @@ def grouped_section(K, L, seed: int = 7):
             K.reduce(x, op)
     ms_1 = _time_ms(one_by_one, 1, stream)
     plan.close()
-    f64_flops = sum(2.0 * M[i] * N[i] * Kd[i] for i in range(1, 4096, 2))
-    return {"gemms": 4096, "row_reductions": 4096, "work_items": st["work_items"],
-            "grouped_graph_ms": round(ms_g, 3), "one_by_one_ms": round(ms_1, 3),
-            "speedup": round(ms_1 / ms_g, 2), "gflops": round(flops / ms_g / 1e6, 1),
-            "f64_share_of_flops": round(f64_flops / flops, 3), "reduce_bytes": rbytes,
-            "tile_choice": f"autotuner: {len(buckets)} shape buckets tuned in {tune_s:.2f} s",
-            "heuristic_tiles_graph_ms": round(ms_h, 3)}
+    out = {"gemms": 4096, "row_reductions": 4096, "work_items": st["work_items"],
+           "grouped_graph_ms": round(ms_g, 3), "untuned_graph_ms": round(ms_h, 3),
+           "f64_on_tensor_cores_untuned_ms": round(ms_o, 3),
+           "f64_tensor_core_gemms": n_tc_final, "f64_slices": s_final, "f64_digit_bits": b_final,
+           "f64_tensor_core_gemms_auto": n_tc, "f64_slices_auto": oz_s,
+           "one_by_one_ms": round(ms_1, 3), "speedup_vs_one_by_one": round(ms_1 / ms_g, 2),
+           "gflops": round(flops / ms_g / 1e6, 1), "f64_share_of_flops": round(f64_flops / flops, 3),
+           "reduce_bytes": rbytes,
+           "autotune": {"seconds": round(tune_s, 2), "buckets": rep["buckets"], "trials": rep["trials"],
+                        "untuned_ms": round(rep["untuned_ms"], 3), "isolated_buckets_ms": round(rep["isolated_ms"], 3),
+                        "ozaki_mode_ms": round(rep["ozaki_ms"], 3), "final_ms": round(rep["final_ms"], 3),
+                        "chosen": rep["plan_kwargs"]}}
+    if peaks:
+        f32_t = f32_flops / (peaks["fp32_fma_tflops"] * 1e12)
+        red_t = rbytes / (_peaks()[0] * 1e9)
+        dmma_t = f64_flops / (peaks["fp64_dmma_tflops"] * 1e12)
+        if n_tc_final:
+            bf16_t = f64_flops * s_final * (s_final + 1) / 2 / (_bf16_peak() * 1e12)
+            t_lb, bound = (bf16_t + f32_t + red_t) * 1e3, "mixed: f64 as BF16 slice products + f32 FMA + HBM"
+        else:
+            t_lb, bound = (dmma_t + f32_t + red_t) * 1e3, "mixed: f64 DMMA + f32 FMA + HBM"
+        out["roofline"] = {"bound": bound, "kernel": "ozaki_tc_kernel (grouped) + grouped_kernel",
+                           "lower_bound_ms": round(t_lb, 3), "achieved_ms": round(ms_g, 3),
+                           "frac": round(t_lb / ms_g, 4), "unit": "ms",
+                           "f64_dmma_floor_ms": round(dmma_t * 1e3, 3)}
+    if cpu:
+        # the oracle's gemm_2d / reduce::sum restatements over the first 256
+        # GEMMs and 256 reductions of the same group, scaled to the 4096 + 4096
+        from oracle import Oracle
+        ora = Oracle()
+        sample = 256
+        ga = [(a.cpu().numpy(), b.cpu().numpy()) for a, b, _, _ in gemms[:sample]]
+        ra = [x.cpu().numpy() for x, _, _ in reds[:sample]]
+        t0 = time.perf_counter()
+        for a, b in ga:
+            ora.gemm(a, b)
+        for x in ra:
+            ora.flat("sum", x)
+        t_s = time.perf_counter() - t0
+        s_flops = sum(2.0 * a.shape[0] * a.shape[1] * b.shape[1] for a, b in ga)
+        s_work = s_flops + sum(x.nbytes for x in ra)
+        out["cpu_baseline"] = {"value": round(t_s * (flops + rbytes) / s_work * 1e3, 1),
+                               "unit": "ms (whole group, scaled by work)", "cores": ora.num_threads(), "kind": "port",
+                               "sample": f"first {sample} GEMMs + {sample} reductions of the group, {t_s:.2f} s",
+                               "gflops": round(s_flops / t_s / 1e9, 2)}
+    return out
+
+
+def selector_section(holdout: int = 300):
+    """C5: the MLP selector trained on the GPU on the committed autotuner
+    timings of this GPU model, evaluated on `holdout` shapes drawn now
+    (another seed of the same distribution) and tuned exhaustively: regret
+    against exhaustive tuning, beside the size heuristic's, and the tuning
+    time the selector saves."""
+    import tune_selector as TS
+    path = os.path.join(ROOT, "tests", "golden", "selector_timings_gb300.npz")
+    if not os.path.exists(path):
+        return {"unavailable": "no committed selector timings"}
+    t0 = time.perf_counter()
+    res, sel = TS.run_from_timings(path, holdout, seed=4242, reps=1)
+    sel.close()
+    res["seconds"] = round(time.perf_counter() - t0, 2)
+    res["target"] = "selector throughput within 5% of exhaustive tuning (>= 0.95)"
+    res["meets_target"] = res["selector"]["throughput_vs_exhaustive"] >= 0.95
+    return res
 
 
 def main():
@@ -581,6 +643,7 @@ def main():
     ap.add_argument("--no-gemm", action="store_true")
     ap.add_argument("--quick-gemm", action="store_true", help="2048^3 instead of 8192^3")
     ap.add_argument("--no-grouped", action="store_true")
+    ap.add_argument("--no-selector", action="store_true")
     ap.add_argument("--no-elementwise", action="store_true")
     ap.add_argument("--no-scan", action="store_true")
     ap.add_argument("--no-io", action="store_true")
@@ -839,7 +902,10 @@ def main():
     if rank == 0 and not args.no_io:
         out["io"] = io_section(K, L)
     if rank == 0 and not args.no_grouped:
-        out["grouped"] = grouped_section(K, L)
+        out["grouped"] = grouped_section(K, L, cpu=not args.no_cpu,
+                                         peaks=(out.get("gemm") or {}).get("peaks") or _gemm_peaks(K, L))
+    if rank == 0 and not args.no_selector:
+        out["selector"] = selector_section()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:

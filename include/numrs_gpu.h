@@ -430,7 +430,36 @@ typedef struct nrs_rowreduce_desc {
   void* out;     /* one element */
 } nrs_rowreduce_desc;
 
+/* Many f64 GEMMs on the tensor cores in one pass (no reference counterpart;
+ * the caller loop over gemm_2d, src/kernels/gemm.rs:246): every row-major
+ * problem's slices are made by one launch of each slicing kernel and every
+ * tile runs in one persistent tcgen05 launch, with one slice count for the
+ * group (0 = measured from each problem's spread, one read-back each; the
+ * largest count is used). Problems with transposed operands, Inf / NaN or a
+ * spread no count covers run on FP64 DMMA instead; on_tensor_cores[i]
+ * (may be NULL) says which. Returns after synchronising the stream. */
+int nrs_gemm_ozaki_grouped(nrs_handle* h, int64_t count, const nrs_gemm_desc* descs, int slices,
+                           int* on_tensor_cores, nrs_ozaki_info* info);
+
 typedef struct nrs_plan nrs_plan;
+
+/* Plan options (nrs_plan_create_ex). f64_mode NRS_PLAN_F64_DMMA (0): f64
+ * GEMMs run as FP64 DMMA tiles of the persistent kernel (nrs_plan_create's
+ * behaviour). NRS_PLAN_F64_OZAKI (1): row-major f64 GEMMs run first as one
+ * grouped Ozaki launch on the tensor cores (nrs_gemm_ozaki's scheme, one
+ * slice count for the group); f64_slices 0 = measured from each problem's
+ * spread when the plan is created (the largest count; problems whose spread
+ * no count covers, or with Inf / NaN, stay on DMMA tiles), 1..16 = given;
+ * f64_digit_bits 0 = the widest digits the group's K allows, or 6..8. The
+ * slice count is fixed when the plan is created: replaying it on data whose
+ * magnitudes are spread wider than at creation loses accuracy -- create the
+ * plan again (or give a count) when the data's range changes. */
+typedef enum nrs_plan_f64_mode { NRS_PLAN_F64_DMMA = 0, NRS_PLAN_F64_OZAKI = 1 } nrs_plan_f64_mode;
+typedef struct nrs_plan_options {
+  int32_t f64_mode;
+  int32_t f64_slices;
+  int32_t f64_digit_bits;
+} nrs_plan_options;
 
 /* Builds the tile/work queue for `n_gemm` GEMMs and `n_red` row reductions
  * (tile shapes from the autotuner's table, see nrs_tune_gemm) and uploads
@@ -438,7 +467,14 @@ typedef struct nrs_plan nrs_plan;
  * plan is used. */
 int nrs_plan_create(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
                     const nrs_rowreduce_desc* reds, nrs_plan** out);
-/* Runs the whole group as ONE persistent kernel launch. With use_graph != 0
+int nrs_plan_create_ex(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
+                       const nrs_rowreduce_desc* reds, const nrs_plan_options* options, nrs_plan** out);
+/* f64 GEMMs the plan runs on the tensor cores, with their slice count and
+ * digit width (0, 0, 0 for a DMMA-only plan). */
+int nrs_plan_f64_info(nrs_plan* plan, int64_t* on_tensor_cores, int* slices, int* digit_bits);
+/* Runs the whole group as ONE persistent kernel launch (preceded, with
+ * NRS_PLAN_F64_OZAKI, by the grouped tensor-core launch of its f64 GEMMs).
+ * With use_graph != 0
  * the launch is captured once into a CUDA graph owned by the plan and
  * replayed on later calls. */
 int nrs_plan_run(nrs_handle* h, nrs_plan* plan, int use_graph);
@@ -462,12 +498,45 @@ int nrs_tile_variant_info(int v, int* tile_m, int* tile_n, int* split_k, int* dt
  * fastest variant to *best. flags: NRS_GEMM_TRANS_A / NRS_GEMM_TRANS_B. */
 int nrs_tune_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, unsigned flags,
                   int64_t batch, int reps, float* times_us, int* best);
+/* Plan-level autotuning of a group (the problems nrs_plan_create would get):
+ * candidates are judged by timing the WHOLE group as one grouped launch, not
+ * one shape alone. Times (median of `reps` launches after a warm-up) the
+ * untuned plan; with `options` f64_mode OZAKI, the f64 GEMMs on the tensor
+ * cores at each digit width (the slice count follows from the width at the
+ * same accuracy); then every remaining shape bucket tuned in isolation
+ * (nrs_tune_gemm); and then, from the fastest so far, tries every other
+ * variant of the buckets with the most estimated work, keeping a change only
+ * if the group gets faster, until `max_trials` group timings. The tile
+ * choices go into the handle's tuner table (a later nrs_plan_create uses
+ * them) and the chosen f64 mode into report->options (pass it to
+ * nrs_plan_create_ex); the result is never slower than the untuned plan as
+ * measured. The group is run many times on the caller's buffers: C's
+ * contents are undefined afterwards (accumulating GEMMs are timed as
+ * overwriting ones). */
+typedef struct nrs_autotune_report {
+  double untuned_ms;   /* selector / size heuristic, f64 on DMMA tiles       */
+  double isolated_ms;  /* every bucket tuned alone                           */
+  double final_ms;     /* the choice written to the table / options          */
+  double ozaki_ms;     /* best tensor-core f64 mode tried (-1 if none)       */
+  int32_t buckets;     /* shape buckets tuned                                */
+  int32_t trials;      /* whole-group timings in the refinement pass         */
+  nrs_plan_options options; /* the f64 mode / digit width chosen             */
+} nrs_autotune_report;
+int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
+                      const nrs_rowreduce_desc* reds, const nrs_plan_options* options, int max_trials,
+                      int reps, nrs_autotune_report* report);
 /* Records the tuned variant for a shape bucket, used by nrs_plan_create. */
 int nrs_tuner_set(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, int variant);
 /* Looks a shape bucket up; -1 if untuned. */
 int nrs_tuner_get(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n);
 /* Clears the table. */
 int nrs_tuner_clear(nrs_handle* h);
+/* Saves / loads the table as a text file keyed by the GPU model, the driver
+ * version and the library build (a hash of its sources). Loading a file made
+ * for another GPU, driver or build returns NRS_ERR_UNSUPPORTED and changes
+ * nothing; loaded entries replace the table's entries for the same buckets. */
+int nrs_tuner_save(nrs_handle* h, const char* path);
+int nrs_tuner_load(nrs_handle* h, const char* path);
 
 /* MLP cost model: features[F] -> 2 x hidden ReLU layers -> one predicted
  * log-time per tile variant. Weights are kept in fp32 (master) and BF16
@@ -494,6 +563,11 @@ int nrs_selector_forward_backward(nrs_handle* h, nrs_selector* s, int64_t batch,
 int nrs_selector_train(nrs_handle* h, nrs_selector* s, int64_t n, const float* x,
                        const float* target, const float* mask, int epochs, int64_t batch,
                        float lr, uint64_t seed, float* loss);
+/* Saves / loads the fp32 master weights with the same key as the tuner
+ * table (refused for another GPU, driver or build; NRS_ERR_SHAPE for another
+ * network shape). */
+int nrs_selector_save(nrs_handle* h, nrs_selector* s, const char* path);
+int nrs_selector_load(nrs_handle* h, nrs_selector* s, const char* path);
 /* Predicted per-variant outputs y[n, V] for x[n, F] (device buffers). */
 int nrs_selector_predict(nrs_handle* h, nrs_selector* s, int64_t n, const float* x, float* y);
 /* Installs `s` (F = 7 features, V = NRS_TILE_VARIANTS outputs) as the choice

@@ -25,6 +25,7 @@ OP_NEG, OP_ABS, OP_SQRT, OP_EXP, OP_LN, OP_MAX, OP_MIN = 6, 7, 8, 9, 10, 11, 12
 GEMM_ACCUMULATE, GEMM_TRANS_A, GEMM_TRANS_B = 1, 2, 4
 GEMM_AUTO, GEMM_DMMA, GEMM_SIMT, GEMM_GENERIC, GEMM_SIMT_SMALL = 0, 1, 2, 3, 4
 PEAK_FP64_DMMA, PEAK_FP32_FMA = 0, 1
+PLAN_F64_DMMA, PLAN_F64_OZAKI = 0, 1
 RNG_UNIFORM, RNG_NORMAL, RNG_INT, RNG_OZAKI = 0, 1, 2, 3
 TILE_VARIANTS = 6
 
@@ -43,6 +44,16 @@ class UfuncOp(C.Structure):
 class OzakiInfo(C.Structure):
     _fields_ = [("slices", C.c_int32), ("products", C.c_int32), ("slice_bits", C.c_int32),
                 ("k_chunk", C.c_int32), ("est_rel_error", C.c_double), ("spread", C.c_double)]
+
+
+class PlanOptions(C.Structure):
+    _fields_ = [("f64_mode", C.c_int32), ("f64_slices", C.c_int32), ("f64_digit_bits", C.c_int32)]
+
+
+class AutotuneReport(C.Structure):
+    _fields_ = [("untuned_ms", C.c_double), ("isolated_ms", C.c_double), ("final_ms", C.c_double),
+                ("ozaki_ms", C.c_double), ("buckets", C.c_int32), ("trials", C.c_int32),
+                ("options", PlanOptions)]
 
 
 class GemmDesc(C.Structure):
@@ -97,6 +108,16 @@ SIGNATURES = {
     "nrs_probe_peak": (_i, [_vp, _i, C.POINTER(C.c_double)]),
     "nrs_gemm_ozaki": (_i, [_vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _u32, _i,
                             C.POINTER(OzakiInfo)]),
+    "nrs_tuner_save": (_i, [_vp, C.c_char_p]),
+    "nrs_tuner_load": (_i, [_vp, C.c_char_p]),
+    "nrs_selector_save": (_i, [_vp, _vp, C.c_char_p]),
+    "nrs_selector_load": (_i, [_vp, _vp, C.c_char_p]),
+    "nrs_plan_autotune": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
+                               C.POINTER(PlanOptions), _i, _i, C.POINTER(AutotuneReport)]),
+    "nrs_plan_create_ex": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
+                                C.POINTER(PlanOptions), C.POINTER(_vp)]),
+    "nrs_plan_f64_info": (_i, [_vp, C.POINTER(_i64), C.POINTER(_i), C.POINTER(_i)]),
+    "nrs_gemm_ozaki_grouped": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i, C.POINTER(_i), C.POINTER(OzakiInfo)]),
     "nrs_plan_create": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
                              C.POINTER(_vp)]),
     "nrs_plan_run": (_i, [_vp, _vp, _i]),

@@ -27,6 +27,18 @@ def nvcc() -> str:
     return cand
 
 
+def source_hash() -> str:
+    """16 hex digits of SHA-256 over the CUDA sources and the ABI header: the
+    build identity that keys saved tuner tables and selector weights."""
+    import hashlib
+    hsh = hashlib.sha256()
+    for p in sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cuh"))) + [
+            os.path.join(HERE, "..", "include", "numrs_gpu.h")]:
+        hsh.update(os.path.basename(p).encode())
+        hsh.update(open(p, "rb").read())
+    return hsh.hexdigest()[:16]
+
+
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     deps = [src] + glob.glob(os.path.join(CSRC, "*.cuh")) + [
@@ -49,9 +61,21 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             os.remove(o)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    # tuner.cu carries the build identity; recompile it whenever it changes
+    sh = source_hash()
+    mark = os.path.join(BUILD, "source_hash.txt")
+    tuner_obj = os.path.join(BUILD, "tuner.cu.o")
+    if not os.path.exists(mark) or open(mark).read().strip() != sh:
+        if os.path.exists(tuner_obj):
+            os.remove(tuner_obj)
+        with open(mark, "w") as f:
+            f.write(sh + "\n")
+
+    def flags(src):
+        return extra + ([f'-DNRS_SOURCE_HASH="{sh}"'] if os.path.basename(src) == "tuner.cu" else [])
     workers = min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(workers) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
+        objs = list(ex.map(lambda s: _compile(s, flags(s)), srcs))
     if os.path.exists(LIB) and not force and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"

@@ -98,7 +98,7 @@ DmmaPlan plan_dmma(int64_t m, int64_t n, int64_t k, int sms) {
 }
 
 template <typename T, int BM, int BN, int BK, int TM, int TN>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+__global__ void __launch_bounds__((BM / TM) * (BN / TN), (BM * BN >= 128 * 128 ? 2 : 1))
     simt_gemm(int64_t m, int64_t n, int64_t k, const T* __restrict__ A, int64_t rsa, int64_t csa,
               const T* __restrict__ B, int64_t rsb, int64_t csb, T* __restrict__ C, int64_t ldc,
               int accumulate) {

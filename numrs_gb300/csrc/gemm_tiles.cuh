@@ -118,15 +118,28 @@ struct Dmma {
 };
 
 // ---------------------------------------------------------------------------
-// SIMT register tile (f32 / f64): thread (tr, tc) owns rows tr + i*(BM/TM),
-// cols tc + j*(BN/TN).
+// SIMT register tile (f32 / f64). f32 tiles with TM, TN multiples of 4: thread
+// (tr, tc) owns TM/4 groups of 4 consecutive rows, group g at
+// g*(BM/(TM/4)) + 4*tr (columns likewise), so each k step reads its A and B
+// fragments as 16-byte shared loads (TM/4 + TN/4 of them per TM*TN FMAs).
+// Otherwise thread (tr, tc) owns rows tr + i*(BM/TM), cols tc + j*(BN/TN).
+// Either way every C element is the same k-ordered FMA chain, so the mapping
+// does not change a bit of the result.
 // ---------------------------------------------------------------------------
 template <typename T, int BM, int BN, int BK, int TM, int TN>
 struct Simt {
   static constexpr int NT = (BM / TM) * (BN / TN);
   static constexpr int LA = BM * BK / NT, LB = BN * BK / NT;
   static constexpr int kSmem = 2 * BK * ((BM + 4) + (BN + 4)) * (int)sizeof(T);
+  static constexpr bool kVec = sizeof(T) == 4 && TM % 4 == 0 && TN % 4 == 0;
   T acc[TM][TN];
+  // Row (column) of fragment element i (j) for thread row tr (column tc).
+  static __device__ __forceinline__ int row_of(int tr, int i) {
+    return kVec ? (i / 4) * (BM / (TM / 4)) + 4 * tr + (i % 4) : tr + i * (BM / TM);
+  }
+  static __device__ __forceinline__ int col_of(int tc, int j) {
+    return kVec ? (j / 4) * (BN / (TN / 4)) + 4 * tc + (j % 4) : tc + j * (BN / TN);
+  }
 
   __device__ __forceinline__ void run(const T* __restrict__ A, int64_t rsa, int64_t csa,
                                       const T* __restrict__ B, int64_t rsb, int64_t csb,
@@ -181,10 +194,23 @@ struct Simt {
 #pragma unroll
       for (int kk = 0; kk < BK; ++kk) {
         T a[TM], b[TN];
+        if constexpr (kVec) {
 #pragma unroll
-        for (int i = 0; i < TM; ++i) a[i] = As[buf][kk][tr + i * (BM / TM)];
+          for (int g = 0; g < TM / 4; ++g) {
+            const float4 v = *reinterpret_cast<const float4*>(&As[buf][kk][row_of(tr, 4 * g)]);
+            a[4 * g] = v.x, a[4 * g + 1] = v.y, a[4 * g + 2] = v.z, a[4 * g + 3] = v.w;
+          }
 #pragma unroll
-        for (int j = 0; j < TN; ++j) b[j] = Bs[buf][kk][tc + j * (BN / TN)];
+          for (int g = 0; g < TN / 4; ++g) {
+            const float4 v = *reinterpret_cast<const float4*>(&Bs[buf][kk][col_of(tc, 4 * g)]);
+            b[4 * g] = v.x, b[4 * g + 1] = v.y, b[4 * g + 2] = v.z, b[4 * g + 3] = v.w;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < TM; ++i) a[i] = As[buf][kk][row_of(tr, i)];
+#pragma unroll
+          for (int j = 0; j < TN; ++j) b[j] = Bs[buf][kk][col_of(tc, j)];
+        }
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -197,8 +223,8 @@ struct Simt {
   __device__ __forceinline__ void coords(int e, int& r, int& c) const {
     const int tid = threadIdx.x;
     const int tr = tid / (BN / TN), tc = tid % (BN / TN);
-    r = tr + (e / TN) * (BM / TM);
-    c = tc + (e % TN) * (BN / TN);
+    r = row_of(tr, e / TN);
+    c = col_of(tc, e % TN);
   }
   __device__ __forceinline__ T value(int e) const { return acc[e / TN][e % TN]; }
   static constexpr int kPerThread = TM * TN;

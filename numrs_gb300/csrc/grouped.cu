@@ -18,6 +18,8 @@
 // the counter for the next replay. No CTA ever waits on another.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <tuple>
 #include <vector>
 
 #include "gemm_tiles.cuh"
@@ -204,6 +206,10 @@ __global__ void __launch_bounds__(kThreads)
 struct nrs_plan {
   nrs_handle* h = nullptr;
   int64_t n_items = 0, gemm_tiles = 0;
+  // f64 GEMMs on the tensor cores (nrs_plan_options.f64_mode = OZAKI); they
+  // run before the persistent kernel, which then holds none of them.
+  nrs_ozaki_group* oz = nullptr;
+  int64_t oz_gemms = 0;
   nrs_gemm_desc* d_gemm = nullptr;
   nrs_rowreduce_desc* d_red = nullptr;
   WorkItem* d_items = nullptr;
@@ -245,6 +251,7 @@ void selector_features(const nrs_gemm_desc& d, int64_t batch, float* f) {
 
 void plan_free(nrs_plan* p) {
   if (!p) return;
+  nrs_ozaki_group_free(p->oz);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -259,8 +266,10 @@ void plan_free(nrs_plan* p) {
 
 // forced >= 0 forces every GEMM onto that variant (autotuning).
 int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
-               const nrs_rowreduce_desc* reds, int forced, nrs_plan** out) {
+               const nrs_rowreduce_desc* reds, int forced, const nrs_plan_options* opt, nrs_plan** out) {
   *out = nullptr;
+  if (opt && (opt->f64_mode != NRS_PLAN_F64_DMMA && opt->f64_mode != NRS_PLAN_F64_OZAKI))
+    return nrs_fail(h, NRS_ERR_INVALID, "unknown f64 mode");
   std::vector<int> var((size_t)n_gemm, -1);
   std::vector<int> need_sel;
   for (int64_t i = 0; i < n_gemm; ++i) {
@@ -310,6 +319,14 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
       return nrs_fail(h, NRS_ERR_INVALID, "grouped reductions: SUM, MEAN, MAX or MIN");
     if (r.len < 0 || !r.out || (r.len > 0 && !r.x)) return nrs_fail(h, NRS_ERR_INVALID, "bad row reduction");
   }
+  // f64 GEMMs on the tensor cores: the group takes what it can, the rest
+  // stays on DMMA tiles.
+  std::vector<int> on_tc((size_t)n_gemm, 0);
+  nrs_ozaki_group* oz = nullptr;
+  if (opt && opt->f64_mode == NRS_PLAN_F64_OZAKI && forced < 0 && n_gemm > 0) {
+    int st = nrs_ozaki_group_build(h, n_gemm, gemms, opt->f64_slices, opt->f64_digit_bits, on_tc.data(), &oz);
+    if (st) return st;
+  }
   // Work items with a cost estimate (ns on one SM) for longest-first order.
   struct Costed {
     double cost;
@@ -320,8 +337,13 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
   const double sms = h->num_sms > 0 ? h->num_sms : 1;
   const double f64_rate = 1.2e12 / sms, f32_rate = 60e12 / sms, bw = 6.5e12 / sms;
   int64_t gemm_tiles = 0;
+  int64_t oz_gemms = 0;
   for (int64_t i = 0; i < n_gemm; ++i) {
     const nrs_gemm_desc& d = gemms[i];
+    if (on_tc[i]) {
+      ++oz_gemms;
+      continue;
+    }
     if (d.m == 0 || d.n == 0) continue;
     const VariantDesc& v = kVariants[var[i]];
     const int tm = (int)((d.m + v.bm - 1) / v.bm), tn = (int)((d.n + v.bn - 1) / v.bn);
@@ -342,10 +364,15 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
     items.push_back({cost, WorkItem{1, (int32_t)i, -1, 0, 0, 0, 1, -1}});
   }
   std::stable_sort(items.begin(), items.end(), [](const Costed& a, const Costed& b) { return a.cost > b.cost; });
-  if (items.size() > 0x7fffffff) return nrs_fail(h, NRS_ERR_TOO_LARGE, "too many work items");
+  if (items.size() > 0x7fffffff) {
+    nrs_ozaki_group_free(oz);
+    return nrs_fail(h, NRS_ERR_TOO_LARGE, "too many work items");
+  }
 
   nrs_plan* p = new nrs_plan();
   p->h = h;
+  p->oz = oz;
+  p->oz_gemms = oz_gemms;
   p->n_items = (int64_t)items.size();
   p->gemm_tiles = gemm_tiles;
   std::vector<WorkItem> wi(items.size());
@@ -381,6 +408,11 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
 }
 
 int plan_launch(nrs_handle* h, nrs_plan* p, cudaStream_t s) {
+  if (p->oz) {
+    int st = nrs_ozaki_group_launch(h, p->oz, s);
+    if (st) return st;
+  }
+  if (p->n_items == 0) return NRS_OK;
   cudaMemsetAsync(p->d_counters, 0, sizeof(unsigned), s);
   grouped_kernel<<<p->grid, kThreads, 0, s>>>(p->d_gemm, p->d_red, p->d_items, (int)p->n_items,
                                               p->d_counters, p->d_counters + 1, p->d_partials);
@@ -396,7 +428,27 @@ extern "C" int nrs_plan_create(nrs_handle* h, int64_t n_gemm, const nrs_gemm_des
   h->last_error.clear();
   int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
   if (st) return st;
-  return plan_build(h, n_gemm, gemms, n_red, reds, -1, out);
+  return plan_build(h, n_gemm, gemms, n_red, reds, -1, nullptr, out);
+}
+
+extern "C" int nrs_plan_create_ex(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
+                                  const nrs_rowreduce_desc* reds, const nrs_plan_options* opt, nrs_plan** out) {
+  if (!h || !out || n_gemm < 0 || n_red < 0 || (n_gemm && !gemms) || (n_red && !reds))
+    return NRS_ERR_INVALID;
+  h->last_error.clear();
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  return plan_build(h, n_gemm, gemms, n_red, reds, -1, opt, out);
+}
+
+extern "C" int nrs_plan_f64_info(nrs_plan* p, int64_t* on_tensor_cores, int* slices, int* digit_bits) {
+  if (!p) return NRS_ERR_INVALID;
+  int s = 0, b = 0;
+  if (p->oz) nrs_ozaki_group_info(p->oz, &s, &b, nullptr);
+  if (on_tensor_cores) *on_tensor_cores = p->oz_gemms;
+  if (slices) *slices = s;
+  if (digit_bits) *digit_bits = b;
+  return NRS_OK;
 }
 
 extern "C" int nrs_plan_run(nrs_handle* h, nrs_plan* p, int use_graph) {
@@ -404,7 +456,7 @@ extern "C" int nrs_plan_run(nrs_handle* h, nrs_plan* p, int use_graph) {
   h->last_error.clear();
   int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
   if (st) return st;
-  if (p->n_items == 0) return NRS_OK;
+  if (p->n_items == 0 && !p->oz) return NRS_OK;
   if (!use_graph) return plan_launch(h, p, h->stream);
   cudaStream_t gs = h->own_stream;
   if (!p->exec) {
@@ -494,7 +546,7 @@ extern "C" int nrs_tune_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int
     times_us[v] = -1.f;
     if (kVariants[v].dtype != dtype) continue;
     nrs_plan* p = nullptr;
-    if ((st = plan_build(h, batch, descs.data(), 0, nullptr, v, &p)) != NRS_OK) break;
+    if ((st = plan_build(h, batch, descs.data(), 0, nullptr, v, nullptr, &p)) != NRS_OK) break;
     plan_launch(h, p, h->stream);
     cudaEventRecord(e0, h->stream);
     for (int r = 0; r < reps; ++r) plan_launch(h, p, h->stream);
@@ -517,4 +569,176 @@ extern "C" int nrs_tune_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int
   cudaFree(Cm);
   if (best) *best = best_v;
   return st;
+}
+
+// ---------------------------------------------------------------------------
+// Plan-level autotuning
+// ---------------------------------------------------------------------------
+// Tuning one shape bucket in isolation (nrs_tune_gemm: a launch of copies of
+// one problem) misses what decides a mixed launch: which tiles share the
+// machine and how the queue balances. nrs_plan_autotune therefore judges
+// every candidate by timing the caller's whole group:
+//   1. the untuned plan (selector or size heuristic), f64 on DMMA tiles,
+//   2. if the caller allows it, the f64 GEMMs on the tensor cores (grouped
+//      Ozaki) at each digit width -- 8, 7 or 6 bits, the slice count
+//      following from the width at the same accuracy -- kept if faster,
+//   3. every remaining bucket tuned in isolation,
+//   4. starting from the faster of 1-2 and 3, a greedy pass over the buckets
+//      with the most estimated work: each alternative variant is kept only
+//      if the whole group gets faster.
+// The final choice is never slower than the untuned plan as measured.
+namespace {
+
+struct TuneBucket {
+  int dtype;
+  int64_t m, k, n;  // a member's shape (every member maps to this bucket)
+  double work;      // estimated seconds at the pipe's rate
+  int64_t count;
+};
+
+int time_group(nrs_handle* h, const std::vector<nrs_gemm_desc>& g, int64_t n_red,
+               const nrs_rowreduce_desc* reds, int reps, cudaEvent_t e0, cudaEvent_t e1, const nrs_plan_options* opt,
+               double* ms) {
+  nrs_plan* p = nullptr;
+  int st = plan_build(h, (int64_t)g.size(), g.data(), n_red, reds, -1, opt, &p);
+  if (st) return st;
+  st = plan_launch(h, p, h->stream);  // warm-up
+  std::vector<float> ts;
+  for (int r = 0; r < reps && st == NRS_OK; ++r) {
+    cudaEventRecord(e0, h->stream);
+    st = plan_launch(h, p, h->stream);
+    cudaEventRecord(e1, h->stream);
+    if (st == NRS_OK) st = nrs_cuda_check(h, cudaEventSynchronize(e1), "autotune run");
+    float t = 0.f;
+    if (st == NRS_OK) cudaEventElapsedTime(&t, e0, e1);
+    ts.push_back(t);
+  }
+  cudaStreamSynchronize(h->stream);
+  plan_free(p);
+  if (st) return st;
+  std::sort(ts.begin(), ts.end());
+  *ms = ts[ts.size() / 2];
+  return NRS_OK;
+}
+
+}  // namespace
+
+extern "C" int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
+                                 const nrs_rowreduce_desc* reds, const nrs_plan_options* opt, int max_trials,
+                                 int reps, nrs_autotune_report* rep) {
+  if (!h || n_gemm < 0 || n_red < 0 || (n_gemm && !gemms) || (n_red && !reds) || max_trials < 0 || reps < 1)
+    return NRS_ERR_INVALID;
+  h->last_error.clear();
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  // The group runs repeatedly: accumulating GEMMs are tuned as overwriting
+  // ones (same tiles, same reads of A and B).
+  std::vector<nrs_gemm_desc> g(gemms, gemms + n_gemm);
+  for (auto& d : g) d.flags &= ~NRS_GEMM_ACCUMULATE;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto done = [&](int s2) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return s2;
+  };
+  auto key_of = [](const nrs_gemm_desc& d) {
+    auto lg = [](int64_t v) { return (int)std::lround(std::log2((double)(v < 1 ? 1 : v))); };
+    return std::make_tuple((int)d.dtype, lg(d.m), lg(d.k), lg(d.n));
+  };
+  // Buckets of the GEMMs the persistent kernel runs (row-major f64 ones
+  // leave it when they go to the tensor cores).
+  auto make_buckets = [&](bool skip_f64) {
+    std::map<std::tuple<int, int, int, int>, TuneBucket> bm;
+    for (const auto& d : g) {
+      if (d.m == 0 || d.n == 0 || d.k == 0 || (d.dtype != NRS_F32 && d.dtype != NRS_F64)) continue;
+      if (skip_f64 && d.dtype == NRS_F64 && !(d.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B))) continue;
+      auto& b = bm[key_of(d)];
+      if (b.count == 0) b = TuneBucket{d.dtype, d.m, d.k, d.n, 0.0, 0};
+      b.work += 2.0 * d.m * d.n * d.k / (d.dtype == NRS_F64 ? 1.1e12 : 70e12);
+      b.count++;
+    }
+    std::vector<TuneBucket> out;
+    for (auto& kv : bm) out.push_back(kv.second);
+    std::sort(out.begin(), out.end(), [](const TuneBucket& a, const TuneBucket& b) { return a.work > b.work; });
+    return out;
+  };
+  // 1. untuned, f64 on DMMA tiles
+  for (const auto& b : make_buckets(false)) nrs_tuner_forget(h, b.dtype, b.m, b.k, b.n);
+  double t_untuned = 0.0, t_isolated = 0.0;
+  if ((st = time_group(h, g, n_red, reds, reps, e0, e1, nullptr, &t_untuned))) return done(st);
+  // 2. the f64 mode: DMMA tiles, or the tensor cores at each digit width
+  nrs_plan_options best_opt{NRS_PLAN_F64_DMMA, 0, 0};
+  double t_mode = t_untuned, t_oz_best = -1.0;
+  if (opt && opt->f64_mode == NRS_PLAN_F64_OZAKI) {
+    for (int bits : {0, 7, 6}) {
+      if (opt->f64_digit_bits != 0 && bits != 0) continue;  // the caller fixed the width
+      nrs_plan_options o{NRS_PLAN_F64_OZAKI, opt->f64_slices, bits ? bits : opt->f64_digit_bits};
+      double t = 0.0;
+      if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &o, &t))) return done(st);
+      if (t_oz_best < 0 || t < t_oz_best) t_oz_best = t;
+      if (t < t_mode) {
+        t_mode = t;
+        best_opt = o;
+      }
+    }
+  }
+  const std::vector<TuneBucket> buckets = make_buckets(best_opt.f64_mode == NRS_PLAN_F64_OZAKI);
+  // 3. every bucket tuned in isolation
+  std::vector<int> untuned(buckets.size()), isolated(buckets.size());
+  for (size_t i = 0; i < buckets.size(); ++i) {
+    const auto& b = buckets[i];
+    untuned[i] = heuristic_variant(b.dtype, b.m, b.k, b.n);
+    float times[NRS_TILE_VARIANTS];
+    int best = -1;
+    if ((st = nrs_tune_gemm(h, b.dtype, b.m, b.k, b.n, 0, b.count < 64 ? b.count : 64, 2, times, &best)))
+      return done(st);
+    isolated[i] = best;
+    nrs_tuner_set(h, b.dtype, b.m, b.k, b.n, best);
+  }
+  if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &best_opt, &t_isolated))) return done(st);
+  // 4. greedy refinement from the faster start
+  std::vector<int> cur = isolated;
+  double t_best = t_isolated;
+  if (t_mode < t_isolated) {
+    cur = untuned;
+    for (size_t i = 0; i < buckets.size(); ++i)
+      nrs_tuner_set(h, buckets[i].dtype, buckets[i].m, buckets[i].k, buckets[i].n, cur[i]);
+    if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &best_opt, &t_best))) return done(st);
+    if (t_best > t_mode) {
+      // the representative shapes' variants lost to the per-problem untuned
+      // choices: keep those (no table entries) as the starting point
+      for (const auto& b : buckets) nrs_tuner_forget(h, b.dtype, b.m, b.k, b.n);
+      std::fill(cur.begin(), cur.end(), -1);
+      t_best = t_mode;
+    }
+  }
+  int trials = 0;
+  for (size_t i = 0; i < buckets.size() && trials < max_trials; ++i) {
+    const auto& b = buckets[i];
+    for (int v = 0; v < NRS_TILE_VARIANTS && trials < max_trials; ++v) {
+      if (kVariants[v].dtype != b.dtype || v == cur[i]) continue;
+      nrs_tuner_set(h, b.dtype, b.m, b.k, b.n, v);
+      double t = 0.0;
+      if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &best_opt, &t))) return done(st);
+      ++trials;
+      if (t < t_best * 0.997) {
+        t_best = t;
+        cur[i] = v;
+      }
+    }
+    if (cur[i] >= 0) nrs_tuner_set(h, b.dtype, b.m, b.k, b.n, cur[i]);
+    else nrs_tuner_forget(h, b.dtype, b.m, b.k, b.n);
+  }
+  if (rep) {
+    rep->untuned_ms = t_untuned;
+    rep->isolated_ms = t_isolated;
+    rep->final_ms = t_best;
+    rep->ozaki_ms = t_oz_best;
+    rep->buckets = (int32_t)buckets.size();
+    rep->trials = trials;
+    rep->options = best_opt;
+  }
+  return done(NRS_OK);
 }

@@ -46,6 +46,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "nrs_internal.cuh"
 
@@ -204,6 +205,41 @@ struct OzParams {
   const float* ra;
   const float* cb;
   uint32_t* est;
+  // Grouped launch only: the tile list and the problems it points into.
+  const struct OzTile* tiles;
+  const struct OzProb* probs;
+  int n_tiles;
+};
+
+// One problem of a grouped launch: its slices are rows [rowoff, rowoff + m)
+// of the stacked A slices and [coloff, coloff + n) of the stacked B^T slices
+// (row pitch = the group's largest kpad; this problem's rows are zero from
+// its own k to its kpad), its exponents sit at the same offsets, and its
+// int128 accumulators at accoff (m x n, row-major).
+struct OzProb {
+  int64_t m, n, kpad;
+  int64_t rowoff, coloff, accoff;
+  double* C;
+  int64_t ldc;
+  int32_t kchunks, n_pairs;
+  int32_t accumulate, pad;
+};
+struct OzTile {
+  int32_t prob, tm, tn, pad;
+};
+
+// Everything a CTA needs about the tile it works on.
+struct TileCtx {
+  int64_t m, n;        // the problem's C dimensions
+  int64_t arow, brow;  // TMA row coordinates of the tile's A / B^T boxes
+  int64_t row0, col0;  // tile origin inside the problem
+  int kblocks, n_pairs, kchunks;
+  const int* ea;
+  const int* eb;
+  __int128* acc;
+  double* C;
+  int64_t ldc;
+  int accumulate;
 };
 
 // Pair order within a tile: diagonals from the least significant (d = S-1)
@@ -233,6 +269,47 @@ __device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm
   tn = r / gm;
 }
 
+template <bool G>
+__device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
+  TileCtx c;
+  if (G) {
+    const OzTile t = P.tiles[tile];
+    const OzProb& q = P.probs[t.prob];
+    c.m = q.m;
+    c.n = q.n;
+    c.row0 = (int64_t)t.tm * OZ_BM;
+    c.col0 = (int64_t)t.tn * OZ_BN;
+    c.arow = q.rowoff + c.row0;
+    c.brow = q.coloff + c.col0;
+    c.kblocks = (int)((q.kpad + OZ_BK - 1) / OZ_BK);
+    c.n_pairs = q.n_pairs;
+    c.kchunks = q.kchunks;
+    c.ea = P.ea + q.rowoff;
+    c.eb = P.eb + q.coloff;
+    c.acc = P.acc + q.accoff;
+    c.C = q.C;
+    c.ldc = q.ldc;
+    c.accumulate = q.accumulate;
+  } else {
+    int tm, tn;
+    tile_coords(tile, P, tm, tn);
+    c.m = P.m;
+    c.n = P.n;
+    c.row0 = c.arow = (int64_t)tm * OZ_BM;
+    c.col0 = c.brow = (int64_t)tn * OZ_BN;
+    c.kblocks = (int)((P.kpad + OZ_BK - 1) / OZ_BK);
+    c.n_pairs = P.n_pairs;
+    c.kchunks = P.kchunks;
+    c.ea = P.ea;
+    c.eb = P.eb;
+    c.acc = P.acc;
+    c.C = P.C;
+    c.ldc = P.ldc;
+    c.accumulate = P.accumulate;
+  }
+  return c;
+}
+
 // EST = false: the slice-pair GEMM described in the file header.
 // EST = true : the same pipeline on the spread-estimate operands (one K chunk
 //              covering all of K): pass 1 (slices = 1) runs the one product
@@ -240,7 +317,7 @@ __device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm
 //              products N = |A'| 1_B^T + 1_A |B'|^T of slices 0 and 1 (|x'|
 //              and the nonzero indicator). The epilogue folds
 //              max_ij (numerator_ij / D_ij) into P.est instead of writing C.
-template <bool EST>
+template <bool EST, bool G>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                     OzParams P) {
@@ -255,8 +332,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_tiles = P.tiles_m * P.tiles_n;
-  const int kblocks_full = (int)((P.kpad + OZ_BK - 1) / OZ_BK);
+  const int n_tiles = G ? P.n_tiles : P.tiles_m * P.tiles_n;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < OZ_STAGES; ++s) {
@@ -298,21 +374,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       uint32_t it = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        int tm, tn;
-        tile_coords(tile, P, tm, tn);
-        for (int u = 0; u < P.n_pairs && ok; ++u) {
-          const PairOf pr = pair_of(u, P.slices, P.kchunks);
+        const TileCtx c = tile_ctx<G>(P, tile);
+        for (int u = 0; u < c.n_pairs && ok; ++u) {
+          const PairOf pr = pair_of(u, P.slices, c.kchunks);
           const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
           int kb1 = kb0 + P.kchunk / OZ_BK;
-          if (kb1 > kblocks_full) kb1 = kblocks_full;
+          if (kb1 > c.kblocks) kb1 = c.kblocks;
           for (int kb = kb0; kb < kb1; ++kb, ++it) {
             const int s = it % OZ_STAGES;
             const uint32_t ph = (it / OZ_STAGES) & 1;
             if (!bounded(&empty[s], ph ^ 1, 1)) { ok = false; break; }
             uint8_t* st = smem + s * OZ_STAGE_BYTES;
             mbar_arrive_expect_tx(&full[s], OZ_STAGE_BYTES);
-            tma_load_3d(st, &mapA, &full[s], kb * OZ_BK, tm * OZ_BM, pr.s);
-            tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, tn * OZ_BN, pr.t);
+            tma_load_3d(st, &mapA, &full[s], kb * OZ_BK, (int32_t)c.arow, pr.s);
+            tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, (int32_t)c.brow, pr.t);
           }
         }
       }
@@ -328,11 +403,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       uint32_t it = 0, ai = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        for (int u = 0; u < P.n_pairs && ok; ++u, ++ai) {
-          const PairOf pr = pair_of(u, P.slices, P.kchunks);
+        const TileCtx c = tile_ctx<G>(P, tile);
+        for (int u = 0; u < c.n_pairs && ok; ++u, ++ai) {
+          const PairOf pr = pair_of(u, P.slices, c.kchunks);
           const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
           int kb1 = kb0 + P.kchunk / OZ_BK;
-          if (kb1 > kblocks_full) kb1 = kblocks_full;
+          if (kb1 > c.kblocks) kb1 = c.kblocks;
           // One accumulator (TMEM columns 0..255); the epilogue frees it as
           // soon as it has folded it into the diagonal sums (columns 256..511).
           const int buf = 0;
@@ -380,13 +456,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     float rmax = 0.0f;
     bool ok = true;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-      int tm, tn;
-      tile_coords(tile, P, tm, tn);
-      const int64_t row = (int64_t)tm * OZ_BM + row_in_tile;
-      const bool row_ok = row < P.m;
-      const int64_t col0 = (int64_t)tn * OZ_BN + half * (OZ_BN / 2);
+      const TileCtx tc = tile_ctx<G>(P, tile);
+      const int64_t row = tc.row0 + row_in_tile;
+      const bool row_ok = row < tc.m;
+      const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
       const float ra = row_ok ? P.ra[row] : 0.0f;
-      for (int u = 0; u < P.n_pairs; ++u, ++ai) {
+      for (int u = 0; u < tc.n_pairs; ++u, ++ai) {
         const PairOf pr = pair_of(u, P.slices, 1);
         if (!bounded(&accf[0], ai & 1, 4)) { ok = false; break; }
         tc_fence_after();
@@ -425,7 +500,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
             const int64_t col = col0 + c * 16 + e;
-            if (col >= P.n) continue;
+            if (col >= tc.n) continue;
             const float D = __uint_as_float(v[c * 16 + e]);
             const float num = P.slices == 2 ? __uint_as_float(w[e]) : ra + P.cb[col];
             float r;
@@ -462,14 +537,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     bool ok = true;
     int prev_d = -1;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-      int tm, tn;
-      tile_coords(tile, P, tm, tn);
-      const int64_t row = (int64_t)tm * OZ_BM + row_in_tile;
-      const bool row_ok = row < P.m;
-      const int64_t col0 = (int64_t)tn * OZ_BN + half * (OZ_BN / 2);
+      const TileCtx tc = tile_ctx<G>(P, tile);
+      const int64_t row = tc.row0 + row_in_tile;
+      const bool row_ok = row < tc.m;
+      const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
       prev_d = -1;
-      for (int u = 0; u < P.n_pairs; ++u, ++ai) {
-        const PairOf pr = pair_of(u, P.slices, P.kchunks);
+      for (int u = 0; u < tc.n_pairs; ++u, ++ai) {
+        const PairOf pr = pair_of(u, P.slices, tc.kchunks);
         const int d = pr.s + pr.t;
         const bool diag_start = (d != prev_d);
         prev_d = d;
@@ -507,13 +581,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_before();
         __syncwarp();
         // Is this the last unit of its diagonal?
-        const bool diag_end = (u == P.n_pairs - 1) || (pair_of(u + 1, P.slices, P.kchunks).s +
-                                                      pair_of(u + 1, P.slices, P.kchunks).t) != d;
+        const bool diag_end = (u == tc.n_pairs - 1) || (pair_of(u + 1, P.slices, tc.kchunks).s +
+                                                       pair_of(u + 1, P.slices, tc.kchunks).t) != d;
         if (!diag_end) continue;
         const bool first = (d == P.slices - 1), last = (d == 0);
         const int shift = P.digit_bits * (P.slices - 1 - d);
-        const int ecol_base = (last && row_ok) ? P.ea[row] + P.final_shift : 0;
-        __int128* accp = P.acc + (row_ok ? row : 0) * P.n + col0;
+        const int ecol_base = (last && row_ok) ? tc.ea[row] + P.final_shift : 0;
+        __int128* accp = tc.acc + (row_ok ? row : 0) * tc.n + col0;
 #pragma unroll 1
         for (int c = 0; c < OZ_BN / 32; ++c) {
           uint32_t w[16];
@@ -523,7 +597,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           for (int e = 0; e < 16; ++e) {
             const int j = c * 16 + e;
             const int64_t col = col0 + j;
-            if (col >= P.n) continue;
+            if (col >= tc.n) continue;
             const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
             const __int128 sum = first ? contrib : (accp[j] + contrib);
             if (!last) {
@@ -537,10 +611,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
               if (hi) sh = 64 - __clzll((long long)hi);
               const uint64_t top = (uint64_t)(mag >> sh);
               double val = (double)top;
-              val = ldexp(val, sh + ecol_base + P.eb[col]);
-              double* cp = P.C + row * P.ldc + col;
+              val = ldexp(val, sh + ecol_base + tc.eb[col]);
+              double* cp = tc.C + row * tc.ldc + col;
               const double r = neg ? -val : val;
-              *cp = P.accumulate ? *cp + r : r;
+              *cp = tc.accumulate ? *cp + r : r;
             }
           }
         }
@@ -763,13 +837,32 @@ __global__ void __launch_bounds__(256)
 // products of small |x'| above FP32's underflow threshold while every sum
 // over K stays below 2^96 * 2^31 < 2^128. Row sums of |x'| (fp32, fixed
 // order) give the pass-1 numerator.
-__device__ __forceinline__ uint32_t bf16_rn_bits(float f) {
-  // round to nearest even on the bit pattern (f is finite and >= 0)
-  const uint32_t u = __float_as_uint(f);
-  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
-}
 constexpr uint32_t kBf16Two48 = 0x5780u;  // 2^48 in BF16
-constexpr float kTwo48 = 281474976710656.0f;
+
+__device__ __forceinline__ bool nonzero(double x) {
+  return ((uint64_t)__double_as_longlong(x) << 1) != 0;  // integer test, +-0 excluded
+}
+
+// |x| 2^-e from the bit pattern alone (no FP64 arithmetic: GB300's FP64 pipe
+// is slow): *f = |x'| as fp32 (mantissa truncated), return value = |x'| 2^48
+// as BF16 (round to nearest even). Subnormal x and values below the formats'
+// normal ranges give 0 (the estimate then only grows).
+__device__ __forceinline__ uint32_t est_bits(double x, int e, float* f) {
+  const uint64_t u = (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+  const int be = (int)(u >> 52);
+  const uint64_t mant = u & 0xFFFFFFFFFFFFFULL;
+  const int fe = be - 1023 - e;  // unbiased exponent of |x'| (<= -1)
+  if (be == 0) {
+    *f = 0.0f;
+    return 0u;
+  }
+  *f = (fe + 127 >= 1) ? __uint_as_float(((uint32_t)(fe + 127) << 23) | (uint32_t)(mant >> 29)) : 0.0f;
+  if (fe + 48 + 127 < 1) return 0u;
+  uint32_t h = ((uint32_t)(fe + 48 + 127) << 7) | (uint32_t)(mant >> 45);
+  const uint64_t rem = mant & ((1ULL << 45) - 1), half = 1ULL << 44;
+  if (rem > half || (rem == half && (h & 1u))) ++h;
+  return h;
+}
 
 // X (rows x k, row pitch ld, contiguous along k) -> out [2][rows][kpad],
 // sums[row] = sum_k |x'|. One warp per row, 8 consecutive k per lane step.
@@ -780,7 +873,7 @@ __global__ void __launch_bounds__(256)
   const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
-  const double sc = ldexp(1.0, -e[row]);
+  const int er = e[row];
   const double* xr = X + row * ld;
   float s = 0.0f;
   for (int64_t j0 = (int64_t)lane * 8; j0 < kpad; j0 += 256) {
@@ -799,11 +892,12 @@ __global__ void __launch_bounds__(256)
     uint32_t pa[4], pi[4];
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
-      const float f0 = (float)(fabs(x[2 * h]) * sc), f1 = (float)(fabs(x[2 * h + 1]) * sc);
+      float f0, f1;
+      const uint32_t b0 = est_bits(x[2 * h], er, &f0), b1 = est_bits(x[2 * h + 1], er, &f1);
       s += f0;
       s += f1;
-      pa[h] = bf16_rn_bits(f0 * kTwo48) | (bf16_rn_bits(f1 * kTwo48) << 16);
-      pi[h] = (x[2 * h] != 0.0 ? kBf16Two48 : 0u) | ((x[2 * h + 1] != 0.0 ? kBf16Two48 : 0u) << 16);
+      pa[h] = b0 | (b1 << 16);
+      pi[h] = (nonzero(x[2 * h]) ? kBf16Two48 : 0u) | ((nonzero(x[2 * h + 1]) ? kBf16Two48 : 0u) << 16);
     }
     uint16_t* o = out + row * kpad + j0;
     *reinterpret_cast<uint4*>(o) = make_uint4(pa[0], pa[1], pa[2], pa[3]);
@@ -824,7 +918,7 @@ __global__ void __launch_bounds__(256)
   const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int64_t nn = n0 + tx;
-  const double sc = nn < cols ? ldexp(1.0, -e[nn]) : 0.0;
+  const int ec = nn < cols ? e[nn] : 0;
   float s = 0.0f;
 #pragma unroll
   for (int r = 0; r < kSliceColK / 16; ++r) {
@@ -832,11 +926,12 @@ __global__ void __launch_bounds__(256)
     const int64_t kk = k0 + 2 * w;
     const double x0 = kk < k && nn < cols ? X[kk * ld + nn] : 0.0;
     const double x1 = kk + 1 < k && nn < cols ? X[(kk + 1) * ld + nn] : 0.0;
-    const float f0 = (float)(fabs(x0) * sc), f1 = (float)(fabs(x1) * sc);
+    float f0, f1;
+    const uint32_t b0 = est_bits(x0, ec, &f0), b1 = est_bits(x1, ec, &f1);
     s += f0;
     s += f1;
-    tile[0][tx][w] = bf16_rn_bits(f0 * kTwo48) | (bf16_rn_bits(f1 * kTwo48) << 16);
-    tile[1][tx][w] = (x0 != 0.0 ? kBf16Two48 : 0u) | ((x1 != 0.0 ? kBf16Two48 : 0u) << 16);
+    tile[0][tx][w] = b0 | (b1 << 16);
+    tile[1][tx][w] = (nonzero(x0) ? kBf16Two48 : 0u) | ((nonzero(x1) ? kBf16Two48 : 0u) << 16);
   }
   csum[ty][tx] = s;
   __syncthreads();
@@ -959,19 +1054,22 @@ int launch_est_operand(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpa
   return nrs_after_launch(h, "ozaki spread operands");
 }
 
-template <bool EST>
-int launch_tc(nrs_handle* h, const void* sa, const void* sb, int S, const OzParams& P) {
+// rows_a / rows_b: rows of the (stacked) slice buffers; P.kpad: their pitch.
+template <bool EST, bool G>
+int launch_tc(nrs_handle* h, const void* sa, const void* sb, int S, const OzParams& P, int64_t rows_a,
+              int64_t rows_b, cudaStream_t stream) {
   CUtensorMap mapA, mapB;
-  if (!make_slice_map(&mapA, sa, P.kpad, P.m, S, OZ_BM) || !make_slice_map(&mapB, sb, P.kpad, P.n, S, OZ_BN))
+  if (!make_slice_map(&mapA, sa, P.kpad, rows_a, S, OZ_BM) || !make_slice_map(&mapB, sb, P.kpad, rows_b, S, OZ_BN))
     return nrs_fail(h, NRS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the slices");
   // Set on every call: the attribute belongs to the current device's context.
-  int st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel<EST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  int st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel<EST, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   OZ_SMEM),
                           "cudaFuncSetAttribute(ozaki)");
   if (st) return st;
-  const int n_tiles = P.tiles_m * P.tiles_n;
+  const int n_tiles = G ? P.n_tiles : P.tiles_m * P.tiles_n;
   const int ctas = n_tiles < h->num_sms ? n_tiles : h->num_sms;
-  ozaki_tc_kernel<EST><<<ctas, OZ_THREADS, OZ_SMEM, h->stream>>>(mapA, mapB, P);
+  if (ctas < 1) return NRS_OK;
+  ozaki_tc_kernel<EST, G><<<ctas, OZ_THREADS, OZ_SMEM, stream>>>(mapA, mapB, P);
   return nrs_after_launch(h, EST ? "ozaki_tc_kernel<est>" : "ozaki_tc_kernel");
 }
 
@@ -1055,7 +1153,7 @@ int spread_estimate(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int6
   P.ra = ra;
   P.cb = cb;
   P.est = word;
-  if ((st = launch_tc<true>(h, sa, sb, 2, P))) return st;
+  if ((st = launch_tc<true, false>(h, sa, sb, 2, P, m, n, s))) return st;
   uint32_t host[2] = {0, 0};
   if ((st = nrs_cuda_check(h, cudaMemcpyAsync(host, word, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync")))
     return st;
@@ -1105,7 +1203,138 @@ int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m,
   P.digit_bits = b;
   P.kchunk = kChunkOf(b);
   P.accumulate = accumulate ? 1 : 0;
-  return launch_tc<false>(h, sa, sb, S, P);
+  return launch_tc<false, false>(h, sa, sb, S, P, m, n, h->stream);
+}
+
+// ---------------------------------------------------------------------------
+// Grouped launch: many f64 problems in one pass of each kernel
+// ---------------------------------------------------------------------------
+// The problems' slices are stacked: problem p owns rows [rowoff, rowoff + m)
+// of the A slices and [coloff, coloff + n) of the B^T slices, all with the
+// group's pitch KP (the largest kpad, a multiple of 64); columns [k, kpad) of
+// its rows are zero and columns beyond its kpad are never read. One launch
+// of each pre-processing kernel covers every problem through a chunk table,
+// and one persistent tensor-core launch covers every tile.
+struct OzIn {
+  const double* A;
+  int64_t lda;
+  const double* B;
+  int64_t ldb;
+  int64_t m, n, k, kpad;
+  int64_t rowoff, coloff;
+};
+struct OzChunk {
+  int32_t prob, r0, k0, pad;  // problem, first row (column), first k
+};
+
+// Row exponents of every A: one warp per row, 8 rows per block.
+__global__ void __launch_bounds__(256)
+    g_row_exponents(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, int* __restrict__ ea) {
+  const OzChunk c = ch[blockIdx.x];
+  const OzIn q = in[c.prob];
+  const int64_t row = (int64_t)c.r0 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= q.m) return;
+  uint64_t mx = 0;
+  for (int64_t j = lane; j < q.k; j += 32) {
+    const uint64_t v = (uint64_t)__double_as_longlong(q.A[row * q.lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = v > mx ? v : mx;
+  }
+  for (int off = 16; off; off >>= 1) {
+    const uint64_t o = __shfl_xor_sync(0xffffffffu, mx, off);
+    mx = o > mx ? o : mx;
+  }
+  if (lane == 0) ea[q.rowoff + row] = ((mx >> 52) == 0) ? -1021 : (int)(mx >> 52) - 1022;
+}
+
+// Column maxima of every B: 256 columns x 256 k per block, atomicMax on the
+// bit patterns into a zeroed array.
+__global__ void __launch_bounds__(256)
+    g_col_max_bits(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, unsigned long long* __restrict__ colmax) {
+  const OzChunk c = ch[blockIdx.x];
+  const OzIn q = in[c.prob];
+  const int64_t col = (int64_t)c.r0 + threadIdx.x;
+  if (col >= q.n) return;
+  const int64_t r1 = (c.k0 + kColStrip) < q.k ? (c.k0 + kColStrip) : q.k;
+  unsigned long long mx = 0;
+  for (int64_t i = c.k0; i < r1; ++i) {
+    const unsigned long long v = (unsigned long long)__double_as_longlong(q.B[i * q.ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = v > mx ? v : mx;
+  }
+  atomicMax(&colmax[q.coloff + col], mx);
+}
+
+// A slices of every problem: a block takes 8 rows of one problem, a thread 8
+// consecutive k of one row (zero beyond k, up to the problem's kpad).
+template <int b>
+__global__ void __launch_bounds__(256)
+    g_slice_rows(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ ea, int S,
+                 int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
+  const OzChunk c = ch[blockIdx.x];
+  const OzIn q = in[c.prob];
+  const int64_t groups = q.kpad / 8;
+  const unsigned __int128 C = digit_offset(S, b);
+  for (int64_t w = threadIdx.x; w < 8 * groups; w += blockDim.x) {
+    const int64_t row = (int64_t)c.r0 + w / groups, j0 = (w % groups) * 8;
+    if (row >= q.m) break;  // w only grows: every later item is beyond m too
+    const int e = ea[q.rowoff + row];
+    const double* src = q.A + row * q.lda + j0;
+    unsigned __int128 Z[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) Z[t] = (unsigned __int128)fixed126(j0 + t < q.k ? src[t] : 0.0, e) + C;
+    uint16_t* o = out + (q.rowoff + row) * pitch + j0;
+#pragma unroll
+    for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+      if (t < S) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int hh = 0; hh < 4; ++hh)
+          pk[hh] = bf16_of_int(digit_at<b>(Z[2 * hh], t)) | (bf16_of_int(digit_at<b>(Z[2 * hh + 1], t)) << 16);
+        *reinterpret_cast<uint4*>(o + (int64_t)t * plane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+  }
+}
+
+// B^T slices of every problem: slice_cols' 64 k x 32 n transposing tile.
+template <int b>
+__global__ void __launch_bounds__(256)
+    g_slice_cols(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ eb, int S,
+                 int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
+  extern __shared__ uint32_t tile[];  // [S][32][33]
+  const OzChunk c = ch[blockIdx.x];
+  const OzIn q = in[c.prob];
+  const int64_t k0 = c.k0, n0 = c.r0;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const unsigned __int128 C = digit_offset(S, b);
+  {
+    const int64_t nn = n0 + tx;
+    const int e = nn < q.n ? eb[q.coloff + nn] : 0;
+#pragma unroll
+    for (int r = 0; r < kSliceColK / 16; ++r) {
+      const int w = ty + 8 * r;
+      const int64_t kk = k0 + 2 * w;
+      const unsigned __int128 Z0 =
+          (unsigned __int128)(kk < q.k && nn < q.n ? fixed126(q.B[kk * q.ldb + nn], e) : (__int128)0) + C;
+      const unsigned __int128 Z1 =
+          (unsigned __int128)(kk + 1 < q.k && nn < q.n ? fixed126(q.B[(kk + 1) * q.ldb + nn], e) : (__int128)0) + C;
+#pragma unroll
+      for (int t = 0; t < OZ_MAX_SLICES; ++t)
+        if (t < S)
+          tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+              bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
+    }
+  }
+  __syncthreads();
+  const int r = threadIdx.x >> 3, cc = threadIdx.x & 7;
+  const int64_t nn = n0 + r, kk = k0 + cc * 8;
+  if (nn < q.n && kk < q.kpad) {
+    for (int t = 0; t < S; ++t) {
+      const uint32_t* src = tile + (t * kSliceColN + r) * kSliceColPitch + cc * 4;
+      *reinterpret_cast<uint4*>(out + (int64_t)t * plane + (q.coloff + nn) * pitch + kk) =
+          make_uint4(src[0], src[1], src[2], src[3]);
+    }
+  }
 }
 
 }  // namespace
@@ -1196,4 +1425,290 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
                                       : std::ldexp(2.0, -b * S);
   }
   return ozaki_run(h, a, bT, m, n, k, kpad, b, S, kchunks, C, ldc, accumulate);
+}
+
+// ---------------------------------------------------------------------------
+// Grouped launch: host side
+// ---------------------------------------------------------------------------
+struct nrs_ozaki_group {
+  int S = 0, b = 0;
+  int64_t pitch = 0, rows_a = 0, rows_b = 0, n_tiles = 0;
+  int64_t n_rowch = 0, n_colch = 0, n_slcol = 0;
+  void* arena = nullptr;
+  OzIn* d_in = nullptr;
+  OzChunk *d_rowch = nullptr, *d_colch = nullptr, *d_slcol = nullptr;
+  OzProb* d_probs = nullptr;
+  OzTile* d_tiles = nullptr;
+  int *d_ea = nullptr, *d_eb = nullptr;
+  unsigned long long* d_colmax = nullptr;
+  uint16_t *d_sa = nullptr, *d_sb = nullptr;
+  __int128* d_acc = nullptr;
+};
+
+void nrs_ozaki_group_free(nrs_ozaki_group* g) {
+  if (!g) return;
+  cudaFree(g->arena);
+  delete g;
+}
+
+int nrs_ozaki_group_info(const nrs_ozaki_group* g, int* slices, int* bits, int64_t* tiles) {
+  if (!g) return NRS_ERR_INVALID;
+  if (slices) *slices = g->S;
+  if (bits) *bits = g->b;
+  if (tiles) *tiles = g->n_tiles;
+  return NRS_OK;
+}
+
+// Slice count for `slices` = 0: each problem's spread measured now (one
+// read-back each); the group takes the largest count. Problems whose spread
+// no count covers, or with Inf / NaN, are left out (they stay on the FP64
+// DMMA tiles). digit_bits 0 = the widest width the group's K allows.
+int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, int slices, int digit_bits,
+                          int* accepted, nrs_ozaki_group** out) {
+  *out = nullptr;
+  if (slices < 0 || slices > OZ_MAX_SLICES) return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
+  if (digit_bits != 0 && (digit_bits < 6 || digit_bits > 8))
+    return nrs_fail(h, NRS_ERR_INVALID, "digit bits must be 0 (widest) or 6..8");
+  std::vector<int64_t> idx;
+  int64_t kp_max = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    accepted[i] = 0;
+    const nrs_gemm_desc& g = d[i];
+    if (g.dtype != NRS_F64 || (g.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B)) || g.m <= 0 || g.n <= 0 || g.k <= 0)
+      continue;
+    idx.push_back(i);
+    kp_max = std::max(kp_max, (g.k + OZ_BK - 1) / OZ_BK * OZ_BK);
+  }
+  if (idx.empty()) return NRS_OK;
+  double bits_max = kTargetBits;
+  std::vector<int64_t> keep;
+  for (int64_t i : idx) {
+    const nrs_gemm_desc& g = d[i];
+    if (slices > 0) {
+      keep.push_back(i);
+      continue;
+    }
+    const int64_t kpad8 = (g.k + 7) / 8 * 8;
+    SpreadResult r{};
+    const OzOperand a{(const double*)g.A, g.lda, g.m, true}, bT{(const double*)g.B, g.ldb, g.n, false};
+    int st = spread_estimate(h, a, bT, g.m, g.n, g.k, kpad8, 1, &r);
+    if (st) return st;
+    if (r.flags & 1u) continue;
+    double need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+    int bb, SS, kc;
+    if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc))) {
+      if ((st = spread_estimate(h, a, bT, g.m, g.n, g.k, kpad8, 2, &r))) return st;
+      need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+      if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc))) continue;
+    }
+    bits_max = std::max(bits_max, need);
+    keep.push_back(i);
+  }
+  if (keep.empty()) return NRS_OK;
+  int b = 0, S = 0, kc_max = 0;
+  if (digit_bits) {
+    // a given width: S from the bits (or as given), if the width's limits hold
+    const int s_c = slices > 0 ? slices : std::max(1, (int)std::ceil(bits_max / digit_bits - 1e-9));
+    const int kc = (int)((kp_max + kChunkOf(digit_bits) - 1) / kChunkOf(digit_bits));
+    if (s_c <= OZ_MAX_SLICES && (int64_t)kc * s_c < 128 && digit_bits * s_c <= 126) {
+      b = digit_bits;
+      S = s_c;
+    } else {
+      return NRS_OK;  // this width cannot carry the bits: all stay on DMMA
+    }
+  } else if (slices > 0) {
+    for (int cand = 8; cand >= 6 && !b; --cand) {
+      const int kc = (int)((kp_max + kChunkOf(cand) - 1) / kChunkOf(cand));
+      if ((int64_t)kc * slices < 128 && cand * slices <= 126) {
+        b = cand;
+        S = slices;
+        kc_max = kc;
+      }
+    }
+    if (!b) return nrs_fail(h, NRS_ERR_TOO_LARGE, "k too large for this slice count");
+  } else if (!choose_digits(kp_max, bits_max, &b, &S, &kc_max)) {
+    return NRS_OK;  // nothing qualifies together: all stay on DMMA
+  }
+  (void)kc_max;
+  // Layout: offsets, chunk tables, tiles (most work first: the persistent
+  // kernel hands tiles out round-robin).
+  std::vector<OzIn> ins;
+  std::vector<OzProb> probs;
+  std::vector<OzChunk> rowch, colch, slcol;
+  struct TileW {
+    double w;
+    OzTile t;
+  };
+  std::vector<TileW> tiles;
+  int64_t rowoff = 0, coloff = 0, accoff = 0;
+  for (int64_t i : keep) {
+    const nrs_gemm_desc& g = d[i];
+    const int64_t kpad = (g.k + OZ_BK - 1) / OZ_BK * OZ_BK;
+    const int p = (int)ins.size();
+    ins.push_back(OzIn{(const double*)g.A, g.lda, (const double*)g.B, g.ldb, g.m, g.n, g.k, kpad, rowoff, coloff});
+    const int kc = (int)((kpad + kChunkOf(b) - 1) / kChunkOf(b));
+    probs.push_back(OzProb{g.m, g.n, kpad, rowoff, coloff, accoff, (double*)g.C, g.ldc, kc,
+                           S * (S + 1) / 2 * kc, (g.flags & NRS_GEMM_ACCUMULATE) ? 1 : 0, 0});
+    for (int64_t r = 0; r < g.m; r += 8) rowch.push_back(OzChunk{p, (int32_t)r, 0, 0});
+    for (int64_t c0 = 0; c0 < g.n; c0 += 256)
+      for (int64_t k0 = 0; k0 < g.k; k0 += kColStrip) colch.push_back(OzChunk{p, (int32_t)c0, (int32_t)k0, 0});
+    for (int64_t c0 = 0; c0 < g.n; c0 += kSliceColN)
+      for (int64_t k0 = 0; k0 < kpad; k0 += kSliceColK) slcol.push_back(OzChunk{p, (int32_t)c0, (int32_t)k0, 0});
+    const int tm_n = (int)((g.m + OZ_BM - 1) / OZ_BM), tn_n = (int)((g.n + OZ_BN - 1) / OZ_BN);
+    for (int a = 0; a < tm_n; ++a)
+      for (int c = 0; c < tn_n; ++c) tiles.push_back({(double)kpad * (S * (S + 1) / 2), OzTile{p, a, c, 0}});
+    rowoff += g.m;
+    coloff += g.n;
+    accoff += g.m * g.n;
+  }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const TileW& x, const TileW& y) { return x.w > y.w; });
+  std::vector<OzTile> tl(tiles.size());
+  for (size_t i = 0; i < tiles.size(); ++i) tl[i] = tiles[i].t;
+  if (rowoff > (1LL << 31) || coloff > (1LL << 31) || (int64_t)tl.size() > (1LL << 30))
+    return NRS_OK;  // beyond the tensor maps' coordinate range: stay on DMMA
+  auto al = [](size_t v) { return (v + 255) & ~size_t(255); };
+  const size_t b_in = al(ins.size() * sizeof(OzIn)), b_rc = al(rowch.size() * sizeof(OzChunk)),
+               b_cc = al(colch.size() * sizeof(OzChunk)), b_sc = al(slcol.size() * sizeof(OzChunk)),
+               b_pr = al(probs.size() * sizeof(OzProb)), b_tl = al(tl.size() * sizeof(OzTile)),
+               b_ea = al((size_t)rowoff * 4), b_eb = al((size_t)coloff * 4), b_cm = al((size_t)coloff * 8),
+               b_sa = al((size_t)S * rowoff * kp_max * 2), b_sb = al((size_t)S * coloff * kp_max * 2),
+               b_acc = al((size_t)accoff * 16);
+  const size_t total = b_in + b_rc + b_cc + b_sc + b_pr + b_tl + b_ea + b_eb + b_cm + b_sa + b_sb + b_acc;
+  nrs_ozaki_group* G = new nrs_ozaki_group();
+  if (cudaMalloc(&G->arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    delete G;
+    return nrs_fail(h, NRS_ERR_ALLOC, "grouped Ozaki buffers");
+  }
+  uint8_t* q = (uint8_t*)G->arena;
+  auto take = [&](size_t bytes) {
+    uint8_t* p = q;
+    q += bytes;
+    return p;
+  };
+  G->d_in = (OzIn*)take(b_in);
+  G->d_rowch = (OzChunk*)take(b_rc);
+  G->d_colch = (OzChunk*)take(b_cc);
+  G->d_slcol = (OzChunk*)take(b_sc);
+  G->d_probs = (OzProb*)take(b_pr);
+  G->d_tiles = (OzTile*)take(b_tl);
+  G->d_ea = (int*)take(b_ea);
+  G->d_eb = (int*)take(b_eb);
+  G->d_colmax = (unsigned long long*)take(b_cm);
+  G->d_sa = (uint16_t*)take(b_sa);
+  G->d_sb = (uint16_t*)take(b_sb);
+  G->d_acc = (__int128*)take(b_acc);
+  G->S = S;
+  G->b = b;
+  G->pitch = kp_max;
+  G->rows_a = rowoff;
+  G->rows_b = coloff;
+  G->n_tiles = (int64_t)tl.size();
+  G->n_rowch = (int64_t)rowch.size();
+  G->n_colch = (int64_t)colch.size();
+  G->n_slcol = (int64_t)slcol.size();
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (!e && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  up(G->d_in, ins.data(), ins.size() * sizeof(OzIn));
+  up(G->d_rowch, rowch.data(), rowch.size() * sizeof(OzChunk));
+  up(G->d_colch, colch.data(), colch.size() * sizeof(OzChunk));
+  up(G->d_slcol, slcol.data(), slcol.size() * sizeof(OzChunk));
+  up(G->d_probs, probs.data(), probs.size() * sizeof(OzProb));
+  up(G->d_tiles, tl.data(), tl.size() * sizeof(OzTile));
+  if (e) {
+    nrs_ozaki_group_free(G);
+    return nrs_cuda_check(h, e, "cudaMemcpy(grouped Ozaki tables)");
+  }
+  for (int64_t i : keep) accepted[i] = 1;
+  *out = G;
+  return NRS_OK;
+}
+
+template <int b>
+int group_slices(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
+  const int64_t plane_a = G->rows_a * G->pitch, plane_b = G->rows_b * G->pitch;
+  g_slice_rows<b><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea, G->S, G->pitch, plane_a, G->d_sa);
+  const int smem = (int)((size_t)G->S * kSliceColN * kSliceColPitch * 4);
+  int st = nrs_cuda_check(h, cudaFuncSetAttribute(g_slice_cols<b>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                          "cudaFuncSetAttribute(g_slice_cols)");
+  if (st) return st;
+  g_slice_cols<b><<<(unsigned)G->n_slcol, 256, smem, s>>>(G->d_in, G->d_slcol, G->d_eb, G->S, G->pitch, plane_b,
+                                                         G->d_sb);
+  return nrs_after_launch(h, "grouped ozaki slicing");
+}
+
+// Enqueues the whole group on `s` (no host synchronisation).
+int nrs_ozaki_group_launch(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
+  if (!G || G->n_tiles == 0) return NRS_OK;
+  int st = nrs_cuda_check(h, cudaMemsetAsync(G->d_colmax, 0, (size_t)G->rows_b * 8, s), "cudaMemsetAsync");
+  if (st) return st;
+  g_row_exponents<<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea);
+  g_col_max_bits<<<(unsigned)G->n_colch, 256, 0, s>>>(G->d_in, G->d_colch, G->d_colmax);
+  exponents_from_bits<<<(unsigned)((G->rows_b + 255) / 256), 256, 0, s>>>(G->d_colmax, G->rows_b, G->d_eb, nullptr);
+  if ((st = nrs_after_launch(h, "grouped ozaki exponents"))) return st;
+  st = G->b == 8 ? group_slices<8>(h, G, s) : G->b == 7 ? group_slices<7>(h, G, s) : group_slices<6>(h, G, s);
+  if (st) return st;
+  OzParams P{};
+  P.kpad = G->pitch;
+  P.slices = G->S;
+  P.group_m = 1;
+  P.ea = G->d_ea;
+  P.eb = G->d_eb;
+  P.acc = G->d_acc;
+  P.final_shift = 2 - 2 * G->b - G->b * (G->S - 1);
+  P.digit_bits = G->b;
+  P.kchunk = kChunkOf(G->b);
+  P.err = h->dev_error;
+  P.tiles = G->d_tiles;
+  P.probs = G->d_probs;
+  P.n_tiles = (int)G->n_tiles;
+  return launch_tc<false, true>(h, G->d_sa, G->d_sb, G->S, P, G->rows_a, G->rows_b, s);
+}
+
+extern "C" int nrs_gemm_ozaki_grouped(nrs_handle* h, int64_t count, const nrs_gemm_desc* descs, int slices,
+                                      int* on_tensor_cores, nrs_ozaki_info* info) {
+  if (!h || count < 0 || (count && !descs)) return NRS_ERR_INVALID;
+  h->last_error.clear();
+  int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (st) return st;
+  for (int64_t i = 0; i < count; ++i) {
+    const nrs_gemm_desc& g = descs[i];
+    if (g.dtype != NRS_F64) return nrs_fail(h, NRS_ERR_DTYPE, "grouped Ozaki takes f64 GEMMs");
+    if (g.flags & ~(NRS_GEMM_ACCUMULATE | NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B))
+      return nrs_fail(h, NRS_ERR_INVALID, "unknown GEMM flag");
+    const bool ta = g.flags & NRS_GEMM_TRANS_A, tb = g.flags & NRS_GEMM_TRANS_B;
+    if (g.m < 0 || g.k < 0 || g.n < 0) return nrs_fail(h, NRS_ERR_SHAPE, "negative GEMM dimension");
+    if (g.ldc < (g.n > 0 ? g.n : 1) || g.lda < ((ta ? g.m : g.k) > 0 ? (ta ? g.m : g.k) : 1) ||
+        g.ldb < ((tb ? g.k : g.n) > 0 ? (tb ? g.k : g.n) : 1))
+      return nrs_fail(h, NRS_ERR_SHAPE, "leading dimension too small");
+    if (g.m * g.n > 0 && (!g.C || (g.k > 0 && (!g.A || !g.B)))) return nrs_fail(h, NRS_ERR_INVALID, "null operand");
+  }
+  std::vector<int> acc((size_t)count);
+  nrs_ozaki_group* G = nullptr;
+  if ((st = nrs_ozaki_group_build(h, count, descs, slices, 0, acc.data(), &G))) return st;
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    if (G) {
+      info->slices = G->S;
+      info->slice_bits = G->b;
+      info->k_chunk = kChunkOf(G->b);
+      info->products = (int32_t)G->n_tiles;
+    }
+  }
+  // the problems the group does not take run one by one on DMMA
+  for (int64_t i = 0; i < count && st == NRS_OK; ++i) {
+    if (on_tensor_cores) on_tensor_cores[i] = acc[i];
+    if (!acc[i]) {
+      const nrs_gemm_desc& g = descs[i];
+      st = nrs_gemm(h, NRS_F64, g.m, g.k, g.n, g.A, g.lda, g.B, g.ldb, g.C, g.ldc, g.flags, NRS_GEMM_DMMA);
+    }
+  }
+  if (st == NRS_OK && G) st = nrs_ozaki_group_launch(h, G, h->stream);
+  if (G) {
+    cudaStreamSynchronize(h->stream);  // the group's buffers are freed below
+    nrs_ozaki_group_free(G);
+  }
+  return st;
 }

@@ -1060,11 +1060,13 @@ int launch_lane_tma(nrs_handle* h, const LaneProblem& p) {
   if (RUNNING && rows && es == 4 && ((uintptr_t)p.x & 15) == 0 && ((uintptr_t)p.out & 15) == 0 &&
       (lstride * es) % 16 == 0 && (bstride * es) % 16 == 0 && (p.alen * es) % 16 == 0) {
     auto kern = lane_running_rows<T, OP>;
+    // The attribute belongs to the current device's context: set it on every
+    // call (cheap), not once per process.
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem(kRowLanes));
     // CTAs resident per SM for each row count (depends only on the kernel).
     static int per_sm[kRowLanes + 1];
     static std::once_flag once;
     std::call_once(once, [&] {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem(kRowLanes));
       for (int r = kRowLanes / 2; r <= kRowLanes; ++r)
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[r], kern, kRowLanes + 32, row_smem(r)) !=
             cudaSuccess)

@@ -327,6 +327,14 @@ extern "C" int nrs_selector_destroy(nrs_selector* s) {
 
 extern "C" int64_t nrs_selector_num_params(nrs_selector* s) { return s ? s->n_params : -1; }
 
+int nrs_selector_shape(nrs_selector* s, int* F, int* H, int* V) {
+  if (!s) return NRS_ERR_INVALID;
+  *F = s->F;
+  *H = s->H;
+  *V = s->V;
+  return NRS_OK;
+}
+
 extern "C" int nrs_selector_get_params(nrs_handle* h, nrs_selector* s, float* host) {
   if (!h || !s || !host) return NRS_ERR_INVALID;
   int st = nrs_cuda_check(h, cudaStreamSynchronize(h->stream), "sync");

@@ -647,32 +647,15 @@ class Plan:
     B may be transposed views); reds: list of (x, op, out) with x a
     contiguous 1-D tensor and out a 1-element tensor."""
 
-    def __init__(self, gemms=(), reds=()):
+    def __init__(self, gemms=(), reds=(), f64_mode: int = L.PLAN_F64_DMMA, f64_slices: int = 0,
+                 f64_digit_bits: int = 0):
         lib = L.load()
         self.h = handle()
-        self._keep = []
-        gd = (L.GemmDesc * _bi.max(1, len(gemms)))()
-        for i, (a, b, c, acc) in enumerate(gemms):
-            _need_cuda(a, b, c)
-            sa, sb = _mat_strides(a), _mat_strides(b)
-            if sa is None or sb is None or c.stride(1) != 1:
-                raise L.NumRs2Error(L.ERR_STRIDE, "grouped GEMM operands must be row- or column-contiguous")
-            flags = (L.GEMM_ACCUMULATE if acc else 0) | (L.GEMM_TRANS_A if sa[1] else 0) | (
-                L.GEMM_TRANS_B if sb[1] else 0)
-            m, k = a.shape
-            n = b.shape[1]
-            gd[i] = L.GemmDesc(dtype_code(c), flags, m, k, n, a.data_ptr(), sa[0], b.data_ptr(), sb[0],
-                               c.data_ptr(), c.stride(0) if m > 1 else _bi.max(n, 1))
-            self._keep += [a, b, c]
-        rd = (L.RowReduceDesc * _bi.max(1, len(reds)))()
-        for i, (x, op, out) in enumerate(reds):
-            _need_cuda(x, out)
-            if not x.is_contiguous():
-                raise L.NumRs2Error(L.ERR_STRIDE, "row reductions need contiguous rows")
-            rd[i] = L.RowReduceDesc(dtype_code(x), op, x.numel(), x.data_ptr(), out.data_ptr())
-            self._keep += [x, out]
+        gd, rd, self._keep = _group_descs(gemms, reds)
         self.p = C.c_void_p()
-        L.check(lib.nrs_plan_create(self.h, len(gemms), gd, len(reds), rd, C.byref(self.p)), self.h)
+        opt = L.PlanOptions(f64_mode, f64_slices, f64_digit_bits)
+        L.check(lib.nrs_plan_create_ex(self.h, len(gemms), gd, len(reds), rd, C.byref(opt), C.byref(self.p)),
+                self.h)
 
     def run(self, use_graph: bool = True) -> None:
         h = handle()
@@ -682,6 +665,12 @@ class Plan:
         wi, gt = C.c_int64(), C.c_int64()
         L.check(L.load().nrs_plan_stats(self.p, C.byref(wi), C.byref(gt)))
         return {"work_items": wi.value, "gemm_tiles": gt.value}
+
+    def f64_info(self):
+        """(f64 GEMMs on the tensor cores, slice count, digit bits)."""
+        n, sl, b = C.c_int64(), C.c_int(), C.c_int()
+        L.check(L.load().nrs_plan_f64_info(self.p, C.byref(n), C.byref(sl), C.byref(b)))
+        return n.value, sl.value, b.value
 
     def close(self) -> None:
         if self.p:
@@ -693,6 +682,64 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def _group_descs(gemms, reds):
+    """Descriptor arrays of a group (and the tensors they point into)."""
+    keep = []
+    gd = (L.GemmDesc * _bi.max(1, len(gemms)))()
+    for i, (a, b, c, acc) in enumerate(gemms):
+        _need_cuda(a, b, c)
+        sa, sb = _mat_strides(a), _mat_strides(b)
+        if sa is None or sb is None or c.stride(1) != 1:
+            raise L.NumRs2Error(L.ERR_STRIDE, "grouped GEMM operands must be row- or column-contiguous")
+        flags = (L.GEMM_ACCUMULATE if acc else 0) | (L.GEMM_TRANS_A if sa[1] else 0) | (
+            L.GEMM_TRANS_B if sb[1] else 0)
+        m, k = a.shape
+        n = b.shape[1]
+        gd[i] = L.GemmDesc(dtype_code(c), flags, m, k, n, a.data_ptr(), sa[0], b.data_ptr(), sb[0],
+                           c.data_ptr(), c.stride(0) if m > 1 else _bi.max(n, 1))
+        keep += [a, b, c]
+    rd = (L.RowReduceDesc * _bi.max(1, len(reds)))()
+    for i, (x, op, out) in enumerate(reds):
+        _need_cuda(x, out)
+        if not x.is_contiguous():
+            raise L.NumRs2Error(L.ERR_STRIDE, "row reductions need contiguous rows")
+        rd[i] = L.RowReduceDesc(dtype_code(x), op, x.numel(), x.data_ptr(), out.data_ptr())
+        keep += [x, out]
+    return gd, rd, keep
+
+
+def autotune_plan(gemms=(), reds=(), max_trials: int = 48, reps: int = 3, f64_ozaki: bool = False) -> dict:
+    """nrs_plan_autotune: tile variants (and, with f64_ozaki, the tensor-core
+    f64 mode and its digit width) chosen by timing the whole group; fills the
+    tuner table that the next Plan uses and returns the Plan keyword
+    arguments in "plan_kwargs". Outputs' contents are undefined afterwards."""
+    lib = L.load()
+    h = handle()
+    gd, rd, keep = _group_descs(gemms, reds)
+    rep = L.AutotuneReport()
+    opt = L.PlanOptions(L.PLAN_F64_OZAKI if f64_ozaki else L.PLAN_F64_DMMA, 0, 0)
+    L.check(lib.nrs_plan_autotune(h, len(gemms), gd, len(reds), rd, C.byref(opt), max_trials, reps,
+                                  C.byref(rep)), h)
+    del keep
+    o = rep.options
+    return {"untuned_ms": rep.untuned_ms, "isolated_ms": rep.isolated_ms, "final_ms": rep.final_ms,
+            "ozaki_ms": rep.ozaki_ms, "buckets": rep.buckets, "trials": rep.trials,
+            "plan_kwargs": {"f64_mode": o.f64_mode, "f64_slices": o.f64_slices, "f64_digit_bits": o.f64_digit_bits}}
+
+
+def gemm_ozaki_grouped(problems, slices: int = 0):
+    """nrs_gemm_ozaki_grouped over (A, B, C, accumulate) f64 problems; returns
+    (list of on-tensor-cores flags, info dict)."""
+    lib = L.load()
+    h = handle()
+    gd, _, keep = _group_descs(problems, ())
+    flags = (C.c_int * _bi.max(1, len(problems)))()
+    info = L.OzakiInfo()
+    L.check(lib.nrs_gemm_ozaki_grouped(h, len(problems), gd, slices, flags, C.byref(info)), h)
+    del keep
+    return [bool(flags[i]) for i in range(len(problems))], {"slices": info.slices, "slice_bits": info.slice_bits}
 
 
 def tile_variants():
@@ -721,6 +768,16 @@ def tuner_set(dtype, m, k, n, variant):
 
 def tuner_get(dtype, m, k, n) -> int:
     return L.load().nrs_tuner_get(handle(), dtype, m, k, n)
+
+
+def tuner_save(path: str) -> None:
+    h = handle()
+    L.check(L.load().nrs_tuner_save(h, path.encode()), h)
+
+
+def tuner_load(path: str) -> None:
+    h = handle()
+    L.check(L.load().nrs_tuner_load(h, path.encode()), h)
 
 
 def tuner_clear():
@@ -773,6 +830,12 @@ class Selector:
         y = torch.empty((x.shape[0], self.V), device=x.device)
         L.check(self.lib.nrs_selector_predict(handle(), self.s, x.shape[0], _ptr(x), _ptr(y)), self.h)
         return y
+
+    def save(self, path: str) -> None:
+        L.check(self.lib.nrs_selector_save(handle(), self.s, path.encode()), self.h)
+
+    def load(self, path: str) -> None:
+        L.check(self.lib.nrs_selector_load(handle(), self.s, path.encode()), self.h)
 
     def install(self, on: bool = True) -> None:
         L.check(self.lib.nrs_tuner_set_selector(handle(), self.s if on else None), self.h)

@@ -35,6 +35,15 @@ CASES = {
     "cumsum_flat_f32": ("f32", "add", None),
     "expr_abc_f32": ("f32", None, None),
     "add_row_f32": ("f32", None, None),
+    "dmma_splitk_f64": ("f64", None, None),
+    "simt_f32": ("f32", None, None),
+    "argmax_rows_f32": ("f32", L.ARGMAX, 1),
+    "argmax_cols_f32": ("f32", L.ARGMAX, 0),
+    "maximum_reduce_cols_f32": ("f32", "maximum", 0),
+    "maximum_reduce_rows_f32": ("f32", "maximum", 1),
+    "add_decode_f32": ("f32", None, None),
+    "selector_train": (None, None, None),
+    "grouped_ozaki": (None, None, None),
 }
 
 
@@ -86,6 +95,43 @@ def main():
             fn = lambda: K.gemm_ozaki(A, B, slices=a.slices, out=C)  # noqa: E731
         else:
             fn = lambda: K.gemm_2d(n, n, n, A, B, C, variant=L.GEMM_DMMA)  # noqa: E731
+    elif a.case == "dmma_splitk_f64":
+        # 512^3: 32x32 tiles in 4 k chunks, then splitk_finish adds the slabs
+        n = 512
+        A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        B, C = torch.empty_like(A), torch.empty_like(A)
+        K.fill_random(A, L.RNG_UNIFORM, 1, -1.0, 1.0)
+        K.fill_random(B, L.RNG_UNIFORM, 2, -1.0, 1.0)
+        fn = lambda: K.gemm_2d(n, n, n, A, B, C, variant=L.GEMM_DMMA)  # noqa: E731
+    elif a.case == "simt_f32":
+        A = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        B, C = torch.empty_like(A), torch.empty_like(A)
+        K.fill_random(A, L.RNG_UNIFORM, 1, -1.0, 1.0)
+        K.fill_random(B, L.RNG_UNIFORM, 2, -1.0, 1.0)
+        fn = lambda: K.gemm_2d(n, n, n, A, B, C, variant=L.GEMM_SIMT)  # noqa: E731
+    elif a.case.startswith("argmax") or a.case.startswith("maximum_reduce"):
+        x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        if a.case.startswith("argmax"):
+            fn = lambda: K.reduce(x, op, axis)  # noqa: E731
+        else:
+            fn = lambda: K.ufunc_reduce(op, x, axis)  # noqa: E731
+    elif a.case == "add_decode_f32":
+        # (n, 128, n/128) views with a strided short last axis: every element
+        # index is decoded (ufunc_decode)
+        x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
+        v = x.view(n, n // 128, 128).transpose(1, 2)
+        fn = lambda: K.add(v, v)  # noqa: E731
+    elif a.case == "selector_train":
+        # the learned selector's training loop: mlp_forward, mlp_backward,
+        # mlp_grad and adam_step per minibatch (20000 samples, batch 256)
+        g = torch.Generator(device="cuda").manual_seed(1)
+        xs = torch.rand((20000, 7), device="cuda", generator=g)
+        ts = torch.randn((20000, L.TILE_VARIANTS), device="cuda", generator=g)
+        ms = torch.ones_like(ts)
+        sel = K.Selector()
+        fn = lambda: sel.train(xs, ts, ms, epochs=1)  # noqa: E731
     else:
         import numpy as np
         r = np.random.default_rng(7)
@@ -97,7 +143,11 @@ def main():
             gemms.append((torch.randn(int(M[i]), int(Kd[i]), dtype=t, device="cuda"),
                           torch.randn(int(Kd[i]), int(N[i]), dtype=t, device="cuda"),
                           torch.empty(int(M[i]), int(N[i]), dtype=t, device="cuda"), False))
-        plan = K.Plan(gemms)
+        if a.case == "grouped_ozaki":
+            # the same mix with its f64 GEMMs on the tensor cores
+            plan = K.Plan(gemms, f64_mode=L.PLAN_F64_OZAKI)
+        else:
+            plan = K.Plan(gemms)
         fn = lambda: plan.run(use_graph=False)  # noqa: E731
     fn()
     torch.cuda.synchronize()

@@ -198,3 +198,100 @@ def test_ozaki_transposed_views_and_accumulate(K, ora):
     assert C is C0
     want = 1.0 + to_np(K.gemm_ozaki(A, B)[0])
     np.testing.assert_array_equal(to_np(C0), want)
+
+
+# ---------------------------------------------------------------------------
+# Grouped tensor-core f64 GEMMs (nrs_gemm_ozaki_grouped, plan f64 mode OZAKI)
+# ---------------------------------------------------------------------------
+def _group_problems(seed, count, hi=512):
+    r = np.random.default_rng(seed)
+    lu = lambda lo, hi_, n: np.exp(r.uniform(np.log(lo), np.log(hi_), n)).astype(np.int64)  # noqa: E731
+    M, N, Kk = lu(1, hi, count), lu(1, hi, count), lu(1, hi, count)
+    probs = []
+    for i in range(count):
+        a = torch.from_numpy(r.uniform(-1, 1, (M[i], Kk[i]))).cuda()
+        b = torch.from_numpy(r.uniform(-1, 1, (Kk[i], N[i])) * np.exp(r.normal(0, 1, (Kk[i], N[i])))).cuda()
+        c = torch.full((M[i], N[i]), float("nan"), dtype=torch.float64, device="cuda")
+        probs.append((a, b, c, False))
+    return probs
+
+
+def _check_against_dd(ora, K, probs, bar=1e-14):
+    for a, b, c, _ in probs:
+        Cdd, ab = ora.gemm_dd(to_np(a), to_np(b))
+        e = _err(to_np(c), Cdd, ab)
+        ed = _err(to_np(K.matmul(a, b, variant=L.GEMM_DMMA)), Cdd, ab)
+        assert e <= bar and e <= max(ed, 1e-15), (a.shape, b.shape, e, ed)
+
+
+def test_ozaki_grouped_against_double_double(K, ora):
+    probs = _group_problems(41, 60)
+    # a transposed A, a long K and a NaN: the first and last go to DMMA
+    at = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, (70, 50))).cuda()
+    probs.append((at.t(), torch.rand((70, 33), dtype=torch.float64, device="cuda"),
+                  torch.empty((50, 33), dtype=torch.float64, device="cuda"), False))
+    probs.append((torch.rand((40, 3000), dtype=torch.float64, device="cuda") - 0.5,
+                  torch.rand((3000, 90), dtype=torch.float64, device="cuda") - 0.5,
+                  torch.empty((40, 90), dtype=torch.float64, device="cuda"), False))
+    bad = torch.rand((16, 16), dtype=torch.float64, device="cuda")
+    bad[3, 4] = float("nan")
+    probs.append((bad, bad.clone(), torch.empty((16, 16), dtype=torch.float64, device="cuda"), False))
+    on_tc, info = K.gemm_ozaki_grouped(probs)
+    assert info["slices"] >= 7 and all(on_tc[:60]) and on_tc[61] and not on_tc[60] and not on_tc[62]
+    _check_against_dd(ora, K, probs[:62])
+    d = K.matmul(bad, bad.clone(), variant=L.GEMM_DMMA)
+    assert torch.equal(torch.isnan(probs[62][2]), torch.isnan(d))
+
+
+def test_plan_f64_on_tensor_cores_replays_and_accumulates(K, ora):
+    probs = _group_problems(43, 40, hi=300)
+    x = [torch.randn(int(n), device="cuda") for n in (100, 5000, 70000)]
+    reds = [(v, L.SUM, torch.empty(1, device="cuda")) for v in x]
+    f32 = [(torch.rand((50, 60), device="cuda"), torch.rand((60, 70), device="cuda"),
+            torch.empty((50, 70), device="cuda"), False)]
+    plan = K.Plan(probs + f32, reds, f64_mode=L.PLAN_F64_OZAKI)
+    n_tc, S, bits = plan.f64_info()
+    assert n_tc == 40 and S >= 7 and bits in (6, 7, 8)
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    _check_against_dd(ora, K, probs)
+    for v, _, o in reds:
+        assert torch.equal(o.reshape(()), K.sum(v).reshape(()))
+    # new values of the same range: the replayed graph picks them up
+    for a, b, c, _ in probs:
+        a.mul_(-0.5)
+        c.fill_(float("nan"))
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    _check_against_dd(ora, K, probs)
+    plan.close()
+    # C += A B through the grouped path
+    accp = [(a, b, torch.ones_like(c), True) for a, b, c, _ in probs[:8]]
+    plan = K.Plan(accp, f64_mode=L.PLAN_F64_OZAKI, f64_slices=8)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    for a, b, c, _ in accp:
+        Cdd, ab = ora.gemm_dd(to_np(a), to_np(b))
+        assert np.max(np.abs(to_np(c) - (Cdd + 1.0)) / (ab + 1.0)) <= 1e-14
+    plan.close()
+
+
+def test_autotune_considers_tensor_core_f64(K, ora):
+    probs = _group_problems(47, 80)
+    f32 = []
+    for i in range(40):
+        m, k, n = 32 + i, 64, 48 + i
+        f32.append((torch.rand((m, k), device="cuda"), torch.rand((k, n), device="cuda"),
+                    torch.empty((m, n), device="cuda"), False))
+    K.tuner_clear()
+    rep = K.autotune_plan(probs + f32, (), max_trials=8, reps=3, f64_ozaki=True)
+    assert rep["final_ms"] <= rep["untuned_ms"]
+    assert rep["ozaki_ms"] > 0
+    for a, b, c, _ in probs:
+        c.fill_(float("nan"))
+    plan = K.Plan(probs + f32, (), **rep["plan_kwargs"])
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    _check_against_dd(ora, K, probs[:20])
+    plan.close()
+    K.tuner_clear()
