@@ -36,7 +36,9 @@
 //                 finished accumulator to registers, hand it back to the MMA
 //                 warp at once, fold the copy into the int32 diagonal sums
 //                 kept in TMEM columns 256..511, and add each finished
-//                 diagonal into the int128 accumulators in global memory.
+//                 diagonal into the CTA's int128 accumulator slot (global,
+//                 one 128 x 256 slot per CTA, column-major so a warp's 32
+//                 rows are contiguous; all slots together fit in L2).
 // Measured at 8192^3 (clock counters per warp): the MMA warp waits for TMA
 // data ~29% of its time and for the epilogue ~8%.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
@@ -191,7 +193,7 @@ struct OzParams {
   int group_m;     // tile rasterisation group height
   const int* ea;   // row exponents of A
   const int* eb;   // column exponents of B
-  __int128* acc;   // m x n exact accumulators
+  __int128* acc;   // exact accumulators: one 128 x 256 slot per CTA, column-major
   double* C;
   int64_t ldc;
   int final_shift; // 2 - 2b - b(S-1) for b-bit digits
@@ -214,11 +216,10 @@ struct OzParams {
 // One problem of a grouped launch: its slices are rows [rowoff, rowoff + m)
 // of the stacked A slices and [coloff, coloff + n) of the stacked B^T slices
 // (row pitch = the group's largest kpad; this problem's rows are zero from
-// its own k to its kpad), its exponents sit at the same offsets, and its
-// int128 accumulators at accoff (m x n, row-major).
+// its own k to its kpad), and its exponents sit at the same offsets.
 struct OzProb {
   int64_t m, n, kpad;
-  int64_t rowoff, coloff, accoff;
+  int64_t rowoff, coloff;
   double* C;
   int64_t ldc;
   int32_t kchunks, n_pairs;
@@ -236,7 +237,6 @@ struct TileCtx {
   int kblocks, n_pairs, kchunks;
   const int* ea;
   const int* eb;
-  __int128* acc;
   double* C;
   int64_t ldc;
   int accumulate;
@@ -286,7 +286,6 @@ __device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
     c.kchunks = q.kchunks;
     c.ea = P.ea + q.rowoff;
     c.eb = P.eb + q.coloff;
-    c.acc = P.acc + q.accoff;
     c.C = q.C;
     c.ldc = q.ldc;
     c.accumulate = q.accumulate;
@@ -302,7 +301,6 @@ __device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
     c.kchunks = P.kchunks;
     c.ea = P.ea;
     c.eb = P.eb;
-    c.acc = P.acc;
     c.C = P.C;
     c.ldc = P.ldc;
     c.accumulate = P.accumulate;
@@ -587,7 +585,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const bool first = (d == P.slices - 1), last = (d == 0);
         const int shift = P.digit_bits * (P.slices - 1 - d);
         const int ecol_base = (last && row_ok) ? tc.ea[row] + P.final_shift : 0;
-        __int128* accp = tc.acc + (row_ok ? row : 0) * tc.n + col0;
+        // This CTA's accumulator slot, column-major within the tile: for a
+        // fixed column the warp's 32 rows are 512 contiguous bytes.
+        __int128* accp = P.acc + (size_t)blockIdx.x * (OZ_BM * OZ_BN) +
+                         (size_t)(half * (OZ_BN / 2)) * OZ_BM + row_in_tile;
 #pragma unroll 1
         for (int c = 0; c < OZ_BN / 32; ++c) {
           uint32_t w[16];
@@ -599,9 +600,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const int64_t col = col0 + j;
             if (col >= tc.n) continue;
             const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
-            const __int128 sum = first ? contrib : (accp[j] + contrib);
+            __int128* ap = accp + (size_t)j * OZ_BM;
+            const __int128 sum = first ? contrib : (*ap + contrib);
             if (!last) {
-              accp[j] = sum;
+              *ap = sum;
             } else {
               // |sum| < 2^127: keep its top 64 significant bits, convert once.
               const bool neg = sum < 0;
@@ -1176,7 +1178,9 @@ int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m,
   // column maxima of a column-major operand go through the accumulators).
   const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4);
   const size_t sa_b = al((size_t)S * m * kpad * 2), sb_b = al((size_t)S * n * kpad * 2);
-  const size_t acc_b = al(std::max((size_t)m * n * 16, (size_t)std::max(m, n) * 8));
+  // one 128 x 256 int128 accumulator slot per persistent CTA (a tile's
+  // accumulators live only while the CTA works on it; 78 MB for 152 CTAs)
+  const size_t acc_b = al(std::max((size_t)h->hw_sms * OZ_BM * OZ_BN * 16, (size_t)std::max(m, n) * 8));
   int st;
   uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + sa_b + sb_b + acc_b, &st);
   if (!ws) return st;
@@ -1540,14 +1544,14 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
     OzTile t;
   };
   std::vector<TileW> tiles;
-  int64_t rowoff = 0, coloff = 0, accoff = 0;
+  int64_t rowoff = 0, coloff = 0;
   for (int64_t i : keep) {
     const nrs_gemm_desc& g = d[i];
     const int64_t kpad = (g.k + OZ_BK - 1) / OZ_BK * OZ_BK;
     const int p = (int)ins.size();
     ins.push_back(OzIn{(const double*)g.A, g.lda, (const double*)g.B, g.ldb, g.m, g.n, g.k, kpad, rowoff, coloff});
     const int kc = (int)((kpad + kChunkOf(b) - 1) / kChunkOf(b));
-    probs.push_back(OzProb{g.m, g.n, kpad, rowoff, coloff, accoff, (double*)g.C, g.ldc, kc,
+    probs.push_back(OzProb{g.m, g.n, kpad, rowoff, coloff, (double*)g.C, g.ldc, kc,
                            S * (S + 1) / 2 * kc, (g.flags & NRS_GEMM_ACCUMULATE) ? 1 : 0, 0});
     for (int64_t r = 0; r < g.m; r += 8) rowch.push_back(OzChunk{p, (int32_t)r, 0, 0});
     for (int64_t c0 = 0; c0 < g.n; c0 += 256)
@@ -1559,7 +1563,6 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
       for (int c = 0; c < tn_n; ++c) tiles.push_back({(double)kpad * (S * (S + 1) / 2), OzTile{p, a, c, 0}});
     rowoff += g.m;
     coloff += g.n;
-    accoff += g.m * g.n;
   }
   std::stable_sort(tiles.begin(), tiles.end(), [](const TileW& x, const TileW& y) { return x.w > y.w; });
   std::vector<OzTile> tl(tiles.size());
@@ -1572,7 +1575,7 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
                b_pr = al(probs.size() * sizeof(OzProb)), b_tl = al(tl.size() * sizeof(OzTile)),
                b_ea = al((size_t)rowoff * 4), b_eb = al((size_t)coloff * 4), b_cm = al((size_t)coloff * 8),
                b_sa = al((size_t)S * rowoff * kp_max * 2), b_sb = al((size_t)S * coloff * kp_max * 2),
-               b_acc = al((size_t)accoff * 16);
+               b_acc = al((size_t)h->hw_sms * OZ_BM * OZ_BN * 16);  // a slot per CTA (grid <= SMs)
   const size_t total = b_in + b_rc + b_cc + b_sc + b_pr + b_tl + b_ea + b_eb + b_cm + b_sa + b_sb + b_acc;
   nrs_ozaki_group* G = new nrs_ozaki_group();
   if (cudaMalloc(&G->arena, total) != cudaSuccess) {
