@@ -36,9 +36,10 @@
 //                 finished accumulator to registers, hand it back to the MMA
 //                 warp at once, fold the copy into the int32 diagonal sums
 //                 kept in TMEM columns 256..511, and add each finished
-//                 diagonal into the CTA's int128 accumulator slot (global,
-//                 one 128 x 256 slot per CTA, column-major so a warp's 32
-//                 rows are contiguous; all slots together fit in L2).
+//                 diagonal into the int128 accumulators in global memory
+//                 (grouped launches: one column-major 128 x 256 slot per
+//                 CTA, so a warp's 32 rows are contiguous and all slots
+//                 together fit in L2).
 // Measured at 8192^3 (clock counters per warp): the MMA warp waits for TMA
 // data ~29% of its time and for the epilogue ~8%.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
@@ -193,7 +194,7 @@ struct OzParams {
   int group_m;     // tile rasterisation group height
   const int* ea;   // row exponents of A
   const int* eb;   // column exponents of B
-  __int128* acc;   // exact accumulators: one 128 x 256 slot per CTA, column-major
+  __int128* acc;   // exact accumulators: m x n (one problem) or a slot per CTA (grouped)
   double* C;
   int64_t ldc;
   int final_shift; // 2 - 2b - b(S-1) for b-bit digits
@@ -267,6 +268,32 @@ __device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm
   const int r = tile % per_group;
   tm = first_m + r % gm;
   tn = r / gm;
+}
+
+// Units of a tile that the tensor cores accumulate together. With one K
+// chunk (kchunks == 1) consecutive units are consecutive pairs; the pairs of
+// one diagonal can share the fp32 accumulator as long as the sum stays an
+// exact integer: each pair's sum is at most kblocks * 64 * 2^(2b-2), so up
+// to 2^24 / that many pairs. Several K chunks (and the spread estimate)
+// keep one unit per accumulation.
+__device__ __forceinline__ int merge_count(const TileCtx& c, const OzParams& P, bool est) {
+  if (est || c.kchunks != 1) return 1;
+  const int64_t per_pair = (int64_t)c.kblocks * OZ_BK << (2 * P.digit_bits - 2);
+  const int64_t g = ((int64_t)1 << 24) / per_pair;
+  return g < 1 ? 1 : (int)g;
+}
+__device__ __forceinline__ int diag_of(int u, int S, int kchunks) {
+  const PairOf p = pair_of(u, S, kchunks);
+  return p.s + p.t;
+}
+// End of the accumulation group starting at unit u: same diagonal, at most
+// `gm` units.
+__device__ __forceinline__ int group_end(int u, int n_pairs, int gm, int S, int kchunks) {
+  if (gm <= 1) return u + 1;
+  const int d = diag_of(u, S, kchunks);
+  int e = u + 1;
+  while (e < n_pairs && e - u < gm && diag_of(e, S, kchunks) == d) ++e;
+  return e;
 }
 
 template <bool G>
@@ -402,11 +429,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       bool ok = true;
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const TileCtx c = tile_ctx<G>(P, tile);
-        for (int u = 0; u < c.n_pairs && ok; ++u, ++ai) {
-          const PairOf pr = pair_of(u, P.slices, c.kchunks);
-          const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
-          int kb1 = kb0 + P.kchunk / OZ_BK;
-          if (kb1 > c.kblocks) kb1 = c.kblocks;
+        const int gm = merge_count(c, P, EST);
+        for (int u = 0; u < c.n_pairs && ok; ++ai) {
+          const int u_end = group_end(u, c.n_pairs, gm, P.slices, c.kchunks);
           // One accumulator (TMEM columns 0..255); the epilogue frees it as
           // soon as it has folded it into the diagonal sums (columns 256..511).
           const int buf = 0;
@@ -414,22 +439,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
           tc_fence_after();
           const uint32_t d_tmem = tmem_base;
-          for (int kb = kb0; kb < kb1; ++kb, ++it) {
-            const int s = it % OZ_STAGES;
-            const uint32_t ph = (it / OZ_STAGES) & 1;
-            if (!bounded(&full[s], ph, 3)) { ok = false; break; }
-            tc_fence_after();
-            const uint32_t a_addr = smem_u32(smem + s * OZ_STAGE_BYTES);
-            const uint32_t b_addr = a_addr + OZ_A_BYTES;
+          for (int uu = u; uu < u_end && ok; ++uu) {
+            const PairOf pr = pair_of(uu, P.slices, c.kchunks);
+            const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
+            int kb1 = kb0 + P.kchunk / OZ_BK;
+            if (kb1 > c.kblocks) kb1 = c.kblocks;
+            for (int kb = kb0; kb < kb1; ++kb, ++it) {
+              const int s = it % OZ_STAGES;
+              const uint32_t ph = (it / OZ_STAGES) & 1;
+              if (!bounded(&full[s], ph, 3)) { ok = false; break; }
+              tc_fence_after();
+              const uint32_t a_addr = smem_u32(smem + s * OZ_STAGE_BYTES);
+              const uint32_t b_addr = a_addr + OZ_A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < OZ_BK / 16; ++kk) {
-              tc_mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
-                          kIdesc, (kb > kb0 || kk > 0) ? 1u : 0u);
+              for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+                tc_mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
+                            kIdesc, (uu > u || kb > kb0 || kk > 0) ? 1u : 0u);
+              }
+              tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
-            tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
           }
           if (!ok) break;
           tc_commit(&accf[buf]);  // accumulator ready once every MMA above completes
+          u = u_end;
         }
       }
       // Make sure no MMA is still running before TMEM is released.
@@ -540,9 +572,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const bool row_ok = row < tc.m;
       const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
       prev_d = -1;
-      for (int u = 0; u < tc.n_pairs; ++u, ++ai) {
-        const PairOf pr = pair_of(u, P.slices, tc.kchunks);
-        const int d = pr.s + pr.t;
+      const int gm = merge_count(tc, P, false);
+      for (int u = 0, u_end = 0; u < tc.n_pairs; u = u_end, ++ai) {
+        u_end = group_end(u, tc.n_pairs, gm, P.slices, tc.kchunks);
+        const int d = diag_of(u, P.slices, tc.kchunks);
         const bool diag_start = (d != prev_d);
         prev_d = d;
         const uint32_t aph = ai & 1;
@@ -579,16 +612,25 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_before();
         __syncwarp();
         // Is this the last unit of its diagonal?
-        const bool diag_end = (u == tc.n_pairs - 1) || (pair_of(u + 1, P.slices, tc.kchunks).s +
-                                                       pair_of(u + 1, P.slices, tc.kchunks).t) != d;
+        const bool diag_end = (u_end == tc.n_pairs) || diag_of(u_end, P.slices, tc.kchunks) != d;
         if (!diag_end) continue;
         const bool first = (d == P.slices - 1), last = (d == 0);
         const int shift = P.digit_bits * (P.slices - 1 - d);
         const int ecol_base = (last && row_ok) ? tc.ea[row] + P.final_shift : 0;
-        // This CTA's accumulator slot, column-major within the tile: for a
-        // fixed column the warp's 32 rows are 512 contiguous bytes.
-        __int128* accp = P.acc + (size_t)blockIdx.x * (OZ_BM * OZ_BN) +
-                         (size_t)(half * (OZ_BN / 2)) * OZ_BM + row_in_tile;
+        // Grouped launches: this CTA's accumulator slot, column-major within
+        // the tile (for a fixed column the warp's 32 rows are 512 contiguous
+        // bytes; all slots together stay in L2). One large problem: an m x n
+        // row-major array (measured 5% faster at 8192^3 than the slots, whose
+        // 78 MB compete in L2 with the slice panels the tensor cores stream).
+        __int128* accp;
+        size_t astep;
+        if (G) {
+          accp = P.acc + (size_t)blockIdx.x * (OZ_BM * OZ_BN) + (size_t)(half * (OZ_BN / 2)) * OZ_BM + row_in_tile;
+          astep = OZ_BM;
+        } else {
+          accp = P.acc + (row_ok ? row : 0) * tc.n + col0;
+          astep = 1;
+        }
 #pragma unroll 1
         for (int c = 0; c < OZ_BN / 32; ++c) {
           uint32_t w[16];
@@ -600,7 +642,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const int64_t col = col0 + j;
             if (col >= tc.n) continue;
             const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
-            __int128* ap = accp + (size_t)j * OZ_BM;
+            __int128* ap = accp + (size_t)j * astep;
             const __int128 sum = first ? contrib : (*ap + contrib);
             if (!last) {
               *ap = sum;
@@ -1178,9 +1220,7 @@ int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m,
   // column maxima of a column-major operand go through the accumulators).
   const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4);
   const size_t sa_b = al((size_t)S * m * kpad * 2), sb_b = al((size_t)S * n * kpad * 2);
-  // one 128 x 256 int128 accumulator slot per persistent CTA (a tile's
-  // accumulators live only while the CTA works on it; 78 MB for 152 CTAs)
-  const size_t acc_b = al(std::max((size_t)h->hw_sms * OZ_BM * OZ_BN * 16, (size_t)std::max(m, n) * 8));
+  const size_t acc_b = al(std::max((size_t)m * n * 16, (size_t)std::max(m, n) * 8));
   int st;
   uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + sa_b + sb_b + acc_b, &st);
   if (!ws) return st;
