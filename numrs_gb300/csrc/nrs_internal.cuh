@@ -95,6 +95,21 @@ int nrs_plain_gemm_launch(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_
 // ---------------------------------------------------------------------------
 #define NRS_DEV __device__ __forceinline__
 
+// 16-byte moves between a shared-memory tile and registers, as one vector
+// access (a byte-pointer memcpy may be split into narrow loads). Callers'
+// tile addresses are 16-byte aligned by construction.
+template <typename T>
+NRS_DEV void lds16(T* dst, const uint8_t* src) {
+  const uint4 q = *reinterpret_cast<const uint4*>(src);
+  memcpy(dst, &q, 16);
+}
+template <typename T>
+NRS_DEV void sts16(uint8_t* dst, const T* src) {
+  uint4 q;
+  memcpy(&q, src, 16);
+  *reinterpret_cast<uint4*>(dst) = q;
+}
+
 NRS_DEV uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

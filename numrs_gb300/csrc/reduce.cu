@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(64)
     } else {
       const uint8_t* row = smem + s * TILE + t * 128;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) memcpy(&v[c * PER16], row + ((c ^ sw) << 4), 16);
+      for (int c = 0; c < 8; ++c) lds16(&v[c * PER16], row + ((c ^ sw) << 4));
     }
     // Unrolled over the tile with constant indices (v stays in registers);
     // positions past the end of the axis are skipped.

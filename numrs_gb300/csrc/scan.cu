@@ -223,7 +223,7 @@ NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
   constexpr int PER16 = 16 / sizeof(T);
   T v[XB];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], tile + swz(t, j), 16);
+  for (int j = 0; j < 8; ++j) lds16(&v[j * PER16], tile + swz(t, j));
   if (cnt == XB) {
     acc = run_block<T, OP, XB>(v, first, acc);
   } else {
@@ -234,7 +234,7 @@ NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
   }
   if (WRITE) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) memcpy(tile + swz(t, j), &v[j * PER16], 16);
+    for (int j = 0; j < 8; ++j) sts16(tile + swz(t, j), &v[j * PER16]);
   }
   return acc;
 }
@@ -487,10 +487,10 @@ NRS_DEV T fold_seg(uint8_t* row, int cnt, bool first, T acc) {
     if (c >= SUB) {
       T v[SUB];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) memcpy(&v[j * PER16], blk + 16 * j, 16);
+      for (int j = 0; j < 8; ++j) lds16(&v[j * PER16], blk + 16 * j);
       acc = run_block<T, OP, SUB>(v, f, acc);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) memcpy(blk + 16 * j, &v[j * PER16], 16);
+      for (int j = 0; j < 8; ++j) sts16(blk + 16 * j, &v[j * PER16]);
     } else {  // the row's last, short block: element by element in place
       T* pv = reinterpret_cast<T*>(blk);
       for (int e = 0; e < c; ++e) {
