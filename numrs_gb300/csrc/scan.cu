@@ -221,20 +221,23 @@ template <typename T, int OP, bool WRITE>
 NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
   constexpr int XB = 128 / sizeof(T);
   constexpr int PER16 = 16 / sizeof(T);
-  T v[XB];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) lds16(&v[j * PER16], tile + swz(t, j));
   if (cnt == XB) {
-    acc = run_block<T, OP, XB>(v, first, acc);
-  } else {
-    for (int e = 0; e < cnt; ++e) {
-      acc = (e == 0 && first) ? v[0] : apply<T, OP>(acc, v[e]);
-      v[e] = acc;
-    }
-  }
-  if (WRITE) {
+    // constant indices only, so v stays in registers
+    T v[XB];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) sts16(tile + swz(t, j), &v[j * PER16]);
+    for (int j = 0; j < 8; ++j) lds16(&v[j * PER16], tile + swz(t, j));
+    acc = run_block<T, OP, XB>(v, first, acc);
+    if (WRITE) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) sts16(tile + swz(t, j), &v[j * PER16]);
+    }
+  } else {
+    // the axis' last, short tile: element by element in the tile itself
+    for (int e = 0; e < cnt; ++e) {
+      T* p = reinterpret_cast<T*>(tile + swz(t, e / PER16)) + (e % PER16);
+      acc = (e == 0 && first) ? *p : apply<T, OP>(acc, *p);
+      if (WRITE) *p = acc;
+    }
   }
   return acc;
 }
