@@ -394,8 +394,8 @@ typedef struct nrs_ozaki_info {
  * (|A'||B'|)_ij is 0, a second pass counts only the k where the other factor
  * is nonzero). Each operand is then carried to 53 + log2(max R) bits, which
  * keeps max_ij |C - AB|_ij / (|A||B|)_ij at about 2^-53. If no count within
- * the limits (16 slices, 126 bits, exact int32 sums for this K) reaches
- * that, or an operand holds Inf or NaN, the call runs the native FP64 DMMA
+ * the limits (16 slices, 126 bits, exact int32 sums for this K, an exact
+ * total within 128 bits: b (S - 1) <= 95 for b-bit digits) reaches that, or an operand holds Inf or NaN, the call runs the native FP64 DMMA
  * GEMM and reports slices = 0. The automatic mode reads the measured spread
  * back to the host: one synchronisation of the handle's stream, so it
  * cannot be captured in a CUDA graph; pass the count a previous call

@@ -36,10 +36,12 @@
 //                 finished accumulator to registers, hand it back to the MMA
 //                 warp at once, fold the copy into the int32 diagonal sums
 //                 kept in TMEM columns 256..511, and add each finished
-//                 diagonal into the int128 accumulators in global memory
-//                 (grouped launches: one column-major 128 x 256 slot per
-//                 CTA, so a warp's 32 rows are contiguous and all slots
-//                 together fit in L2).
+//                 diagonal into an m x n array of int128 accumulators.
+// Grouped launches (many small problems, one tile list) use 128 x 128 tiles,
+// a 6-stage ring and two accumulators in turn, and replace the per-diagonal
+// int128 read-modify-write by carried int32 sums that retire one b-bit digit
+// per diagonal into a write-only per-CTA slot, combined once per tile (the
+// grouped epilogue below describes it).
 // Measured at 8192^3 (clock counters per warp): the MMA warp waits for TMA
 // data ~29% of its time and for the epilogue ~8%.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
@@ -76,6 +78,28 @@ constexpr int kChunkOf(int b) { return 1 << (26 - 2 * b); }
 constexpr int kTopOf(int b) { return 127 - b; }  // position of the top digit in X
 constexpr int OZ_MAX_SLICES = 16;
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+// Tile geometry per launch kind. One large problem: 128 x 256 tiles, one
+// accumulator, 4 stages (the constants above). Grouped launches, mostly
+// small problems: 128 x 128 tiles (less padding for narrow problems), two
+// accumulators in TMEM columns 0..255 so the MMAs of the next group run
+// while the epilogue reads the last one, the diagonal sums in 256..383,
+// and 6 stages of 32 KB.
+template <bool G>
+struct OzGeom {
+  static constexpr int BN = G ? 128 : OZ_BN;
+  static constexpr int STAGES = G ? 6 : OZ_STAGES;
+  static constexpr int B_BYTES = BN * OZ_BK * 2;
+  static constexpr int STAGE_BYTES = OZ_A_BYTES + B_BYTES;
+  static constexpr int ACC_BUFS = G ? 2 : 1;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+  // kind::f16 instruction descriptor (see kIdesc below) for this N.
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                    ((uint32_t)(OZ_BM >> 4) << 24);
+};
+// Grouped launches keep, per CTA, a 128 x 128 slot of 16-byte digit records
+// (column-major: for one column a warp's 32 rows are 512 contiguous bytes).
+constexpr int OZ_DIGIT_BYTES = 16;
 
 
 // ---------------------------------------------------------------------------
@@ -305,7 +329,7 @@ __device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
     c.m = q.m;
     c.n = q.n;
     c.row0 = (int64_t)t.tm * OZ_BM;
-    c.col0 = (int64_t)t.tn * OZ_BN;
+    c.col0 = (int64_t)t.tn * OzGeom<true>::BN;
     c.arow = q.rowoff + c.row0;
     c.brow = q.coloff + c.col0;
     c.kblocks = (int)((q.kpad + OZ_BK - 1) / OZ_BK);
@@ -346,11 +370,12 @@ template <bool EST, bool G>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                     OzParams P) {
+  using Geo = OzGeom<G>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
-  uint64_t* empty = full + OZ_STAGES;
-  uint64_t* accf = empty + OZ_STAGES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Geo::STAGES * Geo::STAGE_BYTES);
+  uint64_t* empty = full + Geo::STAGES;
+  uint64_t* accf = empty + Geo::STAGES;
   uint64_t* acce = accf + 2;
   uint64_t* drain = acce + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
@@ -360,7 +385,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const int n_tiles = G ? P.n_tiles : P.tiles_m * P.tiles_n;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < OZ_STAGES; ++s) {
+    for (int s = 0; s < Geo::STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -406,11 +431,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           int kb1 = kb0 + P.kchunk / OZ_BK;
           if (kb1 > c.kblocks) kb1 = c.kblocks;
           for (int kb = kb0; kb < kb1; ++kb, ++it) {
-            const int s = it % OZ_STAGES;
-            const uint32_t ph = (it / OZ_STAGES) & 1;
+            const int s = it % Geo::STAGES;
+            const uint32_t ph = (it / Geo::STAGES) & 1;
             if (!bounded(&empty[s], ph ^ 1, 1)) { ok = false; break; }
-            uint8_t* st = smem + s * OZ_STAGE_BYTES;
-            mbar_arrive_expect_tx(&full[s], OZ_STAGE_BYTES);
+            uint8_t* st = smem + s * Geo::STAGE_BYTES;
+            mbar_arrive_expect_tx(&full[s], Geo::STAGE_BYTES);
             tma_load_3d(st, &mapA, &full[s], kb * OZ_BK, (int32_t)c.arow, pr.s);
             tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, (int32_t)c.brow, pr.t);
           }
@@ -418,8 +443,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
       if (!ok) {
         // Drain: wait (bounded) for the copies still in flight.
-        for (uint32_t j = (it >= OZ_STAGES ? it - OZ_STAGES : 0); j < it; ++j)
-          mbar_wait_bounded(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1, 1u << 16);
+        for (uint32_t j = (it >= Geo::STAGES ? it - Geo::STAGES : 0); j < it; ++j)
+          mbar_wait_bounded(&full[j % Geo::STAGES], (j / Geo::STAGES) & 1, 1u << 16);
       }
     }
   } else if (warp == 1) {
@@ -432,29 +457,30 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int gm = merge_count(c, P, EST);
         for (int u = 0; u < c.n_pairs && ok; ++ai) {
           const int u_end = group_end(u, c.n_pairs, gm, P.slices, c.kchunks);
-          // One accumulator (TMEM columns 0..255); the epilogue frees it as
-          // soon as it has folded it into the diagonal sums (columns 256..511).
-          const int buf = 0;
-          const uint32_t aph = ai & 1;
+          // One accumulator (TMEM columns 0..255) or two (0..127, 128..255,
+          // grouped launches), used in turn; the epilogue frees one as soon
+          // as it has copied it to registers.
+          const int buf = Geo::ACC_BUFS == 2 ? (int)(ai & 1) : 0;
+          const uint32_t aph = (Geo::ACC_BUFS == 2 ? ai >> 1 : ai) & 1;
           if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t d_tmem = tmem_base;
+          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * Geo::BN);
           for (int uu = u; uu < u_end && ok; ++uu) {
             const PairOf pr = pair_of(uu, P.slices, c.kchunks);
             const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
             int kb1 = kb0 + P.kchunk / OZ_BK;
             if (kb1 > c.kblocks) kb1 = c.kblocks;
             for (int kb = kb0; kb < kb1; ++kb, ++it) {
-              const int s = it % OZ_STAGES;
-              const uint32_t ph = (it / OZ_STAGES) & 1;
+              const int s = it % Geo::STAGES;
+              const uint32_t ph = (it / Geo::STAGES) & 1;
               if (!bounded(&full[s], ph, 3)) { ok = false; break; }
               tc_fence_after();
-              const uint32_t a_addr = smem_u32(smem + s * OZ_STAGE_BYTES);
+              const uint32_t a_addr = smem_u32(smem + s * Geo::STAGE_BYTES);
               const uint32_t b_addr = a_addr + OZ_A_BYTES;
 #pragma unroll
               for (int kk = 0; kk < OZ_BK / 16; ++kk) {
                 tc_mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
-                            kIdesc, (uu > u || kb > kb0 || kk > 0) ? 1u : 0u);
+                            Geo::IDESC, (uu > u || kb > kb0 || kk > 0) ? 1u : 0u);
               }
               tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
@@ -522,8 +548,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           __syncwarp();
           continue;
         }
-#pragma unroll 1
-        for (int c = 0; c < OZ_BN / 32; ++c) {
+#pragma unroll
+        for (int c = 0; c < OZ_BN / 32; ++c) {  // unrolled: v[] stays in registers
           uint32_t w[16];
           if (P.slices == 2) tmem_ld16(dsum_t + c * 16, w);  // warp-uniform
           if (!row_ok) continue;
@@ -547,6 +573,156 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     for (int off = 16; off; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
     if (lane == 0 && ok) atomicMax(P.est, __float_as_uint(rmax));
+  } else if (G) {
+    // ---------------- grouped epilogue (warps 2..9) ----------------
+    // Warp w reads TMEM lane quarter w % 4 (one tile row per thread); the
+    // two warps of a quarter take alternate 16-column chunks (half h:
+    // chunks h, h+2, h+4, h+6), so narrow problems keep both busy. Chunks
+    // right of the problem's n and quarters below its m skip all TMEM work
+    // (warp-uniform tests).
+    //
+    // Exact accumulation without a 128-bit read-modify-write: one int32 per
+    // element, R (TMEM columns 256..383), runs over the diagonals from
+    // d = S-1 (least significant) to d = 0. Moving from diagonal d+1 to d,
+    // R <- floor(R / 2^b) + D_d and the low b bits of the old R are final:
+    // they go, one byte per diagonal, into this CTA's digit slot
+    // (write-only). After d = 0,
+    //   T = R 2^(b(S-1)) + sum_i digit_i 2^(bi)   (digit i from d = S-1-i)
+    // is the exact sum of D_d 2^(b(S-1-d)), converted once to f64.
+    // |R| < 2^31: |D_d| <= 120 * 2^24 (host limit on K chunks x S) and the
+    // carry adds at most |R| / 2^b + 1.
+    constexpr int BN = Geo::BN;
+    constexpr size_t kColPitch = (size_t)OZ_BM * OZ_DIGIT_BYTES;  // slot bytes per tile column
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int row_in_tile = q * 32 + lane;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
+    const uint32_t dsum_t = lane_base + 2 * BN;
+    const int b = P.digit_bits, S = P.slices;
+    const int top_shift = b * (S - 1);
+    const uint32_t dmask = (1u << b) - 1;
+    uint8_t* const slot = reinterpret_cast<uint8_t*>(P.acc) + (size_t)blockIdx.x * (kColPitch * BN) +
+                          (size_t)row_in_tile * OZ_DIGIT_BYTES;
+    uint32_t ai = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+      const TileCtx tc = tile_ctx<G>(P, tile);
+      const int64_t row = tc.row0 + row_in_tile;
+      const bool row_ok = row < tc.m;
+      const int ncols = (int)(tc.n - tc.col0 < BN ? tc.n - tc.col0 : BN);
+      int nch = (ncols - 16 * half + 31) / 32;  // chunks of this warp inside the problem
+      if (nch < 0 || tc.row0 + q * 32 >= tc.m) nch = 0;
+      const int ecol_base = row_ok ? tc.ea[row] + P.final_shift : 0;
+      const int gm = merge_count(tc, P, false);
+      int prev_d = -1;
+      for (int u = 0, u_end = 0; u < tc.n_pairs; u = u_end, ++ai) {
+        u_end = group_end(u, tc.n_pairs, gm, S, tc.kchunks);
+        const int d = diag_of(u, S, tc.kchunks);
+        const bool diag_start = d != prev_d;
+        prev_d = d;
+        const bool final_group = u_end == tc.n_pairs;  // the last group of d = 0
+        const int buf = (int)(ai & 1);
+        if (!bounded(&accf[buf], (ai >> 1) & 1, 4)) { ok = false; break; }
+        tc_fence_after();
+        // Chunk by chunk: the accumulator and R in flight together, R
+        // updated and stored back; the accumulator goes back to the MMA warp
+        // after the last chunk is read (the other one is in use meanwhile).
+        const int dig_i = S - 2 - d;  // digit index of diagonal d + 1
+#pragma unroll
+        for (int i = 0; i < BN / 32; ++i) {
+          if (i >= nch) continue;
+          const int col_t = (2 * i + half) * 16;
+          uint32_t v[16], w[16];
+          tmem_ld16_nowait(lane_base + buf * BN + col_t, v);
+          if (u != 0) tmem_ld16_nowait(dsum_t + col_t, w);
+          tmem_wait_ld();
+          if (u == 0) {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) w[e] = (uint32_t)__float2int_rn(__uint_as_float(v[e]));
+          } else if (diag_start) {
+            uint8_t* sp = slot + (size_t)col_t * kColPitch + dig_i;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+              const int32_t r = (int32_t)w[e];
+              if (row_ok && col_t + e < ncols) sp[(size_t)e * kColPitch] = (uint8_t)((uint32_t)r & dmask);
+              w[e] = (uint32_t)((r >> b) + __float2int_rn(__uint_as_float(v[e])));
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 16; ++e) w[e] = (uint32_t)((int32_t)w[e] + __float2int_rn(__uint_as_float(v[e])));
+          }
+          tmem_st16(dsum_t + col_t, w);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+        tmem_wait_st();
+        // After the last group of d = 0: read R back, combine it with the
+        // digit records, convert, write C.
+#pragma unroll
+        for (int i = 0; i < BN / 32; ++i) {
+          if (!final_group || i >= nch) continue;
+          const int col_t = (2 * i + half) * 16;
+          uint32_t w[16];
+          tmem_ld16(dsum_t + col_t, w);
+          if (!row_ok) continue;
+          // Eight columns at a time: their digit records and column exponents
+          // (all loads in flight), then T, its f64 value and C.
+          const uint8_t* dp = slot + (size_t)col_t * kColPitch;
+#pragma unroll
+          for (int e0 = 0; e0 < 16; e0 += 8) {
+            uint64_t lo[8], hi[8];
+            int ebits[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              lo[e] = hi[e] = 0;
+              ebits[e] = 0;
+              if (col_t + e0 + e < ncols) {
+                const uint8_t* rec = dp + (size_t)(e0 + e) * kColPitch;
+                if (S <= 9) {
+                  lo[e] = __ldcg(reinterpret_cast<const unsigned long long*>(rec));
+                } else {
+                  const uint4 x = __ldcg(reinterpret_cast<const uint4*>(rec));
+                  lo[e] = (uint64_t)x.x | (uint64_t)x.y << 32;
+                  hi[e] = (uint64_t)x.z | (uint64_t)x.w << 32;
+                }
+                ebits[e] = tc.eb[tc.col0 + col_t + e0 + e];
+              }
+            }
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              if (col_t + e0 + e >= ncols) continue;
+              // T = (((R 2^b + digit_{S-2}) 2^b + ...) 2^b + digit_0 as a
+              // 128-bit two's complement (th, tl); a digit fills the b zero
+              // bits the shift leaves.
+              int64_t th = (int64_t)(int32_t)w[e0 + e] >> 63;
+              uint64_t tl = (uint64_t)(int64_t)(int32_t)w[e0 + e];
+#pragma unroll 1
+              for (int t = S - 2; t >= 0; --t) {
+                const uint64_t dg = (t < 8 ? lo[e] >> (8 * t) : hi[e] >> (8 * (t - 8))) & 0xFF;
+                th = (int64_t)(((uint64_t)th << b) | (tl >> (64 - b)));
+                tl = (tl << b) | dg;
+              }
+              // |T| < 2^127: keep its top 64 significant bits, convert once.
+              const bool neg = th < 0;
+              uint64_t mhi = (uint64_t)th, mlo = tl;
+              if (neg) {
+                mlo = ~mlo + 1;
+                mhi = ~mhi + (mlo == 0 ? 1 : 0);
+              }
+              const int sh = mhi ? 64 - __clzll((long long)mhi) : 0;
+              const uint64_t top = sh == 0 ? mlo : sh == 64 ? mhi : (mhi << (64 - sh)) | (mlo >> sh);
+              const double val = ldexp((double)top, sh + ecol_base + ebits[e]);
+              double* cp = tc.C + row * tc.ldc + tc.col0 + col_t + e0 + e;
+              const double r = neg ? -val : val;
+              *cp = tc.accumulate ? *cp + r : r;
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+      }
+    }
   } else {
     // ---------------- epilogue (warps 2..9) ----------------
     // Warp w reads TMEM lane quarter w % 4 (one tile row per thread) and
@@ -617,20 +793,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const bool first = (d == P.slices - 1), last = (d == 0);
         const int shift = P.digit_bits * (P.slices - 1 - d);
         const int ecol_base = (last && row_ok) ? tc.ea[row] + P.final_shift : 0;
-        // Grouped launches: this CTA's accumulator slot, column-major within
-        // the tile (for a fixed column the warp's 32 rows are 512 contiguous
-        // bytes; all slots together stay in L2). One large problem: an m x n
-        // row-major array (measured 5% faster at 8192^3 than the slots, whose
-        // 78 MB compete in L2 with the slice panels the tensor cores stream).
-        __int128* accp;
-        size_t astep;
-        if (G) {
-          accp = P.acc + (size_t)blockIdx.x * (OZ_BM * OZ_BN) + (size_t)(half * (OZ_BN / 2)) * OZ_BM + row_in_tile;
-          astep = OZ_BM;
-        } else {
-          accp = P.acc + (row_ok ? row : 0) * tc.n + col0;
-          astep = 1;
-        }
+        // The int128 accumulators: an m x n row-major array (measured 5%
+        // faster at 8192^3 than per-CTA slots, whose 78 MB compete in L2 with
+        // the slice panels the tensor cores stream).
+        __int128* const accp = P.acc + (row_ok ? row : 0) * tc.n + col0;
 #pragma unroll 1
         for (int c = 0; c < OZ_BN / 32; ++c) {
           uint32_t w[16];
@@ -642,7 +808,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const int64_t col = col0 + j;
             if (col >= tc.n) continue;
             const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
-            __int128* ap = accp + (size_t)j * astep;
+            __int128* ap = accp + j;
             const __int128 sum = first ? contrib : (*ap + contrib);
             if (!last) {
               *ap = sum;
@@ -1103,17 +1269,18 @@ template <bool EST, bool G>
 int launch_tc(nrs_handle* h, const void* sa, const void* sb, int S, const OzParams& P, int64_t rows_a,
               int64_t rows_b, cudaStream_t stream) {
   CUtensorMap mapA, mapB;
-  if (!make_slice_map(&mapA, sa, P.kpad, rows_a, S, OZ_BM) || !make_slice_map(&mapB, sb, P.kpad, rows_b, S, OZ_BN))
+  if (!make_slice_map(&mapA, sa, P.kpad, rows_a, S, OZ_BM) ||
+      !make_slice_map(&mapB, sb, P.kpad, rows_b, S, OzGeom<G>::BN))
     return nrs_fail(h, NRS_ERR_CUDA, "cuTensorMapEncodeTiled failed for the slices");
   // Set on every call: the attribute belongs to the current device's context.
   int st = nrs_cuda_check(h, cudaFuncSetAttribute(ozaki_tc_kernel<EST, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  OZ_SMEM),
+                                                  OzGeom<G>::SMEM),
                           "cudaFuncSetAttribute(ozaki)");
   if (st) return st;
   const int n_tiles = G ? P.n_tiles : P.tiles_m * P.tiles_n;
   const int ctas = n_tiles < h->num_sms ? n_tiles : h->num_sms;
   if (ctas < 1) return NRS_OK;
-  ozaki_tc_kernel<EST, G><<<ctas, OZ_THREADS, OZ_SMEM, stream>>>(mapA, mapB, P);
+  ozaki_tc_kernel<EST, G><<<ctas, OZ_THREADS, OzGeom<G>::SMEM, stream>>>(mapA, mapB, P);
   return nrs_after_launch(h, EST ? "ozaki_tc_kernel<est>" : "ozaki_tc_kernel");
 }
 
@@ -1130,16 +1297,29 @@ OzParams base_params(nrs_handle* h, int64_t m, int64_t n, int64_t k, int64_t kpa
   return P;
 }
 
+// Limits of b-bit digits with S slices over kpad: S <= 16, every digit
+// inside the 126 fraction bits (b S <= 126), int32-exact diagonal sums (at
+// most kc S K-chunk sums of |x| <= 2^24 each, kc = ceil(kpad / 2^(26-2b)):
+// kc S <= 127 for one problem, <= 120 for grouped launches, whose carried
+// sums need the headroom), and the exact total inside a signed 128-bit
+// integer (|total| < 2^(31 + b(S-1)) with b(S-1) <= 95).
+constexpr int64_t kMaxChunkSlices = 127;
+constexpr int64_t kMaxChunkSlicesGrouped = 120;
+bool digits_fit(int b, int S, int64_t kpad, int64_t max_kcs) {
+  const int64_t kc = std::max<int64_t>(1, (kpad + kChunkOf(b) - 1) / kChunkOf(b));
+  return S >= 1 && S <= OZ_MAX_SLICES && b * S <= 126 && b * (S - 1) <= 95 && kc * S <= max_kcs;
+}
+
 // Digit width and count for `bits` bits of each operand's fixed-point value:
-// the widest b (8, 7, 6) with S = ceil(bits / b) <= 16, every digit inside
-// the 126 fraction bits (b S <= 126) and int32-exact diagonal sums
-// (ceil(kpad / 2^(26-2b)) S < 128). false if no width qualifies.
-bool choose_digits(int64_t kpad, double bits, int* b, int* S, int* kchunks) {
+// the widest b (8, 7, 6) with S = ceil(bits / b) inside digits_fit's limits.
+// false if no width qualifies.
+bool choose_digits(int64_t kpad, double bits, int* b, int* S, int* kchunks,
+                   int64_t max_kcs = kMaxChunkSlices) {
   for (int cand = 8; cand >= 6; --cand) {
     int s_c = (int)std::ceil(bits / cand - 1e-9);
     if (s_c < 1) s_c = 1;
     const int64_t kc = (kpad + kChunkOf(cand) - 1) / kChunkOf(cand);
-    if (s_c <= OZ_MAX_SLICES && cand * s_c <= 126 && (kc > 0 ? kc : 1) * s_c < 128) {
+    if (digits_fit(cand, s_c, kpad, max_kcs)) {
       *b = cand;
       *S = s_c;
       *kchunks = (int)kc;
@@ -1405,7 +1585,7 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
     // Widest digits whose int32 diagonal sums stay exact for this K and S.
     for (int cand = 8; cand >= 6 && !b; --cand) {
       const int kc = (int)((kpad + kChunkOf(cand) - 1) / kChunkOf(cand));
-      if ((int64_t)(kc > 0 ? kc : 1) * slices < 128 && cand * slices <= 126) {
+      if (digits_fit(cand, slices, kpad, kMaxChunkSlices)) {
         b = cand;
         S = slices;
         kchunks = kc;
@@ -1540,10 +1720,11 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
     if (r.flags & 1u) continue;
     double need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
     int bb, SS, kc;
-    if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc))) {
+    if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc, kMaxChunkSlicesGrouped))) {
       if ((st = spread_estimate(h, a, bT, g.m, g.n, g.k, kpad8, 2, &r))) return st;
       need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
-      if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc))) continue;
+      if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc, kMaxChunkSlicesGrouped)))
+        continue;
     }
     bits_max = std::max(bits_max, need);
     keep.push_back(i);
@@ -1553,8 +1734,7 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   if (digit_bits) {
     // a given width: S from the bits (or as given), if the width's limits hold
     const int s_c = slices > 0 ? slices : std::max(1, (int)std::ceil(bits_max / digit_bits - 1e-9));
-    const int kc = (int)((kp_max + kChunkOf(digit_bits) - 1) / kChunkOf(digit_bits));
-    if (s_c <= OZ_MAX_SLICES && (int64_t)kc * s_c < 128 && digit_bits * s_c <= 126) {
+    if (digits_fit(digit_bits, s_c, kp_max, kMaxChunkSlicesGrouped)) {
       b = digit_bits;
       S = s_c;
     } else {
@@ -1563,14 +1743,14 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   } else if (slices > 0) {
     for (int cand = 8; cand >= 6 && !b; --cand) {
       const int kc = (int)((kp_max + kChunkOf(cand) - 1) / kChunkOf(cand));
-      if ((int64_t)kc * slices < 128 && cand * slices <= 126) {
+      if (digits_fit(cand, slices, kp_max, kMaxChunkSlicesGrouped)) {
         b = cand;
         S = slices;
         kc_max = kc;
       }
     }
     if (!b) return nrs_fail(h, NRS_ERR_TOO_LARGE, "k too large for this slice count");
-  } else if (!choose_digits(kp_max, bits_max, &b, &S, &kc_max)) {
+  } else if (!choose_digits(kp_max, bits_max, &b, &S, &kc_max, kMaxChunkSlicesGrouped)) {
     return NRS_OK;  // nothing qualifies together: all stay on DMMA
   }
   (void)kc_max;
@@ -1598,7 +1778,8 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
       for (int64_t k0 = 0; k0 < g.k; k0 += kColStrip) colch.push_back(OzChunk{p, (int32_t)c0, (int32_t)k0, 0});
     for (int64_t c0 = 0; c0 < g.n; c0 += kSliceColN)
       for (int64_t k0 = 0; k0 < kpad; k0 += kSliceColK) slcol.push_back(OzChunk{p, (int32_t)c0, (int32_t)k0, 0});
-    const int tm_n = (int)((g.m + OZ_BM - 1) / OZ_BM), tn_n = (int)((g.n + OZ_BN - 1) / OZ_BN);
+    constexpr int kBN = OzGeom<true>::BN;
+    const int tm_n = (int)((g.m + OZ_BM - 1) / OZ_BM), tn_n = (int)((g.n + kBN - 1) / kBN);
     for (int a = 0; a < tm_n; ++a)
       for (int c = 0; c < tn_n; ++c) tiles.push_back({(double)kpad * (S * (S + 1) / 2), OzTile{p, a, c, 0}});
     rowoff += g.m;
@@ -1615,7 +1796,7 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
                b_pr = al(probs.size() * sizeof(OzProb)), b_tl = al(tl.size() * sizeof(OzTile)),
                b_ea = al((size_t)rowoff * 4), b_eb = al((size_t)coloff * 4), b_cm = al((size_t)coloff * 8),
                b_sa = al((size_t)S * rowoff * kp_max * 2), b_sb = al((size_t)S * coloff * kp_max * 2),
-               b_acc = al((size_t)h->hw_sms * OZ_BM * OZ_BN * 16);  // a slot per CTA (grid <= SMs)
+               b_acc = al((size_t)h->hw_sms * OZ_BM * OzGeom<true>::BN * OZ_DIGIT_BYTES);  // a digit slot per CTA
   const size_t total = b_in + b_rc + b_cc + b_sc + b_pr + b_tl + b_ea + b_eb + b_cm + b_sa + b_sb + b_acc;
   nrs_ozaki_group* G = new nrs_ozaki_group();
   if (cudaMalloc(&G->arena, total) != cudaSuccess) {

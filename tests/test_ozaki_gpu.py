@@ -276,6 +276,50 @@ def test_plan_f64_on_tensor_cores_replays_and_accumulates(K, ora):
     plan.close()
 
 
+@pytest.mark.parametrize("bits,slices", [(8, 1), (8, 3), (7, 3), (6, 5)])
+def test_ozaki_grouped_integer_known_answer(K, bits, slices):
+    """Grouped launches carry the diagonal sums through int32 R with one
+    retired digit per diagonal. Integers |x| <= 4096 need two 8- or 7-bit
+    digits (three 6-bit ones), so every nonzero slice product is among the
+    computed pairs and C must equal the exact integer product bit for bit;
+    random signs exercise negative carries. slices = 1 uses |x| <= 3."""
+    r = np.random.default_rng(11 + bits + slices)
+    lim = 3 if slices == 1 else 4096
+    shapes = [(1, 7, 1), (129, 65, 257), (40, 1000, 300), (300, 33, 17), (128, 128, 128), (17, 700, 130)]
+    probs, exact = [], []
+    for m, k, n in shapes:
+        A = r.integers(-lim, lim + 1, (m, k))
+        B = r.integers(-lim, lim + 1, (k, n))
+        exact.append((A @ B).astype(np.float64))
+        probs.append((_dev(A.astype(np.float64)), _dev(B.astype(np.float64)),
+                      torch.full((m, n), float("nan"), dtype=torch.float64, device="cuda"), False))
+    plan = K.Plan(probs, f64_mode=L.PLAN_F64_OZAKI, f64_slices=slices, f64_digit_bits=bits)
+    assert plan.f64_info() == (len(shapes), slices, bits)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    for (_, _, c, _), e in zip(probs, exact):
+        np.testing.assert_array_equal(to_np(c), e)
+    plan.close()
+
+
+@pytest.mark.parametrize("bits,slices", [(8, 12), (7, 10), (6, 14), (7, 9)])
+def test_ozaki_grouped_digit_widths(K, ora, bits, slices):
+    """Every digit width, 8-byte (S <= 9) and 16-byte digit records, and a
+    K of 3000 (three exact K chunks at b = 8), against double-double. Each
+    count carries at least 63 bits: these operands' spread needs more than
+    the 53 of a spread-free product."""
+    probs = _group_problems(53, 24)
+    probs.append((torch.rand((40, 3000), dtype=torch.float64, device="cuda") - 0.5,
+                  torch.rand((3000, 90), dtype=torch.float64, device="cuda") - 0.5,
+                  torch.empty((40, 90), dtype=torch.float64, device="cuda"), False))
+    plan = K.Plan(probs, f64_mode=L.PLAN_F64_OZAKI, f64_slices=slices, f64_digit_bits=bits)
+    assert plan.f64_info() == (len(probs), slices, bits)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    _check_against_dd(ora, K, probs)
+    plan.close()
+
+
 def test_autotune_considers_tensor_core_f64(K, ora):
     probs = _group_problems(47, 80)
     f32 = []
