@@ -65,10 +65,8 @@ constexpr int OZ_BN = 256;
 constexpr int OZ_BK = 64;
 constexpr int OZ_STAGES = 4;
 constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;  // 16 KB
-constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 32 KB
-constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
 constexpr int OZ_THREADS = 320;                 // 10 warps: TMA, MMA, 8 epilogue
-constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
+constexpr int OZ_TMEM_COLS = 512;               // accumulator(s) + diagonal sums
 // Signed digits of b bits: |digit| <= 2^(b-1), exact in BF16 (8-bit
 // significand) for b <= 8; products <= 2^(2b-2), so a K chunk of 2^(26-2b)
 // sums exactly in FP32 (at most 2^24). Wider digits need fewer slices for
@@ -77,7 +75,6 @@ constexpr int OZ_TMEM_COLS = 512;               // 2 accumulators x 256 columns
 constexpr int kChunkOf(int b) { return 1 << (26 - 2 * b); }
 constexpr int kTopOf(int b) { return 127 - b; }  // position of the top digit in X
 constexpr int OZ_MAX_SLICES = 16;
-constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 
 // Tile geometry per launch kind. One large problem: 128 x 256 tiles, one
 // accumulator, 4 stages (the constants above). Grouped launches, mostly
@@ -93,7 +90,9 @@ struct OzGeom {
   static constexpr int STAGE_BYTES = OZ_A_BYTES + B_BYTES;
   static constexpr int ACC_BUFS = G ? 2 : 1;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-  // kind::f16 instruction descriptor (see kIdesc below) for this N.
+  // Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+  // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+  // 17-22, M >> 4 at bits 24-28.
   static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                     ((uint32_t)(OZ_BM >> 4) << 24);
 };
@@ -135,22 +134,6 @@ NRS_DEV void tc_commit(uint64_t* bar) {
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(bar))
       : "memory");
-}
-
-// 32 lanes x 32 consecutive 32-bit columns: thread = lane, v[c] = column c.
-NRS_DEV void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
-        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // 32 lanes x 16 consecutive 32-bit columns.
@@ -202,12 +185,6 @@ NRS_DEV uint64_t smem_desc_sw128(uint32_t saddr) {
   d |= (uint64_t)2 << 61;
   return d;
 }
-
-// Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
-// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
-// 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
-                            ((uint32_t)(OZ_BM >> 4) << 24);
 
 struct OzParams {
   int64_t m, n, k, kpad;
@@ -318,6 +295,95 @@ __device__ __forceinline__ int group_end(int u, int n_pairs, int gm, int S, int 
   int e = u + 1;
   while (e < n_pairs && e - u < gm && diag_of(e, S, kchunks) == d) ++e;
   return e;
+}
+
+// x 2^e for an integer-valued x in [0, 2^64], rounded once: one multiply by
+// an exact power of two, with a pre-scale by 2^1023 or 2^-1022 (exact for
+// such x) when e lies outside the normal exponent range.
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+  if (e > 1023) {
+    x *= 0x1p1023;
+    e -= 1023;
+    if (e > 1023) e = 1023;
+  } else if (e < -1022) {
+    x *= 0x1p-1022;
+    e += 1022;
+    if (e < -1022) e = -1022;
+  }
+  return x * __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// f64 value of the exact total T = R 2^(b(S-1)) + sum_t digit_t 2^(bt)
+// (digit t = byte t of the record lo | hi << 64) times 2^e: T as a 128-bit
+// two's complement (th, tl), its top 64 significant bits converted once.
+__device__ __forceinline__ double retire_value(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int e) {
+  const int nd = S - 1;
+  int64_t th;
+  uint64_t tl;
+  if (b == 8) {
+    // the digits are the record's bytes: T = R 2^(8 nd) + (record mod 2^(8 nd))
+    const int sh = 8 * nd;
+    if (sh < 64) {
+      tl = ((uint64_t)(int64_t)R << sh) | (sh ? lo & (~0ull >> (64 - sh)) : 0);
+      th = sh ? (int64_t)R >> (64 - sh) : (int64_t)R >> 63;
+    } else {
+      tl = lo;
+      th = (int64_t)(((uint64_t)(int64_t)R << (sh - 64)) | (sh > 64 ? hi & (~0ull >> (128 - sh)) : 0));
+    }
+  } else {
+    // Horner: T = ((R 2^b + digit_{nd-1}) 2^b + ...) 2^b + digit_0; each
+    // digit fills the b zero bits the shift leaves.
+    th = (int64_t)R >> 63;
+    tl = (uint64_t)(int64_t)R;
+#pragma unroll 1
+    for (int t = nd - 1; t >= 0; --t) {
+      const uint64_t dg = (t < 8 ? lo >> (8 * t) : hi >> (8 * (t - 8))) & 0xFF;
+      th = (int64_t)(((uint64_t)th << b) | (tl >> (64 - b)));
+      tl = (tl << b) | dg;
+    }
+  }
+  const bool neg = th < 0;
+  uint64_t mhi = (uint64_t)th, mlo = tl;
+  if (neg) {
+    mlo = ~mlo + 1;
+    mhi = ~mhi + (mlo == 0 ? 1 : 0);
+  }
+  const int sh = mhi ? 64 - __clzll((long long)mhi) : 0;
+  const uint64_t top = sh == 0 ? mlo : sh == 64 ? mhi : (mhi << (64 - sh)) | (mlo >> sh);
+  const double v = scale_pow2((double)top, sh + e);
+  return neg ? -v : v;
+}
+
+// Writes 16 consecutive columns of one tile row from their R values, digit
+// records (16 bytes apart by `pitch`) and column exponents; `left` columns
+// of the 16 lie inside the problem. WIDE: 16-byte records (S > 9).
+template <bool WIDE>
+__device__ __forceinline__ void retire_chunk(const uint32_t (&w)[16], const uint8_t* rec, size_t pitch,
+                                             const int* eb, int left, int b, int S, int ebase, double* crow,
+                                             bool accumulate) {
+  uint64_t lo[16], hi[16];
+  int ex[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    lo[e] = hi[e] = 0;
+    ex[e] = 0;
+    if (e < left) {
+      if (WIDE) {
+        const uint4 x = __ldcg(reinterpret_cast<const uint4*>(rec + (size_t)e * pitch));
+        lo[e] = (uint64_t)x.x | (uint64_t)x.y << 32;
+        hi[e] = (uint64_t)x.z | (uint64_t)x.w << 32;
+      } else {
+        lo[e] = __ldcg(reinterpret_cast<const unsigned long long*>(rec + (size_t)e * pitch));
+      }
+      ex[e] = eb[e];
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    if (e >= left) continue;
+    const double r = retire_value((int32_t)w[e], lo[e], hi[e], b, S, ebase + ex[e]);
+    crow[e] = accumulate ? crow[e] + r : r;
+  }
 }
 
 template <bool G>
@@ -599,7 +665,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
     const uint32_t dsum_t = lane_base + 2 * BN;
     const int b = P.digit_bits, S = P.slices;
-    const int top_shift = b * (S - 1);
     const uint32_t dmask = (1u << b) - 1;
     uint8_t* const slot = reinterpret_cast<uint8_t*>(P.acc) + (size_t)blockIdx.x * (kColPitch * BN) +
                           (size_t)row_in_tile * OZ_DIGIT_BYTES;
@@ -666,58 +731,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           uint32_t w[16];
           tmem_ld16(dsum_t + col_t, w);
           if (!row_ok) continue;
-          // Eight columns at a time: their digit records and column exponents
-          // (all loads in flight), then T, its f64 value and C.
-          const uint8_t* dp = slot + (size_t)col_t * kColPitch;
-#pragma unroll
-          for (int e0 = 0; e0 < 16; e0 += 8) {
-            uint64_t lo[8], hi[8];
-            int ebits[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              lo[e] = hi[e] = 0;
-              ebits[e] = 0;
-              if (col_t + e0 + e < ncols) {
-                const uint8_t* rec = dp + (size_t)(e0 + e) * kColPitch;
-                if (S <= 9) {
-                  lo[e] = __ldcg(reinterpret_cast<const unsigned long long*>(rec));
-                } else {
-                  const uint4 x = __ldcg(reinterpret_cast<const uint4*>(rec));
-                  lo[e] = (uint64_t)x.x | (uint64_t)x.y << 32;
-                  hi[e] = (uint64_t)x.z | (uint64_t)x.w << 32;
-                }
-                ebits[e] = tc.eb[tc.col0 + col_t + e0 + e];
-              }
-            }
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              if (col_t + e0 + e >= ncols) continue;
-              // T = (((R 2^b + digit_{S-2}) 2^b + ...) 2^b + digit_0 as a
-              // 128-bit two's complement (th, tl); a digit fills the b zero
-              // bits the shift leaves.
-              int64_t th = (int64_t)(int32_t)w[e0 + e] >> 63;
-              uint64_t tl = (uint64_t)(int64_t)(int32_t)w[e0 + e];
-#pragma unroll 1
-              for (int t = S - 2; t >= 0; --t) {
-                const uint64_t dg = (t < 8 ? lo[e] >> (8 * t) : hi[e] >> (8 * (t - 8))) & 0xFF;
-                th = (int64_t)(((uint64_t)th << b) | (tl >> (64 - b)));
-                tl = (tl << b) | dg;
-              }
-              // |T| < 2^127: keep its top 64 significant bits, convert once.
-              const bool neg = th < 0;
-              uint64_t mhi = (uint64_t)th, mlo = tl;
-              if (neg) {
-                mlo = ~mlo + 1;
-                mhi = ~mhi + (mlo == 0 ? 1 : 0);
-              }
-              const int sh = mhi ? 64 - __clzll((long long)mhi) : 0;
-              const uint64_t top = sh == 0 ? mlo : sh == 64 ? mhi : (mhi << (64 - sh)) | (mlo >> sh);
-              const double val = ldexp((double)top, sh + ecol_base + ebits[e]);
-              double* cp = tc.C + row * tc.ldc + tc.col0 + col_t + e0 + e;
-              const double r = neg ? -val : val;
-              *cp = tc.accumulate ? *cp + r : r;
-            }
-          }
+          const uint8_t* rec = slot + (size_t)col_t * kColPitch;
+          const int* eb = tc.eb + tc.col0 + col_t;
+          double* crow = tc.C + row * tc.ldc + tc.col0 + col_t;
+          if (S <= 9)
+            retire_chunk<false>(w, rec, kColPitch, eb, ncols - col_t, b, S, ecol_base, crow, tc.accumulate);
+          else
+            retire_chunk<true>(w, rec, kColPitch, eb, ncols - col_t, b, S, ecol_base, crow, tc.accumulate);
         }
         tc_fence_before();
         __syncwarp();
