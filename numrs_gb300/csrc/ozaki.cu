@@ -96,9 +96,10 @@ struct OzGeom {
   static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                     ((uint32_t)(OZ_BM >> 4) << 24);
 };
-// Grouped launches keep, per CTA, a 128 x 128 slot of 16-byte digit records
-// (column-major: for one column a warp's 32 rows are 512 contiguous bytes).
-constexpr int OZ_DIGIT_BYTES = 16;
+// Grouped launches with S > 9 keep digits 8..14 in a per-CTA 128 x 128 slot
+// of 8-byte records (column-major: for one column a warp's 32 rows are 256
+// contiguous bytes).
+constexpr int OZ_DIGIT_BYTES = 8;
 
 
 // ---------------------------------------------------------------------------
@@ -160,6 +161,14 @@ NRS_DEV void tmem_ld16_nowait(uint32_t taddr, uint32_t* v) {
         "=r"(v[14]), "=r"(v[15])
       : "r"(taddr)
       : "memory");
+}
+// 32 lanes x 8 columns into v[0..7] without waiting.
+NRS_DEV void tmem_ld8_nowait(uint32_t taddr, uint32_t* v) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                 "=r"(v[7])
+               : "r"(taddr)
+               : "memory");
 }
 NRS_DEV void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -244,20 +253,33 @@ struct TileCtx {
   int accumulate;
 };
 
-// Pair order within a tile: diagonals from the least significant (d = S-1)
-// to the most significant (d = 0), so the last unit of a tile is pair (0,0).
-struct PairOf {
-  int s, t, chunk;
-};
-__device__ __forceinline__ PairOf pair_of(int u, int S, int kchunks) {
-  const int chunk = u % kchunks;
-  int p = u / kchunks;
-  for (int d = S - 1; d >= 0; --d) {
-    if (p < d + 1) return {p, d - p, chunk};
-    p -= d + 1;
+// Work units of a tile, in order: diagonals from the least significant
+// (d = S-1) to the most significant (d = 0), within a diagonal the pairs
+// (s, t = d - s) for s = 0..d, within a pair its K chunks; the last unit of a
+// tile is pair (0,0). Walked incrementally (no search per unit).
+struct PairIter {
+  int d, s, chunk;
+  __device__ __forceinline__ void start(int S) {
+    d = S - 1;
+    s = 0;
+    chunk = 0;
   }
-  return {0, 0, chunk};
-}
+  __device__ __forceinline__ int t() const { return d - s; }
+  __device__ __forceinline__ bool diag_first() const { return s == 0 && chunk == 0; }
+  // units of the current diagonal from this one on, this one included
+  __device__ __forceinline__ int left(int kchunks) const { return (d - s) * kchunks + (kchunks - chunk); }
+  __device__ __forceinline__ void next(int kchunks) {
+    if (++chunk == kchunks) {
+      chunk = 0;
+      if (s < d) {
+        ++s;
+      } else {
+        --d;
+        s = 0;
+      }
+    }
+  }
+};
 
 __device__ __forceinline__ void tile_coords(int tile, const OzParams& P, int& tm, int& tn) {
   // Grouped rasterisation: consecutive tiles walk group_m tile rows before
@@ -283,18 +305,11 @@ __device__ __forceinline__ int merge_count(const TileCtx& c, const OzParams& P, 
   const int64_t g = ((int64_t)1 << 24) / per_pair;
   return g < 1 ? 1 : (int)g;
 }
-__device__ __forceinline__ int diag_of(int u, int S, int kchunks) {
-  const PairOf p = pair_of(u, S, kchunks);
-  return p.s + p.t;
-}
-// End of the accumulation group starting at unit u: same diagonal, at most
-// `gm` units.
-__device__ __forceinline__ int group_end(int u, int n_pairs, int gm, int S, int kchunks) {
-  if (gm <= 1) return u + 1;
-  const int d = diag_of(u, S, kchunks);
-  int e = u + 1;
-  while (e < n_pairs && e - u < gm && diag_of(e, S, kchunks) == d) ++e;
-  return e;
+// Units in the accumulation group that starts at `pi`: the same diagonal, at
+// most `gm` units.
+__device__ __forceinline__ int group_size(const PairIter& pi, int gm, int kchunks) {
+  const int l = pi.left(kchunks);
+  return l < gm ? l : gm;
 }
 
 // x 2^e for an integer-valued x in [0, 2^64], rounded once: one multiply by
@@ -354,34 +369,29 @@ __device__ __forceinline__ double retire_value(int32_t R, uint64_t lo, uint64_t 
   return neg ? -v : v;
 }
 
-// Writes 16 consecutive columns of one tile row from their R values, digit
-// records (16 bytes apart by `pitch`) and column exponents; `left` columns
-// of the 16 lie inside the problem. WIDE: 16-byte records (S > 9).
-template <bool WIDE>
-__device__ __forceinline__ void retire_chunk(const uint32_t (&w)[16], const uint8_t* rec, size_t pitch,
-                                             const int* eb, int left, int b, int S, int ebase, double* crow,
-                                             bool accumulate) {
-  uint64_t lo[16], hi[16];
-  int ex[16];
+// Writes 8 consecutive columns of one tile row: R values w, digits 0..3 (lw)
+// and 4..7 (hw, S > 5 only) as words per column, digits 8..14 from the
+// 8-byte records `pitch` apart (S > 9 only) and the column exponents; `left`
+// of the 8 columns lie inside the problem.
+__device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (&lw)[8], const uint32_t (&hw)[8],
+                                        const uint8_t* rec, size_t pitch, const int* eb, int left, int b, int S,
+                                        int ebase, double* crow, bool accumulate) {
+  uint64_t hi[8];
+  int ex[8];
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
-    lo[e] = hi[e] = 0;
+  for (int e = 0; e < 8; ++e) {
+    hi[e] = 0;
     ex[e] = 0;
     if (e < left) {
-      if (WIDE) {
-        const uint4 x = __ldcg(reinterpret_cast<const uint4*>(rec + (size_t)e * pitch));
-        lo[e] = (uint64_t)x.x | (uint64_t)x.y << 32;
-        hi[e] = (uint64_t)x.z | (uint64_t)x.w << 32;
-      } else {
-        lo[e] = __ldcg(reinterpret_cast<const unsigned long long*>(rec + (size_t)e * pitch));
-      }
+      if (S > 9) hi[e] = __ldcg(reinterpret_cast<const unsigned long long*>(rec + (size_t)e * pitch));
       ex[e] = eb[e];
     }
   }
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
+  for (int e = 0; e < 8; ++e) {
     if (e >= left) continue;
-    const double r = retire_value((int32_t)w[e], lo[e], hi[e], b, S, ebase + ex[e]);
+    const uint64_t lo = S - 1 > 4 ? (uint64_t)lw[e] | (uint64_t)hw[e] << 32 : (uint64_t)lw[e];
+    const double r = retire_value((int32_t)w[e], lo, hi[e], b, S, ebase + ex[e]);
     crow[e] = accumulate ? crow[e] + r : r;
   }
 }
@@ -491,8 +501,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       bool ok = true;
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const TileCtx c = tile_ctx<G>(P, tile);
-        for (int u = 0; u < c.n_pairs && ok; ++u) {
-          const PairOf pr = pair_of(u, P.slices, c.kchunks);
+        PairIter pr;
+        pr.start(P.slices);
+        for (int u = 0; u < c.n_pairs && ok; ++u, pr.next(c.kchunks)) {
           const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
           int kb1 = kb0 + P.kchunk / OZ_BK;
           if (kb1 > c.kblocks) kb1 = c.kblocks;
@@ -503,7 +514,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             uint8_t* st = smem + s * Geo::STAGE_BYTES;
             mbar_arrive_expect_tx(&full[s], Geo::STAGE_BYTES);
             tma_load_3d(st, &mapA, &full[s], kb * OZ_BK, (int32_t)c.arow, pr.s);
-            tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, (int32_t)c.brow, pr.t);
+            tma_load_3d(st + OZ_A_BYTES, &mapB, &full[s], kb * OZ_BK, (int32_t)c.brow, pr.t());
           }
         }
       }
@@ -521,8 +532,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const TileCtx c = tile_ctx<G>(P, tile);
         const int gm = merge_count(c, P, EST);
+        PairIter pr;
+        pr.start(P.slices);
         for (int u = 0; u < c.n_pairs && ok; ++ai) {
-          const int u_end = group_end(u, c.n_pairs, gm, P.slices, c.kchunks);
+          const int g = group_size(pr, gm, c.kchunks);
           // One accumulator (TMEM columns 0..255) or two (0..127, 128..255,
           // grouped launches), used in turn; the epilogue frees one as soon
           // as it has copied it to registers.
@@ -531,8 +544,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
           tc_fence_after();
           const uint32_t d_tmem = tmem_base + (uint32_t)(buf * Geo::BN);
-          for (int uu = u; uu < u_end && ok; ++uu) {
-            const PairOf pr = pair_of(uu, P.slices, c.kchunks);
+          for (int j = 0; j < g && ok; ++j, pr.next(c.kchunks)) {
             const int kb0 = pr.chunk * (P.kchunk / OZ_BK);
             int kb1 = kb0 + P.kchunk / OZ_BK;
             if (kb1 > c.kblocks) kb1 = c.kblocks;
@@ -546,14 +558,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
               for (int kk = 0; kk < OZ_BK / 16; ++kk) {
                 tc_mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
-                            Geo::IDESC, (uu > u || kb > kb0 || kk > 0) ? 1u : 0u);
+                            Geo::IDESC, (j > 0 || kb > kb0 || kk > 0) ? 1u : 0u);
               }
               tc_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
           }
           if (!ok) break;
           tc_commit(&accf[buf]);  // accumulator ready once every MMA above completes
-          u = u_end;
+          u += g;
         }
       }
       // Make sure no MMA is still running before TMEM is released.
@@ -583,8 +595,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const bool row_ok = row < tc.m;
       const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
       const float ra = row_ok ? P.ra[row] : 0.0f;
-      for (int u = 0; u < tc.n_pairs; ++u, ++ai) {
-        const PairOf pr = pair_of(u, P.slices, 1);
+      PairIter pr;
+      pr.start(P.slices);
+      for (int u = 0; u < tc.n_pairs; ++u, ++ai, pr.next(1)) {
         if (!bounded(&accf[0], ai & 1, 4)) { ok = false; break; }
         tc_fence_after();
         uint32_t v[OZ_BN / 2];
@@ -594,7 +607,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acce[0]);
-        if (pr.s + pr.t == 1) {
+        if (pr.d == 1) {
 #pragma unroll
           for (int c = 0; c < OZ_BN / 32; ++c) {
             uint32_t w[16];
@@ -651,23 +664,28 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     // element, R (TMEM columns 256..383), runs over the diagonals from
     // d = S-1 (least significant) to d = 0. Moving from diagonal d+1 to d,
     // R <- floor(R / 2^b) + D_d and the low b bits of the old R are final:
-    // they go, one byte per diagonal, into this CTA's digit slot
-    // (write-only). After d = 0,
-    //   T = R 2^(b(S-1)) + sum_i digit_i 2^(bi)   (digit i from d = S-1-i)
+    // digit S-2-d. After d = 0,
+    //   T = R 2^(b(S-1)) + sum_t digit_t 2^(bt)
     // is the exact sum of D_d 2^(b(S-1-d)), converted once to f64.
     // |R| < 2^31: |D_d| <= 120 * 2^24 (host limit on K chunks x S) and the
     // carry adds at most |R| / 2^b + 1.
+    // Digits are kept one byte each, four to a word per element: digits
+    // 0..3 in a register word that moves to TMEM columns 384..511 once full,
+    // digits 4..7 in the register word after it, digits 8..14 (S > 9 only)
+    // in this CTA's slot of 8-byte records in global memory.
     constexpr int BN = Geo::BN;
     constexpr size_t kColPitch = (size_t)OZ_BM * OZ_DIGIT_BYTES;  // slot bytes per tile column
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16);
-    const uint32_t dsum_t = lane_base + 2 * BN;
-    const int b = P.digit_bits, S = P.slices;
+    const uint32_t dsum_t = lane_base + 2 * BN;  // R
+    const uint32_t dig_t = lane_base + 3 * BN;   // digits 0..3
+    const int b = P.digit_bits, S = P.slices, nd = S - 1;
     const uint32_t dmask = (1u << b) - 1;
     uint8_t* const slot = reinterpret_cast<uint8_t*>(P.acc) + (size_t)blockIdx.x * (kColPitch * BN) +
                           (size_t)row_in_tile * OZ_DIGIT_BYTES;
+    uint32_t dreg[BN / 2];  // this thread's digit word per element (chunk i, column e: [i * 16 + e])
     uint32_t ai = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
@@ -679,69 +697,93 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (nch < 0 || tc.row0 + q * 32 >= tc.m) nch = 0;
       const int ecol_base = row_ok ? tc.ea[row] + P.final_shift : 0;
       const int gm = merge_count(tc, P, false);
-      int prev_d = -1;
-      for (int u = 0, u_end = 0; u < tc.n_pairs; u = u_end, ++ai) {
-        u_end = group_end(u, tc.n_pairs, gm, S, tc.kchunks);
-        const int d = diag_of(u, S, tc.kchunks);
-        const bool diag_start = d != prev_d;
-        prev_d = d;
-        const bool final_group = u_end == tc.n_pairs;  // the last group of d = 0
+#pragma unroll
+      for (int e = 0; e < BN / 2; ++e) dreg[e] = 0;  // (no value survives a tile)
+      PairIter pr;
+      pr.start(S);
+      int last_buf = 0;
+      for (int u = 0; u < tc.n_pairs && ok; ++ai) {
+        const int g = group_size(pr, gm, tc.kchunks);
+        const int d = pr.d;
+        const bool diag_start = pr.diag_first();
+        const bool tile_first = u == 0;
+        u += g;
+        for (int j = 0; j < g; ++j) pr.next(tc.kchunks);
+        const bool final_group = u == tc.n_pairs;  // the last group of d = 0
         const int buf = (int)(ai & 1);
         if (!bounded(&accf[buf], (ai >> 1) & 1, 4)) { ok = false; break; }
         tc_fence_after();
         // Chunk by chunk: the accumulator and R in flight together, R
         // updated and stored back; the accumulator goes back to the MMA warp
         // after the last chunk is read (the other one is in use meanwhile).
-        const int dig_i = S - 2 - d;  // digit index of diagonal d + 1
+        const int dig_i = nd - 1 - d;  // digit index of diagonal d + 1
+        const int dsh = 8 * (dig_i & 3);
 #pragma unroll
         for (int i = 0; i < BN / 32; ++i) {
           if (i >= nch) continue;
           const int col_t = (2 * i + half) * 16;
           uint32_t v[16], w[16];
           tmem_ld16_nowait(lane_base + buf * BN + col_t, v);
-          if (u != 0) tmem_ld16_nowait(dsum_t + col_t, w);
+          if (!tile_first) tmem_ld16_nowait(dsum_t + col_t, w);
           tmem_wait_ld();
-          if (u == 0) {
+          if (tile_first) {
 #pragma unroll
             for (int e = 0; e < 16; ++e) w[e] = (uint32_t)__float2int_rn(__uint_as_float(v[e]));
           } else if (diag_start) {
-            uint8_t* sp = slot + (size_t)col_t * kColPitch + dig_i;
 #pragma unroll
             for (int e = 0; e < 16; ++e) {
               const int32_t r = (int32_t)w[e];
-              if (row_ok && col_t + e < ncols) sp[(size_t)e * kColPitch] = (uint8_t)((uint32_t)r & dmask);
+              const uint32_t dg = (uint32_t)r & dmask;
+              if (dig_i < 8) {
+                dreg[i * 16 + e] = (dsh ? dreg[i * 16 + e] : 0u) | dg << dsh;
+              } else if (row_ok && col_t + e < ncols) {
+                slot[(size_t)(col_t + e) * kColPitch + (dig_i - 8)] = (uint8_t)dg;
+              }
               w[e] = (uint32_t)((r >> b) + __float2int_rn(__uint_as_float(v[e])));
             }
+            if (dig_i == 3) tmem_st16(dig_t + col_t, *reinterpret_cast<const uint32_t(*)[16]>(dreg + i * 16));
           } else {
 #pragma unroll
             for (int e = 0; e < 16; ++e) w[e] = (uint32_t)((int32_t)w[e] + __float2int_rn(__uint_as_float(v[e])));
           }
           tmem_st16(dsum_t + col_t, w);
+          // The last group parks the register digit word in TMEM for the
+          // retire pass below: digits 4..7 in this accumulator's columns
+          // (held until then), or digits 0..S-2 in 384..511 when S <= 5.
+          if (final_group)
+            tmem_st16(nd > 4 ? lane_base + buf * BN + col_t : dig_t + col_t,
+                      *reinterpret_cast<const uint32_t(*)[16]>(dreg + i * 16));
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&acce[buf]);
+        if (!final_group) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acce[buf]);
+        }
         tmem_wait_st();
-        // After the last group of d = 0: read R back, combine it with the
-        // digit records, convert, write C.
-#pragma unroll
-        for (int i = 0; i < BN / 32; ++i) {
-          if (!final_group || i >= nch) continue;
-          const int col_t = (2 * i + half) * 16;
-          uint32_t w[16];
-          tmem_ld16(dsum_t + col_t, w);
-          if (!row_ok) continue;
-          const uint8_t* rec = slot + (size_t)col_t * kColPitch;
-          const int* eb = tc.eb + tc.col0 + col_t;
-          double* crow = tc.C + row * tc.ldc + tc.col0 + col_t;
-          if (S <= 9)
-            retire_chunk<false>(w, rec, kColPitch, eb, ncols - col_t, b, S, ecol_base, crow, tc.accumulate);
-          else
-            retire_chunk<true>(w, rec, kColPitch, eb, ncols - col_t, b, S, ecol_base, crow, tc.accumulate);
-        }
-        tc_fence_before();
-        __syncwarp();
+        last_buf = buf;
       }
+      if (!ok) break;
+      // After the last group of d = 0 (whose accumulator is still held): read
+      // R and the digit words back, add the digits 8.. of the records,
+      // convert, write C, then free the accumulator.
+#pragma unroll 1
+      for (int i = 0; i < nch; ++i) {
+#pragma unroll
+        for (int h8 = 0; h8 < 16; h8 += 8) {
+          const int col_t = (2 * i + half) * 16 + h8;
+          uint32_t w[8], lw[8], hw[8];
+          tmem_ld8_nowait(dsum_t + col_t, w);
+          tmem_ld8_nowait(dig_t + col_t, lw);
+          if (nd > 4) tmem_ld8_nowait(lane_base + last_buf * BN + col_t, hw);
+          tmem_wait_ld();
+          if (!row_ok) continue;
+          retire8(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, tc.eb + tc.col0 + col_t, ncols - col_t,
+                  b, S, ecol_base, tc.C + row * tc.ldc + tc.col0 + col_t, tc.accumulate);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[last_buf]);
     }
   } else {
     // ---------------- epilogue (warps 2..9) ----------------
@@ -761,19 +803,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t dsum_t = lane_base + OZ_BN;  // diagonal-sum columns
     uint32_t ai = 0;
     bool ok = true;
-    int prev_d = -1;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
       const TileCtx tc = tile_ctx<G>(P, tile);
       const int64_t row = tc.row0 + row_in_tile;
       const bool row_ok = row < tc.m;
       const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
-      prev_d = -1;
       const int gm = merge_count(tc, P, false);
-      for (int u = 0, u_end = 0; u < tc.n_pairs; u = u_end, ++ai) {
-        u_end = group_end(u, tc.n_pairs, gm, P.slices, tc.kchunks);
-        const int d = diag_of(u, P.slices, tc.kchunks);
-        const bool diag_start = (d != prev_d);
-        prev_d = d;
+      PairIter pr;
+      pr.start(P.slices);
+      for (int u = 0; u < tc.n_pairs; ++ai) {
+        const int g = group_size(pr, gm, tc.kchunks);
+        const int d = pr.d;
+        const bool diag_start = pr.diag_first();
+        const bool diag_end = g == pr.left(tc.kchunks);  // the group closes its diagonal
+        u += g;
+        for (int j = 0; j < g; ++j) pr.next(tc.kchunks);
         const uint32_t aph = ai & 1;
         if (!bounded(&accf[0], aph, 4)) { ok = false; break; }
         tc_fence_after();
@@ -807,8 +851,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tmem_wait_st();
         tc_fence_before();
         __syncwarp();
-        // Is this the last unit of its diagonal?
-        const bool diag_end = (u_end == tc.n_pairs) || diag_of(u_end, P.slices, tc.kchunks) != d;
         if (!diag_end) continue;
         const bool first = (d == P.slices - 1), last = (d == 0);
         const int shift = P.digit_bits * (P.slices - 1 - d);
