@@ -1,0 +1,139 @@
+// The grouped Ozaki epilogue's exact total of a C element and its 128-bit
+// integer to f64 conversion, written for host and device alike so that the
+// CPU tests check the same code the kernels run.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define NRS_HD __host__ __device__ __forceinline__
+#else
+#define NRS_HD inline
+#endif
+
+NRS_HD int nrs_clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
+NRS_HD double nrs_f64_from_bits(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// (-1)^neg (mhi:mlo) 2^e rounded to nearest (ties to even), the f64 bit
+// pattern assembled with integer operations: GB300's FP64 pipe runs a few
+// operations per clock per SM, which a per-element int-to-double conversion
+// and scaling would saturate. Subnormal results take an exact 128-bit
+// shift-and-round path; overflow gives infinity.
+NRS_HD double int128_to_f64(bool neg, uint64_t mhi, uint64_t mlo, int e) {
+  const uint64_t sign = (uint64_t)neg << 63;
+  if ((mhi | mlo) == 0) return nrs_f64_from_bits(sign);
+  int p;           // position of the leading one
+  uint64_t top;    // the 64 bits from the leading one down, left-aligned
+  bool below;      // any one bit below those 64
+  if (mhi) {
+    const int lz = nrs_clz64(mhi);
+    p = 127 - lz;
+    top = lz ? (mhi << lz) | (mlo >> (64 - lz)) : mhi;
+    below = (lz ? mlo << lz : mlo) != 0;
+  } else {
+    const int lz = nrs_clz64(mlo);
+    p = 63 - lz;
+    top = mlo << lz;
+    below = false;
+  }
+  const int be = p + e + 1023;  // biased exponent of the leading one
+  if (be > 0) {
+    uint64_t mant = top >> 11;  // 53 bits
+    const bool rnd = (top >> 10) & 1, sticky = (top & 0x3FF) != 0 || below;
+    int pe = be;
+    if (rnd && (sticky || (mant & 1))) {
+      if (++mant >> 53) {
+        mant >>= 1;
+        ++pe;
+      }
+    }
+    if (pe >= 2047) return nrs_f64_from_bits(sign | 0x7FF0000000000000ULL);
+    return nrs_f64_from_bits(sign | (uint64_t)pe << 52 | (mant & 0xFFFFFFFFFFFFFull));
+  }
+  // subnormal (or zero after rounding): the value in units of 2^-1074
+  const unsigned __int128 m = (unsigned __int128)mhi << 64 | mlo;
+  const int sh = -(e + 1074);  // right shift onto the subnormal grid
+  uint64_t q;
+  if (sh <= 0) {
+    q = (uint64_t)(m << -sh);  // exact: below 2^52 here
+  } else if (sh >= 128) {
+    q = sh == 128 && m > ((unsigned __int128)1 << 127) ? 1 : 0;  // at most one unit
+  } else {
+    q = (uint64_t)(m >> sh);
+    const unsigned __int128 rem = m & (((unsigned __int128)1 << sh) - 1), half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) ++q;
+  }
+  return nrs_f64_from_bits(sign | q);
+}
+
+// The same conversion without branches for the common case, so that several
+// elements' operation chains interleave: returns the f64 bits when the
+// magnitude is nonzero and the result normal and finite; otherwise sets
+// `special` (the caller then uses int128_to_f64).
+NRS_HD uint64_t int128_to_f64_bits_fast(bool neg, uint64_t mhi, uint64_t mlo, int e, bool& special) {
+  const bool hz = mhi == 0;
+  const uint64_t x = hz ? mlo : mhi;
+  const int lz = nrs_clz64(x | 1);  // (x = 0 is special below)
+  const int p = (hz ? 63 : 127) - lz;
+  const uint64_t hi_part = (mhi << lz) | ((mlo >> 1) >> (63 - lz));
+  const uint64_t top = hz ? mlo << lz : hi_part;
+  const uint64_t below = hz ? 0 : mlo << lz;
+  uint64_t mant = top >> 11;
+  const uint64_t rnd = (top >> 10) & 1;
+  const uint64_t sticky = ((top & 0x3FF) | below) != 0;
+  mant += rnd & (sticky | (mant & 1));
+  const uint64_t carry = mant >> 53;
+  mant >>= carry;
+  const int pe = p + e + 1023 + (int)carry;
+  special = (x == 0) | (pe <= 0) | (pe >= 2047);
+  return (uint64_t)neg << 63 | (uint64_t)(pe & 0x7FF) << 52 | (mant & 0xFFFFFFFFFFFFFull);
+}
+
+// The exact total T = R 2^(b(S-1)) + sum_t digit_t 2^(bt) of a grouped Ozaki
+// element (R: the carried int32 sum, digit t = byte t of lo | hi << 64,
+// digits below 2^b) as sign and 128-bit magnitude. For b = 8 the digits are
+// the bytes themselves: T = R 2^(8(S-1)) + (the record's low 8(S-1) bits),
+// straight-line; other widths fold them in by Horner's rule,
+// T = ((R 2^b + digit_{S-2}) 2^b + ...) 2^b + digit_0.
+NRS_HD void ozaki_exact_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S, bool& neg, uint64_t& mhi,
+                              uint64_t& mlo) {
+  const int nd = S - 1;
+  const uint64_t r64 = (uint64_t)(int64_t)R;
+  const uint64_t high = (uint64_t)((int64_t)R >> 63);
+  uint64_t th, tl;
+  if (b == 8) {
+    const int sh = 8 * nd;  // 0..112
+    const bool small = sh < 64;
+    const int s1 = small ? sh : 0, s2 = small ? 0 : sh - 64;
+    const uint64_t lmask = (~0ull >> 1) >> (63 - s1);  // the low s1 bits
+    const uint64_t hmask = (~0ull >> 1) >> (63 - s2);  // the low s2 bits
+    tl = small ? (r64 << s1) | (lo & lmask) : lo;
+    th = small ? (high << s1) | ((r64 >> 1) >> (63 - s1)) : (r64 << s2) | (hi & hmask);
+  } else {
+    th = high;
+    tl = r64;
+    for (int t = nd - 1; t >= 0; --t) {
+      const uint64_t dg = (t < 8 ? lo >> (8 * t) : hi >> (8 * (t - 8))) & 0xFF;
+      th = (th << b) | (tl >> (64 - b));
+      tl = (tl << b) | dg;
+    }
+  }
+  neg = (int64_t)th < 0;
+  mlo = neg ? ~tl + 1 : tl;
+  mhi = neg ? ~th + (tl == 0 ? 1 : 0) : th;
+}

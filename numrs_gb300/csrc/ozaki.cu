@@ -53,6 +53,7 @@
 #include <string>
 #include <vector>
 
+#include "f64_round.cuh"
 #include "nrs_internal.cuh"
 
 namespace {
@@ -89,7 +90,10 @@ struct OzGeom {
   static constexpr int B_BYTES = BN * OZ_BK * 2;
   static constexpr int STAGE_BYTES = OZ_A_BYTES + B_BYTES;
   static constexpr int ACC_BUFS = G ? 2 : 1;
-  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+  // Grouped epilogue: the column exponents of each epilogue warp's 64 tile
+  // columns, staged once per tile.
+  static constexpr int EB_BYTES = G ? 8 * 64 * 4 : 0;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + EB_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   // Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16
   // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
   // 17-22, M >> 4 at bits 24-28.
@@ -312,72 +316,19 @@ __device__ __forceinline__ int group_size(const PairIter& pi, int gm, int kchunk
   return l < gm ? l : gm;
 }
 
-// x 2^e for an integer-valued x in [0, 2^64], rounded once: one multiply by
-// an exact power of two, with a pre-scale by 2^1023 or 2^-1022 (exact for
-// such x) when e lies outside the normal exponent range.
-__device__ __forceinline__ double scale_pow2(double x, int e) {
-  if (e > 1023) {
-    x *= 0x1p1023;
-    e -= 1023;
-    if (e > 1023) e = 1023;
-  } else if (e < -1022) {
-    x *= 0x1p-1022;
-    e += 1022;
-    if (e < -1022) e = -1022;
-  }
-  return x * __longlong_as_double((long long)(e + 1023) << 52);
-}
 
-// f64 value of the exact total T = R 2^(b(S-1)) + sum_t digit_t 2^(bt)
-// (digit t = byte t of the record lo | hi << 64) times 2^e: T as a 128-bit
-// two's complement (th, tl), its top 64 significant bits converted once.
-__device__ __forceinline__ double retire_value(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int e) {
-  const int nd = S - 1;
-  int64_t th;
-  uint64_t tl;
-  if (b == 8) {
-    // the digits are the record's bytes: T = R 2^(8 nd) + (record mod 2^(8 nd))
-    const int sh = 8 * nd;
-    if (sh < 64) {
-      tl = ((uint64_t)(int64_t)R << sh) | (sh ? lo & (~0ull >> (64 - sh)) : 0);
-      th = sh ? (int64_t)R >> (64 - sh) : (int64_t)R >> 63;
-    } else {
-      tl = lo;
-      th = (int64_t)(((uint64_t)(int64_t)R << (sh - 64)) | (sh > 64 ? hi & (~0ull >> (128 - sh)) : 0));
-    }
-  } else {
-    // Horner: T = ((R 2^b + digit_{nd-1}) 2^b + ...) 2^b + digit_0; each
-    // digit fills the b zero bits the shift leaves.
-    th = (int64_t)R >> 63;
-    tl = (uint64_t)(int64_t)R;
-#pragma unroll 1
-    for (int t = nd - 1; t >= 0; --t) {
-      const uint64_t dg = (t < 8 ? lo >> (8 * t) : hi >> (8 * (t - 8))) & 0xFF;
-      th = (int64_t)(((uint64_t)th << b) | (tl >> (64 - b)));
-      tl = (tl << b) | dg;
-    }
-  }
-  const bool neg = th < 0;
-  uint64_t mhi = (uint64_t)th, mlo = tl;
-  if (neg) {
-    mlo = ~mlo + 1;
-    mhi = ~mhi + (mlo == 0 ? 1 : 0);
-  }
-  const int sh = mhi ? 64 - __clzll((long long)mhi) : 0;
-  const uint64_t top = sh == 0 ? mlo : sh == 64 ? mhi : (mhi << (64 - sh)) | (mlo >> sh);
-  const double v = scale_pow2((double)top, sh + e);
-  return neg ? -v : v;
-}
-
-// Writes 8 consecutive columns of one tile row: R values w, digits 0..3 (lw)
-// and 4..7 (hw, S > 5 only) as words per column, digits 8..14 from the
-// 8-byte records `pitch` apart (S > 9 only) and the column exponents; `left`
-// of the 8 columns lie inside the problem.
+// Writes 8 consecutive columns of one tile row: R values w, digit words per
+// column (S <= 5: digits 0..S-2 in lw; else digits 0..3 in lw and 4..7 in
+// hw), digits 8..14 from the 8-byte records `pitch` apart (S > 9 only) and
+// the column exponents; `left` of the 8 columns lie inside the problem. The
+// conversions run straight-line for all 8 (interleaved); zero, subnormal and
+// overflowing results are redone by the exact path.
 __device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (&lw)[8], const uint32_t (&hw)[8],
                                         const uint8_t* rec, size_t pitch, const int* eb, int left, int b, int S,
                                         int ebase, double* crow, bool accumulate) {
-  uint64_t hi[8];
+  uint64_t hi[8], bits[8];
   int ex[8];
+  unsigned special = 0;
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     hi[e] = 0;
@@ -389,9 +340,28 @@ __device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (
   }
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
-    if (e >= left) continue;
     const uint64_t lo = S - 1 > 4 ? (uint64_t)lw[e] | (uint64_t)hw[e] << 32 : (uint64_t)lw[e];
-    const double r = retire_value((int32_t)w[e], lo, hi[e], b, S, ebase + ex[e]);
+    bool neg, sp;
+    uint64_t mhi, mlo;
+    ozaki_exact_total((int32_t)w[e], lo, hi[e], b, S, neg, mhi, mlo);
+    bits[e] = int128_to_f64_bits_fast(neg, mhi, mlo, ebase + ex[e], sp);
+    special |= (unsigned)sp << e;
+  }
+  if (special) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      if (!((special >> e) & 1)) continue;
+      const uint64_t lo = S - 1 > 4 ? (uint64_t)lw[e] | (uint64_t)hw[e] << 32 : (uint64_t)lw[e];
+      bool neg;
+      uint64_t mhi, mlo;
+      ozaki_exact_total((int32_t)w[e], lo, hi[e], b, S, neg, mhi, mlo);
+      bits[e] = (uint64_t)__double_as_longlong(int128_to_f64(neg, mhi, mlo, ebase + ex[e]));
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    if (e >= left) continue;
+    const double r = __longlong_as_double((long long)bits[e]);
     crow[e] = accumulate ? crow[e] + r : r;
   }
 }
@@ -449,7 +419,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   using Geo = OzGeom<G>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Geo::STAGES * Geo::STAGE_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Geo::STAGES * Geo::STAGE_BYTES + Geo::EB_BYTES);
   uint64_t* empty = full + Geo::STAGES;
   uint64_t* accf = empty + Geo::STAGES;
   uint64_t* acce = accf + 2;
@@ -538,7 +508,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const int g = group_size(pr, gm, c.kchunks);
           // One accumulator (TMEM columns 0..255) or two (0..127, 128..255,
           // grouped launches), used in turn; the epilogue frees one as soon
-          // as it has copied it to registers.
+          // as it has read it.
           const int buf = Geo::ACC_BUFS == 2 ? (int)(ai & 1) : 0;
           const uint32_t aph = (Geo::ACC_BUFS == 2 ? ai >> 1 : ai) & 1;
           if (!bounded(&acce[buf], aph ^ 1, 2)) { ok = false; break; }
@@ -686,6 +656,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     uint8_t* const slot = reinterpret_cast<uint8_t*>(P.acc) + (size_t)blockIdx.x * (kColPitch * BN) +
                           (size_t)row_in_tile * OZ_DIGIT_BYTES;
     uint32_t dreg[BN / 2];  // this thread's digit word per element (chunk i, column e: [i * 16 + e])
+    // this warp's column exponents, [i * 16 + e] for chunk i, column e
+    int* const sm_eb = reinterpret_cast<int*>(smem + Geo::STAGES * Geo::STAGE_BYTES) + (warp - 2) * 64;
     uint32_t ai = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
@@ -696,6 +668,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       int nch = (ncols - 16 * half + 31) / 32;  // chunks of this warp inside the problem
       if (nch < 0 || tc.row0 + q * 32 >= tc.m) nch = 0;
       const int ecol_base = row_ok ? tc.ea[row] + P.final_shift : 0;
+      // Column exponents of this warp's columns j = lane, lane + 32 (chunk
+      // j / 16, column j % 16): loaded now, used by the retire pass at the
+      // end of the tile (their latency hides behind the tile's groups).
+      int ebj[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int j = lane + 32 * t;
+        const int64_t col = tc.col0 + (2 * (j >> 4) + half) * 16 + (j & 15);
+        ebj[t] = col < tc.n ? tc.eb[col] : 0;
+      }
       const int gm = merge_count(tc, P, false);
 #pragma unroll
       for (int e = 0; e < BN / 2; ++e) dreg[e] = 0;  // (no value survives a tile)
@@ -766,6 +748,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       // After the last group of d = 0 (whose accumulator is still held): read
       // R and the digit words back, add the digits 8.. of the records,
       // convert, write C, then free the accumulator.
+      sm_eb[lane] = ebj[0];
+      sm_eb[lane + 32] = ebj[1];
+      __syncwarp();
 #pragma unroll 1
       for (int i = 0; i < nch; ++i) {
 #pragma unroll
@@ -777,12 +762,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (nd > 4) tmem_ld8_nowait(lane_base + last_buf * BN + col_t, hw);
           tmem_wait_ld();
           if (!row_ok) continue;
-          retire8(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, tc.eb + tc.col0 + col_t, ncols - col_t,
-                  b, S, ecol_base, tc.C + row * tc.ldc + tc.col0 + col_t, tc.accumulate);
+          retire8(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, sm_eb + i * 16 + h8, ncols - col_t, b, S,
+                  ecol_base, tc.C + row * tc.ldc + tc.col0 + col_t, tc.accumulate);
         }
       }
       tc_fence_before();
-      __syncwarp();
+      __syncwarp();  // (also: sm_eb is rewritten by the next tile only after this)
       if (lane == 0) mbar_arrive(&acce[last_buf]);
     }
   } else {
@@ -875,17 +860,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             if (!last) {
               *ap = sum;
             } else {
-              // |sum| < 2^127: keep its top 64 significant bits, convert once.
+              // |sum| < 2^127: rounded once to f64.
               const bool neg = sum < 0;
-              unsigned __int128 mag = neg ? (unsigned __int128)(-sum) : (unsigned __int128)sum;
-              const uint64_t hi = (uint64_t)(mag >> 64);
-              int sh = 0;
-              if (hi) sh = 64 - __clzll((long long)hi);
-              const uint64_t top = (uint64_t)(mag >> sh);
-              double val = (double)top;
-              val = ldexp(val, sh + ecol_base + tc.eb[col]);
+              const unsigned __int128 mag = neg ? (unsigned __int128)(-sum) : (unsigned __int128)sum;
+              const double r = int128_to_f64(neg, (uint64_t)(mag >> 64), (uint64_t)mag, ecol_base + tc.eb[col]);
               double* cp = tc.C + row * tc.ldc + col;
-              const double r = neg ? -val : val;
               *cp = tc.accumulate ? *cp + r : r;
             }
           }

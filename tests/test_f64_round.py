@@ -1,0 +1,136 @@
+"""The grouped Ozaki epilogue's exact element total and its 128-bit integer
+-> f64 conversion (numrs_gb300/csrc/f64_round.cuh, host/device code),
+compiled for the host with g++: the exact path and the straight-line fast
+path against exact rational rounding (round to nearest, ties to even) over
+random magnitudes and scales, ties, carries into the next binade, overflow
+to infinity and the subnormal range; the total T = R 2^(b(S-1)) +
+sum_t digit_t 2^(bt) against Python integers for every digit width."""
+import ctypes
+import os
+import random
+import shutil
+import struct
+import subprocess
+from fractions import Fraction
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HDR = os.path.join(HERE, "..", "numrs_gb300", "csrc", "f64_round.cuh")
+
+HARNESS = r"""
+#include "f64_round.cuh"
+extern "C" double nrs_test_int128_to_f64(uint64_t hi, uint64_t lo, int e, int neg) {
+  return int128_to_f64(neg != 0, hi, lo, e);
+}
+extern "C" uint64_t nrs_test_fast(uint64_t hi, uint64_t lo, int e, int neg, int* special) {
+  bool sp = false;
+  const uint64_t r = int128_to_f64_bits_fast(neg != 0, hi, lo, e, sp);
+  *special = sp;
+  return r;
+}
+extern "C" void nrs_test_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int* neg, uint64_t* mhi,
+                               uint64_t* mlo) {
+  bool n = false;
+  ozaki_exact_total(R, lo, hi, b, S, n, *mhi, *mlo);
+  *neg = n;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("f64round")
+    src, so = d / "h.cpp", d / "h.so"
+    src.write_text(HARNESS)
+    subprocess.run([cxx, "-O2", "-shared", "-fPIC", "-I", os.path.dirname(HDR), str(src), "-o", str(so)],
+                   check=True, capture_output=True)
+    return ctypes.CDLL(str(so))
+
+
+@pytest.fixture(scope="module")
+def conv(lib):
+    f = lib.nrs_test_int128_to_f64
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+    return lambda m, e, neg: f(m >> 64, m & ((1 << 64) - 1), e, neg)
+
+
+def _exact(m, e, neg):
+    if m == 0:
+        return -0.0 if neg else 0.0
+    try:
+        v = float(Fraction(m) * Fraction(2) ** e)
+    except OverflowError:
+        v = float("inf")
+    return -v if neg else v
+
+
+def _cases():
+    r = random.Random(5)
+    out = []
+    for _ in range(60000):
+        bits = r.randint(0, 128)
+        m = r.getrandbits(bits) if bits else r.randint(0, 3)
+        e = r.choice([r.randint(-200, 200), r.randint(-1250, -1000), r.randint(900, 1100)])
+        out.append((m, e, r.randint(0, 1)))
+    for k in range(54, 128):
+        base = 1 << k
+        for e in (-1100, -1074, -1022 - k, -1023 - k, 0, 1023 - k, 1024 - k):
+            for m in (base | (1 << (k - 53)), base | (3 << (k - 54)), (1 << (k + 1)) - 1,
+                      base | (1 << (k - 53)) | 1, base + (1 << (k - 53)) - 1):
+                out += [(m, e, 0), (m, e, 1)]
+    out += [((1 << 127) + 1, -1202, 0), (1 << 127, -1202, 0), ((1 << 128) - 1, -1202, 1)]
+    return out
+
+
+def test_int128_to_f64_rounds_exactly(conv):
+    bad = []
+    for m, e, neg in _cases():
+        got, want = conv(m, e, neg), _exact(m, e, neg)
+        if not (got == want and repr(got) == repr(want)):
+            bad.append((hex(m), e, neg, got, want))
+    assert not bad, bad[:5]
+
+
+def test_fast_path_matches_exact_or_defers(lib, conv):
+    """The straight-line path gives the exact path's bits, or flags the
+    element (zero, subnormal, overflow) for it."""
+    f = lib.nrs_test_fast
+    f.restype = ctypes.c_uint64
+    f.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    sp = ctypes.c_int()
+    n_fast = 0
+    for m, e, neg in _cases():
+        bits = f(m >> 64, m & ((1 << 64) - 1), e, neg, ctypes.byref(sp))
+        if sp.value:
+            continue
+        n_fast += 1
+        want = struct.unpack("<Q", struct.pack("<d", _exact(m, e, neg)))[0]
+        assert bits == want, (hex(m), e, neg, hex(bits), hex(want))
+    assert n_fast > 30000  # the rest: zero, subnormal or overflowing (a third of the mix)
+
+
+@pytest.mark.parametrize("b", [8, 7, 6])
+def test_exact_total_every_width(lib, b):
+    f = lib.nrs_test_total
+    f.restype = None
+    f.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    r = random.Random(b)
+    neg, mhi, mlo = ctypes.c_int(), ctypes.c_uint64(), ctypes.c_uint64()
+    for S in range(1, 17):
+        if b * (S - 1) > 95:
+            continue
+        for _ in range(400):
+            R = r.choice([r.randint(-(1 << 31), (1 << 31) - 1), r.randint(-3, 3)])
+            digits = [r.randrange(1 << b) for _ in range(S - 1)]
+            rec = sum(d << (8 * t) for t, d in enumerate(digits))
+            rec |= r.getrandbits(128) >> (8 * (S - 1)) << (8 * (S - 1)) if S - 1 < 16 else 0  # junk above
+            T = R * (1 << (b * (S - 1))) + sum(d << (b * t) for t, d in enumerate(digits))
+            f(R, rec & ((1 << 64) - 1), rec >> 64, b, S, ctypes.byref(neg), ctypes.byref(mhi), ctypes.byref(mlo))
+            got = (mhi.value << 64 | mlo.value) * (-1 if neg.value else 1)
+            assert got == T and bool(neg.value) == (T < 0), (b, S, R, digits)
