@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define NRS_ABI_VERSION 2
+#define NRS_ABI_VERSION 3
 
 typedef struct nrs_handle nrs_handle;
 
@@ -453,12 +453,21 @@ typedef struct nrs_plan nrs_plan;
  * f64_digit_bits 0 = the widest digits the group's K allows, or 6..8. The
  * slice count is fixed when the plan is created: replaying it on data whose
  * magnitudes are spread wider than at creation loses accuracy -- create the
- * plan again (or give a count) when the data's range changes. */
+ * plan again (or give a count) when the data's range changes.
+ * f32_mode NRS_PLAN_F32_FMA (0): f32 GEMMs run as FP32 FMA tiles of the
+ * persistent kernel. NRS_PLAN_F32_OZAKI (1): row-major f32 GEMMs run as a
+ * second grouped launch of the same scheme, each operand carried to
+ * 26 + log2(max R) bits (f32's 24 and two guard bits; the slice count is
+ * measured when the plan is created), the exact sums rounded once to f32:
+ * max_ij |C - AB|_ij / (|A||B|)_ij stays near 2^-24 for any K, where the
+ * FMA tiles' sequential f32 sum grows with K. */
 typedef enum nrs_plan_f64_mode { NRS_PLAN_F64_DMMA = 0, NRS_PLAN_F64_OZAKI = 1 } nrs_plan_f64_mode;
+typedef enum nrs_plan_f32_mode { NRS_PLAN_F32_FMA = 0, NRS_PLAN_F32_OZAKI = 1 } nrs_plan_f32_mode;
 typedef struct nrs_plan_options {
   int32_t f64_mode;
   int32_t f64_slices;
   int32_t f64_digit_bits;
+  int32_t f32_mode;
 } nrs_plan_options;
 
 /* Builds the tile/work queue for `n_gemm` GEMMs and `n_red` row reductions
@@ -472,8 +481,11 @@ int nrs_plan_create_ex(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms
 /* f64 GEMMs the plan runs on the tensor cores, with their slice count and
  * digit width (0, 0, 0 for a DMMA-only plan). */
 int nrs_plan_f64_info(nrs_plan* plan, int64_t* on_tensor_cores, int* slices, int* digit_bits);
+/* The same for the plan's f32 GEMMs (NRS_PLAN_F32_OZAKI). */
+int nrs_plan_f32_info(nrs_plan* plan, int64_t* on_tensor_cores, int* slices, int* digit_bits);
 /* Runs the whole group as ONE persistent kernel launch (preceded, with
- * NRS_PLAN_F64_OZAKI, by the grouped tensor-core launch of its f64 GEMMs).
+ * NRS_PLAN_F64_OZAKI / NRS_PLAN_F32_OZAKI, by the grouped tensor-core
+ * launches of its f64 / f32 GEMMs).
  * With use_graph != 0
  * the launch is captured once into a CUDA graph owned by the plan and
  * replayed on later calls. */
@@ -503,7 +515,9 @@ int nrs_tune_gemm(nrs_handle* h, int dtype, int64_t m, int64_t k, int64_t n, uns
  * one shape alone. Times (median of `reps` launches after a warm-up) the
  * untuned plan; with `options` f64_mode OZAKI, the f64 GEMMs on the tensor
  * cores at each digit width (the slice count follows from the width at the
- * same accuracy); then every remaining shape bucket tuned in isolation
+ * same accuracy); with `options` f32_mode OZAKI, the f32 GEMMs on the tensor
+ * cores on top of the best of those; then every remaining shape bucket
+ * tuned in isolation
  * (nrs_tune_gemm); and then, from the fastest so far, tries every other
  * variant of the buckets with the most estimated work, keeping a change only
  * if the group gets faster, until `max_trials` group timings. The tile
@@ -520,7 +534,8 @@ typedef struct nrs_autotune_report {
   double ozaki_ms;     /* best tensor-core f64 mode tried (-1 if none)       */
   int32_t buckets;     /* shape buckets tuned                                */
   int32_t trials;      /* whole-group timings in the refinement pass         */
-  nrs_plan_options options; /* the f64 mode / digit width chosen             */
+  nrs_plan_options options; /* the f64 / f32 modes and digit width chosen     */
+  double ozaki_f32_ms; /* with the f32 GEMMs on the tensor cores (-1: not tried) */
 } nrs_autotune_report;
 int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_t n_red,
                       const nrs_rowreduce_desc* reds, const nrs_plan_options* options, int max_trials,

@@ -26,6 +26,7 @@ GEMM_ACCUMULATE, GEMM_TRANS_A, GEMM_TRANS_B = 1, 2, 4
 GEMM_AUTO, GEMM_DMMA, GEMM_SIMT, GEMM_GENERIC, GEMM_SIMT_SMALL = 0, 1, 2, 3, 4
 PEAK_FP64_DMMA, PEAK_FP32_FMA = 0, 1
 PLAN_F64_DMMA, PLAN_F64_OZAKI = 0, 1
+PLAN_F32_FMA, PLAN_F32_OZAKI = 0, 1
 RNG_UNIFORM, RNG_NORMAL, RNG_INT, RNG_OZAKI = 0, 1, 2, 3
 TILE_VARIANTS = 6
 
@@ -47,13 +48,14 @@ class OzakiInfo(C.Structure):
 
 
 class PlanOptions(C.Structure):
-    _fields_ = [("f64_mode", C.c_int32), ("f64_slices", C.c_int32), ("f64_digit_bits", C.c_int32)]
+    _fields_ = [("f64_mode", C.c_int32), ("f64_slices", C.c_int32), ("f64_digit_bits", C.c_int32),
+                ("f32_mode", C.c_int32)]
 
 
 class AutotuneReport(C.Structure):
     _fields_ = [("untuned_ms", C.c_double), ("isolated_ms", C.c_double), ("final_ms", C.c_double),
                 ("ozaki_ms", C.c_double), ("buckets", C.c_int32), ("trials", C.c_int32),
-                ("options", PlanOptions)]
+                ("options", PlanOptions), ("ozaki_f32_ms", C.c_double)]
 
 
 class GemmDesc(C.Structure):
@@ -117,6 +119,7 @@ SIGNATURES = {
     "nrs_plan_create_ex": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
                                 C.POINTER(PlanOptions), C.POINTER(_vp)]),
     "nrs_plan_f64_info": (_i, [_vp, C.POINTER(_i64), C.POINTER(_i), C.POINTER(_i)]),
+    "nrs_plan_f32_info": (_i, [_vp, C.POINTER(_i64), C.POINTER(_i), C.POINTER(_i)]),
     "nrs_gemm_ozaki_grouped": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i, C.POINTER(_i), C.POINTER(OzakiInfo)]),
     "nrs_plan_create": (_i, [_vp, _i64, C.POINTER(GemmDesc), _i64, C.POINTER(RowReduceDesc),
                              C.POINTER(_vp)]),

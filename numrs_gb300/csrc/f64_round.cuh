@@ -1,6 +1,6 @@
 // The grouped Ozaki epilogue's exact total of a C element and its 128-bit
-// integer to f64 conversion, written for host and device alike so that the
-// CPU tests check the same code the kernels run.
+// integer to f64 / f32 conversion, written for host and device alike so that
+// the CPU tests check the same code the kernels run.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -29,17 +29,38 @@ NRS_HD double nrs_f64_from_bits(uint64_t b) {
 #endif
 }
 
-// (-1)^neg (mhi:mlo) 2^e rounded to nearest (ties to even), the f64 bit
-// pattern assembled with integer operations: GB300's FP64 pipe runs a few
-// operations per clock per SM, which a per-element int-to-double conversion
-// and scaling would saturate. Subnormal results take an exact 128-bit
-// shift-and-round path; overflow gives infinity.
-NRS_HD double int128_to_f64(bool neg, uint64_t mhi, uint64_t mlo, int e) {
-  const uint64_t sign = (uint64_t)neg << 63;
-  if ((mhi | mlo) == 0) return nrs_f64_from_bits(sign);
-  int p;           // position of the leading one
-  uint64_t top;    // the 64 bits from the leading one down, left-aligned
-  bool below;      // any one bit below those 64
+NRS_HD float nrs_f32_from_bits(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float f;
+  memcpy(&f, &b, sizeof f);
+  return f;
+#endif
+}
+
+// Binary floating-point formats: WIDTH bits, MANT stored mantissa bits, BIAS
+// exponent bias, EMAX the all-ones biased exponent (infinity).
+struct NrsF64Fmt {
+  static constexpr int WIDTH = 64, MANT = 52, BIAS = 1023, EMAX = 2047;
+};
+struct NrsF32Fmt {
+  static constexpr int WIDTH = 32, MANT = 23, BIAS = 127, EMAX = 255;
+};
+
+// (-1)^neg (mhi:mlo) 2^e rounded to nearest (ties to even) in format F, the
+// bit pattern assembled with integer operations: GB300's FP64 pipe runs a
+// few operations per clock per SM, which a per-element int-to-double
+// conversion and scaling would saturate. Subnormal results take an exact
+// 128-bit shift-and-round path; overflow gives infinity.
+template <typename F>
+NRS_HD uint64_t int128_to_float_bits(bool neg, uint64_t mhi, uint64_t mlo, int e) {
+  constexpr int W = F::WIDTH;
+  const uint64_t sign = (uint64_t)neg << (W - 1);
+  if ((mhi | mlo) == 0) return sign;
+  int p;         // position of the leading one
+  uint64_t top;  // the 64 bits from the leading one down, left-aligned
+  bool below;    // any one bit below those 64
   if (mhi) {
     const int lz = nrs_clz64(mhi);
     p = 127 - lz;
@@ -51,26 +72,28 @@ NRS_HD double int128_to_f64(bool neg, uint64_t mhi, uint64_t mlo, int e) {
     top = mlo << lz;
     below = false;
   }
-  const int be = p + e + 1023;  // biased exponent of the leading one
+  constexpr int DROP = 63 - F::MANT;  // bits of `top` below the mantissa
+  const int be = p + e + F::BIAS;     // biased exponent of the leading one
   if (be > 0) {
-    uint64_t mant = top >> 11;  // 53 bits
-    const bool rnd = (top >> 10) & 1, sticky = (top & 0x3FF) != 0 || below;
+    uint64_t mant = top >> DROP;  // MANT + 1 bits
+    const bool rnd = (top >> (DROP - 1)) & 1, sticky = (top & ((1ull << (DROP - 1)) - 1)) != 0 || below;
     int pe = be;
     if (rnd && (sticky || (mant & 1))) {
-      if (++mant >> 53) {
+      if (++mant >> (F::MANT + 1)) {
         mant >>= 1;
         ++pe;
       }
     }
-    if (pe >= 2047) return nrs_f64_from_bits(sign | 0x7FF0000000000000ULL);
-    return nrs_f64_from_bits(sign | (uint64_t)pe << 52 | (mant & 0xFFFFFFFFFFFFFull));
+    if (pe >= F::EMAX) return sign | (uint64_t)F::EMAX << F::MANT;
+    return sign | (uint64_t)pe << F::MANT | (mant & ((1ull << F::MANT) - 1));
   }
-  // subnormal (or zero after rounding): the value in units of 2^-1074
+  // subnormal (or zero after rounding): the value in units of the smallest
+  // subnormal, 2^(1 - BIAS - MANT)
   const unsigned __int128 m = (unsigned __int128)mhi << 64 | mlo;
-  const int sh = -(e + 1074);  // right shift onto the subnormal grid
+  const int sh = -(e + F::BIAS - 1 + F::MANT);  // right shift onto the subnormal grid
   uint64_t q;
   if (sh <= 0) {
-    q = (uint64_t)(m << -sh);  // exact: below 2^52 here
+    q = (uint64_t)(m << -sh);  // exact: below 2^MANT here
   } else if (sh >= 128) {
     q = sh == 128 && m > ((unsigned __int128)1 << 127) ? 1 : 0;  // at most one unit
   } else {
@@ -78,14 +101,24 @@ NRS_HD double int128_to_f64(bool neg, uint64_t mhi, uint64_t mlo, int e) {
     const unsigned __int128 rem = m & (((unsigned __int128)1 << sh) - 1), half = (unsigned __int128)1 << (sh - 1);
     if (rem > half || (rem == half && (q & 1))) ++q;
   }
-  return nrs_f64_from_bits(sign | q);
+  return sign | q;
+}
+
+NRS_HD double int128_to_f64(bool neg, uint64_t mhi, uint64_t mlo, int e) {
+  return nrs_f64_from_bits(int128_to_float_bits<NrsF64Fmt>(neg, mhi, mlo, e));
+}
+NRS_HD float int128_to_f32(bool neg, uint64_t mhi, uint64_t mlo, int e) {
+  return nrs_f32_from_bits((uint32_t)int128_to_float_bits<NrsF32Fmt>(neg, mhi, mlo, e));
 }
 
 // The same conversion without branches for the common case, so that several
-// elements' operation chains interleave: returns the f64 bits when the
-// magnitude is nonzero and the result normal and finite; otherwise sets
-// `special` (the caller then uses int128_to_f64).
-NRS_HD uint64_t int128_to_f64_bits_fast(bool neg, uint64_t mhi, uint64_t mlo, int e, bool& special) {
+// elements' operation chains interleave: returns the bits when the magnitude
+// is nonzero and the result normal and finite; otherwise sets `special` (the
+// caller then uses int128_to_float_bits).
+template <typename F>
+NRS_HD uint64_t int128_to_float_bits_fast(bool neg, uint64_t mhi, uint64_t mlo, int e, bool& special) {
+  constexpr int W = F::WIDTH;
+  constexpr int DROP = 63 - F::MANT;
   const bool hz = mhi == 0;
   const uint64_t x = hz ? mlo : mhi;
   const int lz = nrs_clz64(x | 1);  // (x = 0 is special below)
@@ -93,15 +126,18 @@ NRS_HD uint64_t int128_to_f64_bits_fast(bool neg, uint64_t mhi, uint64_t mlo, in
   const uint64_t hi_part = (mhi << lz) | ((mlo >> 1) >> (63 - lz));
   const uint64_t top = hz ? mlo << lz : hi_part;
   const uint64_t below = hz ? 0 : mlo << lz;
-  uint64_t mant = top >> 11;
-  const uint64_t rnd = (top >> 10) & 1;
-  const uint64_t sticky = ((top & 0x3FF) | below) != 0;
+  uint64_t mant = top >> DROP;
+  const uint64_t rnd = (top >> (DROP - 1)) & 1;
+  const uint64_t sticky = ((top & ((1ull << (DROP - 1)) - 1)) | below) != 0;
   mant += rnd & (sticky | (mant & 1));
-  const uint64_t carry = mant >> 53;
+  const uint64_t carry = mant >> (F::MANT + 1);
   mant >>= carry;
-  const int pe = p + e + 1023 + (int)carry;
-  special = (x == 0) | (pe <= 0) | (pe >= 2047);
-  return (uint64_t)neg << 63 | (uint64_t)(pe & 0x7FF) << 52 | (mant & 0xFFFFFFFFFFFFFull);
+  const int pe = p + e + F::BIAS + (int)carry;
+  special = (x == 0) | (pe <= 0) | (pe >= F::EMAX);
+  return (uint64_t)neg << (W - 1) | (uint64_t)(pe & F::EMAX) << F::MANT | (mant & ((1ull << F::MANT) - 1));
+}
+NRS_HD uint64_t int128_to_f64_bits_fast(bool neg, uint64_t mhi, uint64_t mlo, int e, bool& special) {
+  return int128_to_float_bits_fast<NrsF64Fmt>(neg, mhi, mlo, e, special);
 }
 
 // The exact total T = R 2^(b(S-1)) + sum_t digit_t 2^(bt) of a grouped Ozaki

@@ -206,10 +206,13 @@ __global__ void __launch_bounds__(kThreads)
 struct nrs_plan {
   nrs_handle* h = nullptr;
   int64_t n_items = 0, gemm_tiles = 0;
-  // f64 GEMMs on the tensor cores (nrs_plan_options.f64_mode = OZAKI); they
-  // run before the persistent kernel, which then holds none of them.
+  // f64 / f32 GEMMs on the tensor cores (nrs_plan_options.f64_mode /
+  // f32_mode = OZAKI); they run before the persistent kernel, which then
+  // holds none of them.
   nrs_ozaki_group* oz = nullptr;
   int64_t oz_gemms = 0;
+  nrs_ozaki_group* oz32 = nullptr;
+  int64_t oz32_gemms = 0;
   nrs_gemm_desc* d_gemm = nullptr;
   nrs_rowreduce_desc* d_red = nullptr;
   WorkItem* d_items = nullptr;
@@ -252,6 +255,7 @@ void selector_features(const nrs_gemm_desc& d, int64_t batch, float* f) {
 void plan_free(nrs_plan* p) {
   if (!p) return;
   nrs_ozaki_group_free(p->oz);
+  nrs_ozaki_group_free(p->oz32);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
@@ -270,6 +274,8 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
   *out = nullptr;
   if (opt && (opt->f64_mode != NRS_PLAN_F64_DMMA && opt->f64_mode != NRS_PLAN_F64_OZAKI))
     return nrs_fail(h, NRS_ERR_INVALID, "unknown f64 mode");
+  if (opt && (opt->f32_mode != NRS_PLAN_F32_FMA && opt->f32_mode != NRS_PLAN_F32_OZAKI))
+    return nrs_fail(h, NRS_ERR_INVALID, "unknown f32 mode");
   std::vector<int> var((size_t)n_gemm, -1);
   std::vector<int> need_sel;
   for (int64_t i = 0; i < n_gemm; ++i) {
@@ -319,13 +325,22 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
       return nrs_fail(h, NRS_ERR_INVALID, "grouped reductions: SUM, MEAN, MAX or MIN");
     if (r.len < 0 || !r.out || (r.len > 0 && !r.x)) return nrs_fail(h, NRS_ERR_INVALID, "bad row reduction");
   }
-  // f64 GEMMs on the tensor cores: the group takes what it can, the rest
-  // stays on DMMA tiles.
-  std::vector<int> on_tc((size_t)n_gemm, 0);
+  // f64 / f32 GEMMs on the tensor cores: each group takes what it can, the
+  // rest stays on DMMA / FMA tiles.
+  std::vector<int> on_tc((size_t)n_gemm, 0), on_tc32((size_t)n_gemm, 0);
   nrs_ozaki_group* oz = nullptr;
+  nrs_ozaki_group* oz32 = nullptr;
   if (opt && opt->f64_mode == NRS_PLAN_F64_OZAKI && forced < 0 && n_gemm > 0) {
-    int st = nrs_ozaki_group_build(h, n_gemm, gemms, opt->f64_slices, opt->f64_digit_bits, on_tc.data(), &oz);
+    int st = nrs_ozaki_group_build(h, n_gemm, gemms, NRS_F64, opt->f64_slices, opt->f64_digit_bits, on_tc.data(),
+                                   &oz);
     if (st) return st;
+  }
+  if (opt && opt->f32_mode == NRS_PLAN_F32_OZAKI && forced < 0 && n_gemm > 0) {
+    int st = nrs_ozaki_group_build(h, n_gemm, gemms, NRS_F32, 0, 0, on_tc32.data(), &oz32);
+    if (st) {
+      nrs_ozaki_group_free(oz);
+      return st;
+    }
   }
   // Work items with a cost estimate (ns on one SM) for longest-first order.
   struct Costed {
@@ -337,11 +352,11 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
   const double sms = h->num_sms > 0 ? h->num_sms : 1;
   const double f64_rate = 1.2e12 / sms, f32_rate = 60e12 / sms, bw = 6.5e12 / sms;
   int64_t gemm_tiles = 0;
-  int64_t oz_gemms = 0;
+  int64_t oz_gemms = 0, oz32_gemms = 0;
   for (int64_t i = 0; i < n_gemm; ++i) {
     const nrs_gemm_desc& d = gemms[i];
-    if (on_tc[i]) {
-      ++oz_gemms;
+    if (on_tc[i] || on_tc32[i]) {
+      ++(on_tc[i] ? oz_gemms : oz32_gemms);
       continue;
     }
     if (d.m == 0 || d.n == 0) continue;
@@ -366,6 +381,7 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
   std::stable_sort(items.begin(), items.end(), [](const Costed& a, const Costed& b) { return a.cost > b.cost; });
   if (items.size() > 0x7fffffff) {
     nrs_ozaki_group_free(oz);
+    nrs_ozaki_group_free(oz32);
     return nrs_fail(h, NRS_ERR_TOO_LARGE, "too many work items");
   }
 
@@ -373,6 +389,8 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
   p->h = h;
   p->oz = oz;
   p->oz_gemms = oz_gemms;
+  p->oz32 = oz32;
+  p->oz32_gemms = oz32_gemms;
   p->n_items = (int64_t)items.size();
   p->gemm_tiles = gemm_tiles;
   std::vector<WorkItem> wi(items.size());
@@ -408,8 +426,9 @@ int plan_build(nrs_handle* h, int64_t n_gemm, const nrs_gemm_desc* gemms, int64_
 }
 
 int plan_launch(nrs_handle* h, nrs_plan* p, cudaStream_t s) {
-  if (p->oz) {
-    int st = nrs_ozaki_group_launch(h, p->oz, s);
+  for (nrs_ozaki_group* g : {p->oz, p->oz32}) {
+    if (!g) continue;
+    int st = nrs_ozaki_group_launch(h, g, s);
     if (st) return st;
   }
   if (p->n_items == 0) return NRS_OK;
@@ -451,12 +470,22 @@ extern "C" int nrs_plan_f64_info(nrs_plan* p, int64_t* on_tensor_cores, int* sli
   return NRS_OK;
 }
 
+extern "C" int nrs_plan_f32_info(nrs_plan* p, int64_t* on_tensor_cores, int* slices, int* digit_bits) {
+  if (!p) return NRS_ERR_INVALID;
+  int s = 0, b = 0;
+  if (p->oz32) nrs_ozaki_group_info(p->oz32, &s, &b, nullptr);
+  if (on_tensor_cores) *on_tensor_cores = p->oz32_gemms;
+  if (slices) *slices = s;
+  if (digit_bits) *digit_bits = b;
+  return NRS_OK;
+}
+
 extern "C" int nrs_plan_run(nrs_handle* h, nrs_plan* p, int use_graph) {
   if (!h || !p || p->h != h) return NRS_ERR_INVALID;
   h->last_error.clear();
   int st = nrs_cuda_check(h, cudaSetDevice(h->device), "cudaSetDevice");
   if (st) return st;
-  if (p->n_items == 0 && !p->oz) return NRS_OK;
+  if (p->n_items == 0 && !p->oz && !p->oz32) return NRS_OK;
   if (!use_graph) return plan_launch(h, p, h->stream);
   cudaStream_t gs = h->own_stream;
   if (!p->exec) {
@@ -647,13 +676,14 @@ extern "C" int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_d
     auto lg = [](int64_t v) { return (int)std::lround(std::log2((double)(v < 1 ? 1 : v))); };
     return std::make_tuple((int)d.dtype, lg(d.m), lg(d.k), lg(d.n));
   };
-  // Buckets of the GEMMs the persistent kernel runs (row-major f64 ones
-  // leave it when they go to the tensor cores).
-  auto make_buckets = [&](bool skip_f64) {
+  // Buckets of the GEMMs the persistent kernel runs (row-major f64 / f32
+  // ones leave it when they go to the tensor cores).
+  auto make_buckets = [&](bool skip_f64, bool skip_f32) {
     std::map<std::tuple<int, int, int, int>, TuneBucket> bm;
     for (const auto& d : g) {
       if (d.m == 0 || d.n == 0 || d.k == 0 || (d.dtype != NRS_F32 && d.dtype != NRS_F64)) continue;
-      if (skip_f64 && d.dtype == NRS_F64 && !(d.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B))) continue;
+      const bool row_major = !(d.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B));
+      if (row_major && ((skip_f64 && d.dtype == NRS_F64) || (skip_f32 && d.dtype == NRS_F32))) continue;
       auto& b = bm[key_of(d)];
       if (b.count == 0) b = TuneBucket{d.dtype, d.m, d.k, d.n, 0.0, 0};
       b.work += 2.0 * d.m * d.n * d.k / (d.dtype == NRS_F64 ? 1.1e12 : 70e12);
@@ -665,16 +695,17 @@ extern "C" int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_d
     return out;
   };
   // 1. untuned, f64 on DMMA tiles
-  for (const auto& b : make_buckets(false)) nrs_tuner_forget(h, b.dtype, b.m, b.k, b.n);
+  for (const auto& b : make_buckets(false, false)) nrs_tuner_forget(h, b.dtype, b.m, b.k, b.n);
   double t_untuned = 0.0, t_isolated = 0.0;
   if ((st = time_group(h, g, n_red, reds, reps, e0, e1, nullptr, &t_untuned))) return done(st);
-  // 2. the f64 mode: DMMA tiles, or the tensor cores at each digit width
-  nrs_plan_options best_opt{NRS_PLAN_F64_DMMA, 0, 0};
-  double t_mode = t_untuned, t_oz_best = -1.0;
+  // 2. the f64 mode: DMMA tiles, or the tensor cores at each digit width;
+  //    then the f32 GEMMs on the tensor cores on top of the best
+  nrs_plan_options best_opt{NRS_PLAN_F64_DMMA, 0, 0, NRS_PLAN_F32_FMA};
+  double t_mode = t_untuned, t_oz_best = -1.0, t_oz32 = -1.0;
   if (opt && opt->f64_mode == NRS_PLAN_F64_OZAKI) {
     for (int bits : {0, 7, 6}) {
       if (opt->f64_digit_bits != 0 && bits != 0) continue;  // the caller fixed the width
-      nrs_plan_options o{NRS_PLAN_F64_OZAKI, opt->f64_slices, bits ? bits : opt->f64_digit_bits};
+      nrs_plan_options o{NRS_PLAN_F64_OZAKI, opt->f64_slices, bits ? bits : opt->f64_digit_bits, NRS_PLAN_F32_FMA};
       double t = 0.0;
       if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &o, &t))) return done(st);
       if (t_oz_best < 0 || t < t_oz_best) t_oz_best = t;
@@ -684,7 +715,17 @@ extern "C" int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_d
       }
     }
   }
-  const std::vector<TuneBucket> buckets = make_buckets(best_opt.f64_mode == NRS_PLAN_F64_OZAKI);
+  if (opt && opt->f32_mode == NRS_PLAN_F32_OZAKI) {
+    nrs_plan_options o = best_opt;
+    o.f32_mode = NRS_PLAN_F32_OZAKI;
+    if ((st = time_group(h, g, n_red, reds, reps, e0, e1, &o, &t_oz32))) return done(st);
+    if (t_oz32 < t_mode) {
+      t_mode = t_oz32;
+      best_opt = o;
+    }
+  }
+  const std::vector<TuneBucket> buckets =
+      make_buckets(best_opt.f64_mode == NRS_PLAN_F64_OZAKI, best_opt.f32_mode == NRS_PLAN_F32_OZAKI);
   // 3. every bucket tuned in isolation
   std::vector<int> untuned(buckets.size()), isolated(buckets.size());
   for (size_t i = 0; i < buckets.size(); ++i) {
@@ -739,6 +780,7 @@ extern "C" int nrs_plan_autotune(nrs_handle* h, int64_t n_gemm, const nrs_gemm_d
     rep->buckets = (int32_t)buckets.size();
     rep->trials = trials;
     rep->options = best_opt;
+    rep->ozaki_f32_ms = t_oz32;
   }
   return done(NRS_OK);
 }

@@ -70,13 +70,14 @@ typedef CUresult (*nrs_encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuin
                                         CUtensorMapFloatOOBfill);
 nrs_encode_tiled_fn nrs_get_encode_tiled();
 
-// Grouped Ozaki (ozaki.cu): the tensor-core form of many f64 GEMMs. build
-// decides which problems it takes (accepted[i] = 1: row-major operands and
-// a spread the slice count covers) and allocates every buffer; launch
-// enqueues the whole group without host synchronisation.
+// Grouped Ozaki (ozaki.cu): the tensor-core form of many f64 (or f32)
+// GEMMs. build decides which problems of element type `dtype` it takes
+// (accepted[i] = 1: row-major operands and a spread the slice count covers)
+// and allocates every buffer; launch enqueues the whole group without host
+// synchronisation.
 struct nrs_ozaki_group;
-int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* descs, int slices, int digit_bits,
-                          int* accepted, nrs_ozaki_group** out);
+int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* descs, int dtype, int slices,
+                          int digit_bits, int* accepted, nrs_ozaki_group** out);
 int nrs_ozaki_group_launch(nrs_handle* h, nrs_ozaki_group* g, cudaStream_t s);
 int nrs_ozaki_group_info(const nrs_ozaki_group* g, int* slices, int* bits, int64_t* tiles);
 void nrs_ozaki_group_free(nrs_ozaki_group* g);

@@ -51,6 +51,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "f64_round.cuh"
@@ -235,10 +236,10 @@ struct OzParams {
 struct OzProb {
   int64_t m, n, kpad;
   int64_t rowoff, coloff;
-  double* C;
+  void* C;  // double, or float when f32
   int64_t ldc;
   int32_t kchunks, n_pairs;
-  int32_t accumulate, pad;
+  int32_t accumulate, f32;
 };
 struct OzTile {
   int32_t prob, tm, tn, pad;
@@ -252,9 +253,9 @@ struct TileCtx {
   int kblocks, n_pairs, kchunks;
   const int* ea;
   const int* eb;
-  double* C;
+  void* C;  // double, or float when f32
   int64_t ldc;
-  int accumulate;
+  int accumulate, f32;
 };
 
 // Work units of a tile, in order: diagonals from the least significant
@@ -317,15 +318,18 @@ __device__ __forceinline__ int group_size(const PairIter& pi, int gm, int kchunk
 }
 
 
-// Writes 8 consecutive columns of one tile row: R values w, digit words per
-// column (S <= 5: digits 0..S-2 in lw; else digits 0..3 in lw and 4..7 in
-// hw), digits 8..14 from the 8-byte records `pitch` apart (S > 9 only) and
-// the column exponents; `left` of the 8 columns lie inside the problem. The
+// Writes 8 consecutive columns of one tile row of C (f64, or f32 when F32):
+// R values w, digit words per column (S <= 5: digits 0..S-2 in lw; else
+// digits 0..3 in lw and 4..7 in hw), digits 8..14 from the 8-byte records
+// `pitch` apart (S > 9 only) and the column exponents; `left` of the 8
+// columns lie inside the problem; the row starts at element `off` of C. The
 // conversions run straight-line for all 8 (interleaved); zero, subnormal and
 // overflowing results are redone by the exact path.
+template <bool F32>
 __device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (&lw)[8], const uint32_t (&hw)[8],
                                         const uint8_t* rec, size_t pitch, const int* eb, int left, int b, int S,
-                                        int ebase, double* crow, bool accumulate) {
+                                        int ebase, void* C, int64_t off, bool accumulate) {
+  using Fmt = typename std::conditional<F32, NrsF32Fmt, NrsF64Fmt>::type;
   uint64_t hi[8], bits[8];
   int ex[8];
   unsigned special = 0;
@@ -338,14 +342,29 @@ __device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (
       ex[e] = eb[e];
     }
   }
+  if (F32 && b == 8 && S <= 5) {
+    // T = R 2^(8(S-1)) + digits < 2^63: one rounding int64 -> f32 in
+    // hardware, the scale added to the exponent field (exact while the
+    // result stays normal; otherwise the exact path below).
+    const int sh = 8 * (S - 1);
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const uint64_t lo = S - 1 > 4 ? (uint64_t)lw[e] | (uint64_t)hw[e] << 32 : (uint64_t)lw[e];
-    bool neg, sp;
-    uint64_t mhi, mlo;
-    ozaki_exact_total((int32_t)w[e], lo, hi[e], b, S, neg, mhi, mlo);
-    bits[e] = int128_to_f64_bits_fast(neg, mhi, mlo, ebase + ex[e], sp);
-    special |= (unsigned)sp << e;
+    for (int e = 0; e < 8; ++e) {
+      const int64_t t = (int64_t)(int32_t)w[e] * ((int64_t)1 << sh) + (int64_t)(lw[e] & (uint32_t)((1ull << sh) - 1));
+      const uint32_t fb = __float_as_uint(__ll2float_rn(t));
+      const int fe = (int)((fb >> 23) & 0xFF) + ebase + ex[e];
+      bits[e] = fb + ((uint32_t)(ebase + ex[e]) << 23);
+      special |= (unsigned)(t == 0 || fe < 1 || fe > 254) << e;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const uint64_t lo = S - 1 > 4 ? (uint64_t)lw[e] | (uint64_t)hw[e] << 32 : (uint64_t)lw[e];
+      bool neg, sp;
+      uint64_t mhi, mlo;
+      ozaki_exact_total((int32_t)w[e], lo, hi[e], b, S, neg, mhi, mlo);
+      bits[e] = int128_to_float_bits_fast<Fmt>(neg, mhi, mlo, ebase + ex[e], sp);
+      special |= (unsigned)sp << e;
+    }
   }
   if (special) {
 #pragma unroll
@@ -355,14 +374,21 @@ __device__ __forceinline__ void retire8(const uint32_t (&w)[8], const uint32_t (
       bool neg;
       uint64_t mhi, mlo;
       ozaki_exact_total((int32_t)w[e], lo, hi[e], b, S, neg, mhi, mlo);
-      bits[e] = (uint64_t)__double_as_longlong(int128_to_f64(neg, mhi, mlo, ebase + ex[e]));
+      bits[e] = int128_to_float_bits<Fmt>(neg, mhi, mlo, ebase + ex[e]);
     }
   }
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     if (e >= left) continue;
-    const double r = __longlong_as_double((long long)bits[e]);
-    crow[e] = accumulate ? crow[e] + r : r;
+    if (F32) {
+      float* cp = static_cast<float*>(C) + off + e;
+      const float r = __uint_as_float((uint32_t)bits[e]);
+      *cp = accumulate ? *cp + r : r;
+    } else {
+      double* cp = static_cast<double*>(C) + off + e;
+      const double r = __longlong_as_double((long long)bits[e]);
+      *cp = accumulate ? *cp + r : r;
+    }
   }
 }
 
@@ -386,6 +412,7 @@ __device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
     c.C = q.C;
     c.ldc = q.ldc;
     c.accumulate = q.accumulate;
+    c.f32 = q.f32;
   } else {
     int tm, tn;
     tile_coords(tile, P, tm, tn);
@@ -401,6 +428,7 @@ __device__ __forceinline__ TileCtx tile_ctx(const OzParams& P, int tile) {
     c.C = P.C;
     c.ldc = P.ldc;
     c.accumulate = P.accumulate;
+    c.f32 = 0;
   }
   return c;
 }
@@ -762,8 +790,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (nd > 4) tmem_ld8_nowait(lane_base + last_buf * BN + col_t, hw);
           tmem_wait_ld();
           if (!row_ok) continue;
-          retire8(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, sm_eb + i * 16 + h8, ncols - col_t, b, S,
-                  ecol_base, tc.C + row * tc.ldc + tc.col0 + col_t, tc.accumulate);
+          const int64_t off = row * tc.ldc + tc.col0 + col_t;
+          if (tc.f32)
+            retire8<true>(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, sm_eb + i * 16 + h8,
+                          ncols - col_t, b, S, ecol_base, tc.C, off, tc.accumulate);
+          else
+            retire8<false>(w, lw, hw, slot + (size_t)col_t * kColPitch, kColPitch, sm_eb + i * 16 + h8,
+                           ncols - col_t, b, S, ecol_base, tc.C, off, tc.accumulate);
         }
       }
       tc_fence_before();
@@ -864,7 +897,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
               const bool neg = sum < 0;
               const unsigned __int128 mag = neg ? (unsigned __int128)(-sum) : (unsigned __int128)sum;
               const double r = int128_to_f64(neg, (uint64_t)(mag >> 64), (uint64_t)mag, ecol_base + tc.eb[col]);
-              double* cp = tc.C + row * tc.ldc + col;
+              double* cp = (double*)tc.C + row * tc.ldc + col;
               *cp = tc.accumulate ? *cp + r : r;
             }
           }
@@ -883,16 +916,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 // ---------------------------------------------------------------------------
 // Scaling exponents and slicing
 // ---------------------------------------------------------------------------
-// frexp-style exponent of max |x| over a row (one warp per row).
-// `flag` (may be null) gets bit 0 set when a row holds an Inf or a NaN.
-__global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda,
+// frexp-style exponent of max |x| over a row (one warp per row; T double or
+// float, widened exactly). `flag` (may be null) gets bit 0 set when a row
+// holds an Inf or a NaN.
+template <typename T>
+__global__ void row_exponents(const T* __restrict__ A, int64_t m, int64_t k, int64_t lda,
                               int* __restrict__ ea, uint32_t* __restrict__ flag) {
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (row >= m) return;
   uint64_t mx = 0;
   for (int64_t j = lane; j < k; j += 32) {
-    uint64_t b = (uint64_t)__double_as_longlong(A[row * lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
+    uint64_t b = (uint64_t)__double_as_longlong((double)A[row * lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
     mx = b > mx ? b : mx;
   }
   for (int off = 16; off; off >>= 1) {
@@ -911,7 +946,8 @@ __global__ void row_exponents(const double* __restrict__ A, int64_t m, int64_t k
 // the magnitudes): a 2-D grid of 256-row strips, coalesced across columns,
 // combined with atomicMax on the bit pattern into a zeroed array.
 constexpr int kColStrip = 256;
-__global__ void col_max_bits(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
+template <typename T>
+__global__ void col_max_bits(const T* __restrict__ B, int64_t k, int64_t n, int64_t ldb,
                              unsigned long long* __restrict__ colmax) {
   const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= n) return;
@@ -920,7 +956,7 @@ __global__ void col_max_bits(const double* __restrict__ B, int64_t k, int64_t n,
   unsigned long long mx = 0;
   for (int64_t i = r0; i < r1; ++i) {
     const unsigned long long b =
-        (unsigned long long)__double_as_longlong(B[i * ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
+        (unsigned long long)__double_as_longlong((double)B[i * ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
     mx = b > mx ? b : mx;
   }
   atomicMax(&colmax[col], mx);
@@ -1117,19 +1153,19 @@ __device__ __forceinline__ uint32_t est_bits(double x, int e, float* f) {
 
 // X (rows x k, row pitch ld, contiguous along k) -> out [2][rows][kpad],
 // sums[row] = sum_k |x'|. One warp per row, 8 consecutive k per lane step.
-template <bool VEC>
+template <bool VEC, typename T>
 __global__ void __launch_bounds__(256)
-    est_rows(const double* __restrict__ X, int64_t rows, int64_t k, int64_t ld, int64_t kpad,
+    est_rows(const T* __restrict__ X, int64_t rows, int64_t k, int64_t ld, int64_t kpad,
              const int* __restrict__ e, uint16_t* __restrict__ out, float* __restrict__ sums) {
   const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
   const int er = e[row];
-  const double* xr = X + row * ld;
+  const T* xr = X + row * ld;
   float s = 0.0f;
   for (int64_t j0 = (int64_t)lane * 8; j0 < kpad; j0 += 256) {
     double x[8];
-    if (VEC && j0 + 8 <= k) {
+    if (VEC && j0 + 8 <= k) {  // (T = double only)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const double2 d2 = reinterpret_cast<const double2*>(xr + j0)[q];
@@ -1138,7 +1174,7 @@ __global__ void __launch_bounds__(256)
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < 8; ++q) x[q] = j0 + q < k ? xr[j0 + q] : 0.0;
+      for (int q = 0; q < 8; ++q) x[q] = j0 + q < k ? (double)xr[j0 + q] : 0.0;
     }
     uint32_t pa[4], pi[4];
 #pragma unroll
@@ -1161,8 +1197,9 @@ __global__ void __launch_bounds__(256)
 // X (k x cols row-major) -> out [2][cols][kpad] (transposed through shared
 // memory like slice_cols), part[strip][col] = sum of |x'| over the block's
 // 64 k; est_strip_sums adds the strips in order (deterministic).
+template <typename T>
 __global__ void __launch_bounds__(256)
-    est_cols(const double* __restrict__ X, int64_t k, int64_t cols, int64_t ld, int64_t kpad,
+    est_cols(const T* __restrict__ X, int64_t k, int64_t cols, int64_t ld, int64_t kpad,
              const int* __restrict__ e, uint16_t* __restrict__ out, float* __restrict__ part) {
   __shared__ uint32_t tile[2][kSliceColN][kSliceColPitch];
   __shared__ float csum[8][kSliceColN];
@@ -1175,8 +1212,8 @@ __global__ void __launch_bounds__(256)
   for (int r = 0; r < kSliceColK / 16; ++r) {
     const int w = ty + 8 * r;
     const int64_t kk = k0 + 2 * w;
-    const double x0 = kk < k && nn < cols ? X[kk * ld + nn] : 0.0;
-    const double x1 = kk + 1 < k && nn < cols ? X[(kk + 1) * ld + nn] : 0.0;
+    const double x0 = kk < k && nn < cols ? (double)X[kk * ld + nn] : 0.0;
+    const double x1 = kk + 1 < k && nn < cols ? (double)X[(kk + 1) * ld + nn] : 0.0;
     float f0, f1;
     const uint32_t b0 = est_bits(x0, ec, &f0), b1 = est_bits(x1, ec, &f1);
     s += f0;
@@ -1235,22 +1272,31 @@ bool make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t ro
 // passed transposed); otherwise at p[kk * ld + r] (B as given, or A passed
 // transposed), which the column kernels read coalesced and transpose.
 struct OzOperand {
-  const double* p;
+  const void* p;  // double, or float when f32 (the spread estimate only)
   int64_t ld;
   int64_t rows;
   bool rows_contig;
+  bool f32 = false;
+  const double* d() const { return static_cast<const double*>(p); }
+  const float* f() const { return static_cast<const float*>(p); }
 };
 
 int launch_exponents(nrs_handle* h, const OzOperand& o, int64_t k, int* e,
                      unsigned long long* colmax, uint32_t* flag) {
   cudaStream_t s = h->stream;
   if (o.rows_contig) {
-    row_exponents<<<(unsigned)((o.rows + 7) / 8), 256, 0, s>>>(o.p, o.rows, k, o.ld, e, flag);
+    if (o.f32)
+      row_exponents<float><<<(unsigned)((o.rows + 7) / 8), 256, 0, s>>>(o.f(), o.rows, k, o.ld, e, flag);
+    else
+      row_exponents<double><<<(unsigned)((o.rows + 7) / 8), 256, 0, s>>>(o.d(), o.rows, k, o.ld, e, flag);
   } else {
     int st = nrs_cuda_check(h, cudaMemsetAsync(colmax, 0, (size_t)o.rows * 8, s), "cudaMemsetAsync");
     if (st) return st;
-    col_max_bits<<<dim3((unsigned)((o.rows + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip)), 256,
-                   0, s>>>(o.p, k, o.rows, o.ld, colmax);
+    const dim3 grid((unsigned)((o.rows + 255) / 256), (unsigned)((k + kColStrip - 1) / kColStrip));
+    if (o.f32)
+      col_max_bits<float><<<grid, 256, 0, s>>>(o.f(), k, o.rows, o.ld, colmax);
+    else
+      col_max_bits<double><<<grid, 256, 0, s>>>(o.d(), k, o.rows, o.ld, colmax);
     exponents_from_bits<<<(unsigned)((o.rows + 255) / 256), 256, 0, s>>>(colmax, o.rows, e, flag);
   }
   return nrs_after_launch(h, "ozaki exponents");
@@ -1265,9 +1311,9 @@ int launch_slices_b(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, 
     const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
     // 16-byte row loads when every row start is 16-byte aligned.
     if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
-      slice_rows<b, true><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, S, out);
+      slice_rows<b, true><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
     else
-      slice_rows<b, false><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, S, out);
+      slice_rows<b, false><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
   } else {
     const int smem = (int)((size_t)S * kSliceColN * kSliceColPitch * 4);
     int st = nrs_cuda_check(h, cudaFuncSetAttribute(slice_cols<b>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1275,7 +1321,7 @@ int launch_slices_b(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, 
                             "cudaFuncSetAttribute(slice_cols)");
     if (st) return st;
     dim3 g((unsigned)((o.rows + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
-    slice_cols<b><<<g, 256, smem, s>>>(o.p, k, o.rows, o.ld, kpad, e, S, out);
+    slice_cols<b><<<g, 256, smem, s>>>(o.d(), k, o.rows, o.ld, kpad, e, S, out);
   }
   return nrs_after_launch(h, "ozaki slicing");
 }
@@ -1292,14 +1338,19 @@ int launch_est_operand(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpa
   cudaStream_t s = h->stream;
   if (o.rows_contig) {
     const unsigned grid = (unsigned)((o.rows + 7) / 8);
-    if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
-      est_rows<true><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, out, sums);
+    if (o.f32)
+      est_rows<false, float><<<grid, 256, 0, s>>>(o.f(), o.rows, k, o.ld, kpad, e, out, sums);
+    else if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
+      est_rows<true, double><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, out, sums);
     else
-      est_rows<false><<<grid, 256, 0, s>>>(o.p, o.rows, k, o.ld, kpad, e, out, sums);
+      est_rows<false, double><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, out, sums);
   } else {
     const int64_t strips = (kpad + kSliceColK - 1) / kSliceColK;
     dim3 g((unsigned)((o.rows + kSliceColN - 1) / kSliceColN), (unsigned)strips);
-    est_cols<<<g, 256, 0, s>>>(o.p, k, o.rows, o.ld, kpad, e, out, part);
+    if (o.f32)
+      est_cols<float><<<g, 256, 0, s>>>(o.f(), k, o.rows, o.ld, kpad, e, out, part);
+    else
+      est_cols<double><<<g, 256, 0, s>>>(o.d(), k, o.rows, o.ld, kpad, e, out, part);
     est_strip_sums<<<(unsigned)((o.rows + 255) / 256), 256, 0, s>>>(part, strips, o.rows, sums);
   }
   return nrs_after_launch(h, "ozaki spread operands");
@@ -1481,9 +1532,9 @@ int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m,
 // of each pre-processing kernel covers every problem through a chunk table,
 // and one persistent tensor-core launch covers every tile.
 struct OzIn {
-  const double* A;
+  const void* A;  // double or float, as the group's element type T
   int64_t lda;
-  const double* B;
+  const void* B;
   int64_t ldb;
   int64_t m, n, k, kpad;
   int64_t rowoff, coloff;
@@ -1492,7 +1543,9 @@ struct OzChunk {
   int32_t prob, r0, k0, pad;  // problem, first row (column), first k
 };
 
-// Row exponents of every A: one warp per row, 8 rows per block.
+// Row exponents of every A: one warp per row, 8 rows per block. T (double or
+// float) is the group's element type; floats widen to double exactly.
+template <typename T>
 __global__ void __launch_bounds__(256)
     g_row_exponents(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, int* __restrict__ ea) {
   const OzChunk c = ch[blockIdx.x];
@@ -1502,7 +1555,8 @@ __global__ void __launch_bounds__(256)
   if (row >= q.m) return;
   uint64_t mx = 0;
   for (int64_t j = lane; j < q.k; j += 32) {
-    const uint64_t v = (uint64_t)__double_as_longlong(q.A[row * q.lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
+    const uint64_t v =
+        (uint64_t)__double_as_longlong((double)static_cast<const T*>(q.A)[row * q.lda + j]) & 0x7FFFFFFFFFFFFFFFULL;
     mx = v > mx ? v : mx;
   }
   for (int off = 16; off; off >>= 1) {
@@ -1513,7 +1567,8 @@ __global__ void __launch_bounds__(256)
 }
 
 // Column maxima of every B: 256 columns x 256 k per block, atomicMax on the
-// bit patterns into a zeroed array.
+// bit patterns (of the values widened to double) into a zeroed array.
+template <typename T>
 __global__ void __launch_bounds__(256)
     g_col_max_bits(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, unsigned long long* __restrict__ colmax) {
   const OzChunk c = ch[blockIdx.x];
@@ -1523,7 +1578,9 @@ __global__ void __launch_bounds__(256)
   const int64_t r1 = (c.k0 + kColStrip) < q.k ? (c.k0 + kColStrip) : q.k;
   unsigned long long mx = 0;
   for (int64_t i = c.k0; i < r1; ++i) {
-    const unsigned long long v = (unsigned long long)__double_as_longlong(q.B[i * q.ldb + col]) & 0x7FFFFFFFFFFFFFFFULL;
+    const unsigned long long v =
+        (unsigned long long)__double_as_longlong((double)static_cast<const T*>(q.B)[i * q.ldb + col]) &
+        0x7FFFFFFFFFFFFFFFULL;
     mx = v > mx ? v : mx;
   }
   atomicMax(&colmax[q.coloff + col], mx);
@@ -1531,7 +1588,7 @@ __global__ void __launch_bounds__(256)
 
 // A slices of every problem: a block takes 8 rows of one problem, a thread 8
 // consecutive k of one row (zero beyond k, up to the problem's kpad).
-template <int b>
+template <typename T, int b>
 __global__ void __launch_bounds__(256)
     g_slice_rows(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ ea, int S,
                  int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
@@ -1543,10 +1600,10 @@ __global__ void __launch_bounds__(256)
     const int64_t row = (int64_t)c.r0 + w / groups, j0 = (w % groups) * 8;
     if (row >= q.m) break;  // w only grows: every later item is beyond m too
     const int e = ea[q.rowoff + row];
-    const double* src = q.A + row * q.lda + j0;
+    const T* src = static_cast<const T*>(q.A) + row * q.lda + j0;
     unsigned __int128 Z[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) Z[t] = (unsigned __int128)fixed126(j0 + t < q.k ? src[t] : 0.0, e) + C;
+    for (int t = 0; t < 8; ++t) Z[t] = (unsigned __int128)fixed126(j0 + t < q.k ? (double)src[t] : 0.0, e) + C;
     uint16_t* o = out + (q.rowoff + row) * pitch + j0;
 #pragma unroll
     for (int t = 0; t < OZ_MAX_SLICES; ++t) {
@@ -1562,7 +1619,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // B^T slices of every problem: slice_cols' 64 k x 32 n transposing tile.
-template <int b>
+template <typename T, int b>
 __global__ void __launch_bounds__(256)
     g_slice_cols(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ eb, int S,
                  int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
@@ -1572,6 +1629,7 @@ __global__ void __launch_bounds__(256)
   const int64_t k0 = c.k0, n0 = c.r0;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const unsigned __int128 C = digit_offset(S, b);
+  const T* const Bq = static_cast<const T*>(q.B);
   {
     const int64_t nn = n0 + tx;
     const int e = nn < q.n ? eb[q.coloff + nn] : 0;
@@ -1580,9 +1638,9 @@ __global__ void __launch_bounds__(256)
       const int w = ty + 8 * r;
       const int64_t kk = k0 + 2 * w;
       const unsigned __int128 Z0 =
-          (unsigned __int128)(kk < q.k && nn < q.n ? fixed126(q.B[kk * q.ldb + nn], e) : (__int128)0) + C;
+          (unsigned __int128)(kk < q.k && nn < q.n ? fixed126((double)Bq[kk * q.ldb + nn], e) : (__int128)0) + C;
       const unsigned __int128 Z1 =
-          (unsigned __int128)(kk + 1 < q.k && nn < q.n ? fixed126(q.B[(kk + 1) * q.ldb + nn], e) : (__int128)0) + C;
+          (unsigned __int128)(kk + 1 < q.k && nn < q.n ? fixed126((double)Bq[(kk + 1) * q.ldb + nn], e) : (__int128)0) + C;
 #pragma unroll
       for (int t = 0; t < OZ_MAX_SLICES; ++t)
         if (t < S)
@@ -1697,6 +1755,7 @@ extern "C" int nrs_gemm_ozaki(nrs_handle* h, int64_t m, int64_t k, int64_t n, co
 // ---------------------------------------------------------------------------
 struct nrs_ozaki_group {
   int S = 0, b = 0;
+  int f32 = 0;  // element type of the group's problems: float (1) or double (0)
   int64_t pitch = 0, rows_a = 0, rows_b = 0, n_tiles = 0;
   int64_t n_rowch = 0, n_colch = 0, n_slcol = 0;
   void* arena = nullptr;
@@ -1724,12 +1783,16 @@ int nrs_ozaki_group_info(const nrs_ozaki_group* g, int* slices, int* bits, int64
   return NRS_OK;
 }
 
-// Slice count for `slices` = 0: each problem's spread measured now (one
-// read-back each); the group takes the largest count. Problems whose spread
-// no count covers, or with Inf / NaN, are left out (they stay on the FP64
-// DMMA tiles). digit_bits 0 = the widest width the group's K allows.
-int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, int slices, int digit_bits,
-                          int* accepted, nrs_ozaki_group** out) {
+// The row-major GEMMs of element type `dtype` (NRS_F64 or NRS_F32) as one
+// group. Slice count for `slices` = 0: each problem's spread measured now
+// (one read-back each); the group takes the largest count, carrying each
+// operand to 53 + log2(max R) bits for f64 and 26 + log2(max R) (f32's 24
+// and two guard bits) for f32. Problems whose spread no count covers, or
+// with Inf / NaN, are left out (they stay on the persistent kernel's DMMA or
+// FP32 tiles). digit_bits 0 = the widest width the group's K allows.
+constexpr double kTargetBits32 = 26.0;
+int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, int dtype, int slices,
+                          int digit_bits, int* accepted, nrs_ozaki_group** out) {
   *out = nullptr;
   if (slices < 0 || slices > OZ_MAX_SLICES) return nrs_fail(h, NRS_ERR_INVALID, "slices must be 0 (auto) or 1..16");
   if (digit_bits != 0 && (digit_bits < 6 || digit_bits > 8))
@@ -1739,13 +1802,15 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   for (int64_t i = 0; i < count; ++i) {
     accepted[i] = 0;
     const nrs_gemm_desc& g = d[i];
-    if (g.dtype != NRS_F64 || (g.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B)) || g.m <= 0 || g.n <= 0 || g.k <= 0)
+    if (g.dtype != dtype || (g.flags & (NRS_GEMM_TRANS_A | NRS_GEMM_TRANS_B)) || g.m <= 0 || g.n <= 0 || g.k <= 0)
       continue;
     idx.push_back(i);
     kp_max = std::max(kp_max, (g.k + OZ_BK - 1) / OZ_BK * OZ_BK);
   }
   if (idx.empty()) return NRS_OK;
-  double bits_max = kTargetBits;
+  const bool f32 = dtype == NRS_F32;
+  const double target = f32 ? kTargetBits32 : kTargetBits;
+  double bits_max = target;
   std::vector<int64_t> keep;
   for (int64_t i : idx) {
     const nrs_gemm_desc& g = d[i];
@@ -1755,15 +1820,15 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
     }
     const int64_t kpad8 = (g.k + 7) / 8 * 8;
     SpreadResult r{};
-    const OzOperand a{(const double*)g.A, g.lda, g.m, true}, bT{(const double*)g.B, g.ldb, g.n, false};
+    const OzOperand a{g.A, g.lda, g.m, true, f32}, bT{g.B, g.ldb, g.n, false, f32};
     int st = spread_estimate(h, a, bT, g.m, g.n, g.k, kpad8, 1, &r);
     if (st) return st;
     if (r.flags & 1u) continue;
-    double need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+    double need = target + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
     int bb, SS, kc;
     if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc, kMaxChunkSlicesGrouped))) {
       if ((st = spread_estimate(h, a, bT, g.m, g.n, g.k, kpad8, 2, &r))) return st;
-      need = kTargetBits + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
+      need = target + (r.rmax > 1.0f ? std::log2((double)r.rmax) : 0.0);
       if (!(std::isfinite((double)r.rmax) && choose_digits(kp_max, need, &bb, &SS, &kc, kMaxChunkSlicesGrouped)))
         continue;
     }
@@ -1810,10 +1875,10 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
     const nrs_gemm_desc& g = d[i];
     const int64_t kpad = (g.k + OZ_BK - 1) / OZ_BK * OZ_BK;
     const int p = (int)ins.size();
-    ins.push_back(OzIn{(const double*)g.A, g.lda, (const double*)g.B, g.ldb, g.m, g.n, g.k, kpad, rowoff, coloff});
+    ins.push_back(OzIn{g.A, g.lda, g.B, g.ldb, g.m, g.n, g.k, kpad, rowoff, coloff});
     const int kc = (int)((kpad + kChunkOf(b) - 1) / kChunkOf(b));
-    probs.push_back(OzProb{g.m, g.n, kpad, rowoff, coloff, (double*)g.C, g.ldc, kc,
-                           S * (S + 1) / 2 * kc, (g.flags & NRS_GEMM_ACCUMULATE) ? 1 : 0, 0});
+    probs.push_back(OzProb{g.m, g.n, kpad, rowoff, coloff, g.C, g.ldc, kc, S * (S + 1) / 2 * kc,
+                           (g.flags & NRS_GEMM_ACCUMULATE) ? 1 : 0, f32 ? 1 : 0});
     for (int64_t r = 0; r < g.m; r += 8) rowch.push_back(OzChunk{p, (int32_t)r, 0, 0});
     for (int64_t c0 = 0; c0 < g.n; c0 += 256)
       for (int64_t k0 = 0; k0 < g.k; k0 += kColStrip) colch.push_back(OzChunk{p, (int32_t)c0, (int32_t)k0, 0});
@@ -1865,6 +1930,7 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   G->d_acc = (__int128*)take(b_acc);
   G->S = S;
   G->b = b;
+  G->f32 = f32 ? 1 : 0;
   G->pitch = kp_max;
   G->rows_a = rowoff;
   G->rows_b = coloff;
@@ -1891,17 +1957,30 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   return NRS_OK;
 }
 
-template <int b>
+template <typename T, int b>
 int group_slices(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
   const int64_t plane_a = G->rows_a * G->pitch, plane_b = G->rows_b * G->pitch;
-  g_slice_rows<b><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea, G->S, G->pitch, plane_a, G->d_sa);
+  g_slice_rows<T, b><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea, G->S, G->pitch, plane_a,
+                                                          G->d_sa);
   const int smem = (int)((size_t)G->S * kSliceColN * kSliceColPitch * 4);
-  int st = nrs_cuda_check(h, cudaFuncSetAttribute(g_slice_cols<b>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+  int st = nrs_cuda_check(h,
+                          cudaFuncSetAttribute(g_slice_cols<T, b>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                           "cudaFuncSetAttribute(g_slice_cols)");
   if (st) return st;
-  g_slice_cols<b><<<(unsigned)G->n_slcol, 256, smem, s>>>(G->d_in, G->d_slcol, G->d_eb, G->S, G->pitch, plane_b,
-                                                         G->d_sb);
+  g_slice_cols<T, b><<<(unsigned)G->n_slcol, 256, smem, s>>>(G->d_in, G->d_slcol, G->d_eb, G->S, G->pitch, plane_b,
+                                                            G->d_sb);
   return nrs_after_launch(h, "grouped ozaki slicing");
+}
+
+template <typename T>
+int group_prepare(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
+  g_row_exponents<T><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea);
+  g_col_max_bits<T><<<(unsigned)G->n_colch, 256, 0, s>>>(G->d_in, G->d_colch, G->d_colmax);
+  exponents_from_bits<<<(unsigned)((G->rows_b + 255) / 256), 256, 0, s>>>(G->d_colmax, G->rows_b, G->d_eb, nullptr);
+  int st = nrs_after_launch(h, "grouped ozaki exponents");
+  if (st) return st;
+  return G->b == 8 ? group_slices<T, 8>(h, G, s) : G->b == 7 ? group_slices<T, 7>(h, G, s)
+                                                             : group_slices<T, 6>(h, G, s);
 }
 
 // Enqueues the whole group on `s` (no host synchronisation).
@@ -1909,11 +1988,7 @@ int nrs_ozaki_group_launch(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
   if (!G || G->n_tiles == 0) return NRS_OK;
   int st = nrs_cuda_check(h, cudaMemsetAsync(G->d_colmax, 0, (size_t)G->rows_b * 8, s), "cudaMemsetAsync");
   if (st) return st;
-  g_row_exponents<<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea);
-  g_col_max_bits<<<(unsigned)G->n_colch, 256, 0, s>>>(G->d_in, G->d_colch, G->d_colmax);
-  exponents_from_bits<<<(unsigned)((G->rows_b + 255) / 256), 256, 0, s>>>(G->d_colmax, G->rows_b, G->d_eb, nullptr);
-  if ((st = nrs_after_launch(h, "grouped ozaki exponents"))) return st;
-  st = G->b == 8 ? group_slices<8>(h, G, s) : G->b == 7 ? group_slices<7>(h, G, s) : group_slices<6>(h, G, s);
+  st = G->f32 ? group_prepare<float>(h, G, s) : group_prepare<double>(h, G, s);
   if (st) return st;
   OzParams P{};
   P.kpad = G->pitch;
@@ -1952,7 +2027,7 @@ extern "C" int nrs_gemm_ozaki_grouped(nrs_handle* h, int64_t count, const nrs_ge
   }
   std::vector<int> acc((size_t)count);
   nrs_ozaki_group* G = nullptr;
-  if ((st = nrs_ozaki_group_build(h, count, descs, slices, 0, acc.data(), &G))) return st;
+  if ((st = nrs_ozaki_group_build(h, count, descs, NRS_F64, slices, 0, acc.data(), &G))) return st;
   if (info) {
     std::memset(info, 0, sizeof(*info));
     if (G) {

@@ -645,15 +645,17 @@ class Plan:
 
     gemms: list of (A, B, C, accumulate) 2-D CUDA tensors (f32 or f64; A and
     B may be transposed views); reds: list of (x, op, out) with x a
-    contiguous 1-D tensor and out a 1-element tensor."""
+    contiguous 1-D tensor and out a 1-element tensor. f64_mode / f32_mode:
+    nrs_plan_options (PLAN_F64_OZAKI / PLAN_F32_OZAKI put the row-major
+    GEMMs of that type on the tensor cores)."""
 
     def __init__(self, gemms=(), reds=(), f64_mode: int = L.PLAN_F64_DMMA, f64_slices: int = 0,
-                 f64_digit_bits: int = 0):
+                 f64_digit_bits: int = 0, f32_mode: int = L.PLAN_F32_FMA):
         lib = L.load()
         self.h = handle()
         gd, rd, self._keep = _group_descs(gemms, reds)
         self.p = C.c_void_p()
-        opt = L.PlanOptions(f64_mode, f64_slices, f64_digit_bits)
+        opt = L.PlanOptions(f64_mode, f64_slices, f64_digit_bits, f32_mode)
         L.check(lib.nrs_plan_create_ex(self.h, len(gemms), gd, len(reds), rd, C.byref(opt), C.byref(self.p)),
                 self.h)
 
@@ -670,6 +672,12 @@ class Plan:
         """(f64 GEMMs on the tensor cores, slice count, digit bits)."""
         n, sl, b = C.c_int64(), C.c_int(), C.c_int()
         L.check(L.load().nrs_plan_f64_info(self.p, C.byref(n), C.byref(sl), C.byref(b)))
+        return n.value, sl.value, b.value
+
+    def f32_info(self):
+        """(f32 GEMMs on the tensor cores, slice count, digit bits)."""
+        n, sl, b = C.c_int64(), C.c_int(), C.c_int()
+        L.check(L.load().nrs_plan_f32_info(self.p, C.byref(n), C.byref(sl), C.byref(b)))
         return n.value, sl.value, b.value
 
     def close(self) -> None:
@@ -710,23 +718,28 @@ def _group_descs(gemms, reds):
     return gd, rd, keep
 
 
-def autotune_plan(gemms=(), reds=(), max_trials: int = 48, reps: int = 3, f64_ozaki: bool = False) -> dict:
-    """nrs_plan_autotune: tile variants (and, with f64_ozaki, the tensor-core
-    f64 mode and its digit width) chosen by timing the whole group; fills the
-    tuner table that the next Plan uses and returns the Plan keyword
-    arguments in "plan_kwargs". Outputs' contents are undefined afterwards."""
+def autotune_plan(gemms=(), reds=(), max_trials: int = 48, reps: int = 3, f64_ozaki: bool = False,
+                  f32_ozaki: bool = False) -> dict:
+    """nrs_plan_autotune: tile variants (and, with f64_ozaki / f32_ozaki, the
+    tensor-core f64 mode and its digit width / the tensor-core f32 mode)
+    chosen by timing the whole group; fills the tuner table that the next
+    Plan uses and returns the Plan keyword arguments in "plan_kwargs".
+    Outputs' contents are undefined afterwards."""
     lib = L.load()
     h = handle()
     gd, rd, keep = _group_descs(gemms, reds)
     rep = L.AutotuneReport()
-    opt = L.PlanOptions(L.PLAN_F64_OZAKI if f64_ozaki else L.PLAN_F64_DMMA, 0, 0)
+    opt = L.PlanOptions(L.PLAN_F64_OZAKI if f64_ozaki else L.PLAN_F64_DMMA, 0, 0,
+                        L.PLAN_F32_OZAKI if f32_ozaki else L.PLAN_F32_FMA)
     L.check(lib.nrs_plan_autotune(h, len(gemms), gd, len(reds), rd, C.byref(opt), max_trials, reps,
                                   C.byref(rep)), h)
     del keep
     o = rep.options
     return {"untuned_ms": rep.untuned_ms, "isolated_ms": rep.isolated_ms, "final_ms": rep.final_ms,
-            "ozaki_ms": rep.ozaki_ms, "buckets": rep.buckets, "trials": rep.trials,
-            "plan_kwargs": {"f64_mode": o.f64_mode, "f64_slices": o.f64_slices, "f64_digit_bits": o.f64_digit_bits}}
+            "ozaki_ms": rep.ozaki_ms, "ozaki_f32_ms": rep.ozaki_f32_ms, "buckets": rep.buckets,
+            "trials": rep.trials,
+            "plan_kwargs": {"f64_mode": o.f64_mode, "f64_slices": o.f64_slices, "f64_digit_bits": o.f64_digit_bits,
+                            "f32_mode": o.f32_mode}}
 
 
 def gemm_ozaki_grouped(problems, slices: int = 0):

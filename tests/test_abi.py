@@ -35,7 +35,7 @@ def test_python_binding_covers_header():
 def test_status_strings_and_version(lib_path):
     from numrs_gb300 import _lib as L
     lib = L.load()
-    assert lib.nrs_abi_version() == 2
+    assert lib.nrs_abi_version() == 3
     for s in range(0, -12, -1):
         assert lib.nrs_status_string(s)
     # Null handles are rejected on the host, before any CUDA call.

@@ -1,5 +1,5 @@
 """The grouped Ozaki epilogue's exact element total and its 128-bit integer
--> f64 conversion (numrs_gb300/csrc/f64_round.cuh, host/device code),
+-> f64 / f32 conversions (numrs_gb300/csrc/f64_round.cuh, host/device code),
 compiled for the host with g++: the exact path and the straight-line fast
 path against exact rational rounding (round to nearest, ties to even) over
 random magnitudes and scales, ties, carries into the next binade, overflow
@@ -28,6 +28,17 @@ extern "C" uint64_t nrs_test_fast(uint64_t hi, uint64_t lo, int e, int neg, int*
   const uint64_t r = int128_to_f64_bits_fast(neg != 0, hi, lo, e, sp);
   *special = sp;
   return r;
+}
+extern "C" uint32_t nrs_test_f32(uint64_t hi, uint64_t lo, int e, int neg, int fast, int* special) {
+  bool sp = false;
+  uint64_t r;
+  if (fast) {
+    r = int128_to_float_bits_fast<NrsF32Fmt>(neg != 0, hi, lo, e, sp);
+  } else {
+    r = int128_to_float_bits<NrsF32Fmt>(neg != 0, hi, lo, e);
+  }
+  *special = sp;
+  return (uint32_t)r;
 }
 extern "C" void nrs_test_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int* neg, uint64_t* mhi,
                                uint64_t* mlo) {
@@ -134,3 +145,58 @@ def test_exact_total_every_width(lib, b):
             f(R, rec & ((1 << 64) - 1), rec >> 64, b, S, ctypes.byref(neg), ctypes.byref(mhi), ctypes.byref(mlo))
             got = (mhi.value << 64 | mlo.value) * (-1 if neg.value else 1)
             assert got == T and bool(neg.value) == (T < 0), (b, S, R, digits)
+
+
+def _f32_bits(m, e, neg):
+    """Round m 2^e to binary32 (nearest, ties to even) with integers only."""
+    sign = (1 << 31) if neg else 0
+    if m == 0:
+        return sign
+
+    def rne(num, sh):  # round(num / 2^sh), ties to even (sh may be <= 0)
+        if sh <= 0:
+            return num << -sh
+        q, r = num >> sh, num & ((1 << sh) - 1)
+        half = 1 << (sh - 1)
+        return q + 1 if r > half or (r == half and q & 1) else q
+
+    p = m.bit_length() - 1
+    if p + e >= -126:
+        mant = rne(m, p - 23)  # 24 bits (or 2^24 after a carry)
+        E = p + e
+        if mant >> 24:
+            mant >>= 1
+            E += 1
+        if E > 127:
+            return sign | 0x7F800000
+        return sign | (E + 127) << 23 | (mant & 0x7FFFFF)
+    return sign | rne(m, -(e + 149))  # subnormal grid 2^-149 (2^-126 after a carry)
+
+
+def test_int128_to_f32_exact_and_fast(lib):
+    f = lib.nrs_test_f32
+    f.restype = ctypes.c_uint32
+    f.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_int)]
+    r = random.Random(9)
+    sp = ctypes.c_int()
+    cases = []
+    for _ in range(40000):
+        bits = r.randint(0, 128)
+        m = r.getrandbits(bits) if bits else r.randint(0, 3)
+        cases.append((m, r.choice([r.randint(-100, 60), r.randint(-300, -130), r.randint(-40, 140)]), r.randint(0, 1)))
+    for k in range(25, 127):
+        for e in (-149 - k, -126 - k, -127 - k, 0, 127 - k, 128 - k):
+            base = 1 << k
+            for m in (base | (1 << (k - 24)), base | (3 << (k - 25)), (1 << (k + 1)) - 1, base | (1 << (k - 24)) | 1):
+                cases += [(m, e, 0), (m, e, 1)]
+    n_fast = 0
+    for m, e, neg in cases:
+        want = _f32_bits(m, e, neg)
+        got = f(m >> 64, m & ((1 << 64) - 1), e, neg, 0, ctypes.byref(sp))
+        assert got == want, ("exact", hex(m), e, neg, hex(got), hex(want))
+        got = f(m >> 64, m & ((1 << 64) - 1), e, neg, 1, ctypes.byref(sp))
+        if not sp.value:
+            n_fast += 1
+            assert got == want, ("fast", hex(m), e, neg, hex(got), hex(want))
+    assert n_fast > 10000

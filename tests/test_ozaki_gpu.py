@@ -320,6 +320,99 @@ def test_ozaki_grouped_digit_widths(K, ora, bits, slices):
     plan.close()
 
 
+# ---------------------------------------------------------------------------
+# f32 GEMMs on the tensor cores (plan option f32_mode = PLAN_F32_OZAKI)
+# ---------------------------------------------------------------------------
+def _f32_problems(seed, count, hi=512, phi=0.0):
+    r = np.random.default_rng(seed)
+    lu = lambda lo, hi_, n: np.exp(r.uniform(np.log(lo), np.log(hi_), n)).astype(np.int64)  # noqa: E731
+    M, N, Kk = lu(1, hi, count), lu(1, hi, count), lu(1, hi, count)
+    probs = []
+    for i in range(count):
+        a = r.uniform(-1, 1, (M[i], Kk[i])) * np.exp(phi * r.normal(0, 1, (M[i], Kk[i])))
+        b = r.uniform(-1, 1, (Kk[i], N[i])) * np.exp(phi * r.normal(0, 1, (Kk[i], N[i])))
+        probs.append((_dev(a.astype(np.float32)), _dev(b.astype(np.float32)),
+                      torch.full((M[i], N[i]), float("nan"), dtype=torch.float32, device="cuda"), False))
+    return probs
+
+
+def test_plan_f32_on_tensor_cores_integer_known_answer(K):
+    """Integers |x| <= 64 with K <= 1000: every product sum is an integer
+    below 2^24, exact in f32, so C must equal it bit for bit."""
+    r = np.random.default_rng(21)
+    shapes = [(1, 7, 1), (129, 65, 257), (40, 1000, 300), (300, 33, 17), (128, 128, 128)]
+    probs, exact = [], []
+    for m, k, n in shapes:
+        A = r.integers(-64, 65, (m, k))
+        B = r.integers(-64, 65, (k, n))
+        exact.append((A @ B).astype(np.float32))
+        probs.append((_dev(A.astype(np.float32)), _dev(B.astype(np.float32)),
+                      torch.full((m, n), float("nan"), dtype=torch.float32, device="cuda"), False))
+    plan = K.Plan(probs, f32_mode=L.PLAN_F32_OZAKI)
+    n_tc, S, bits = plan.f32_info()
+    assert n_tc == len(shapes) and S >= 3 and bits in (6, 7, 8)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    for (_, _, c, _), e in zip(probs, exact):
+        np.testing.assert_array_equal(to_np(c), e)
+    plan.close()
+
+
+@pytest.mark.parametrize("phi", [0.0, 2.0])
+def test_plan_f32_on_tensor_cores_accuracy(K, ora, phi):
+    """Against the double-double product of the f32 operands: the error stays
+    at f32 rounding (componentwise <= 2^-23 of (|A||B|)_ij), at most the
+    FMA tiles' own error, with magnitudes spread by exp(phi N(0,1))."""
+    probs = _f32_problems(31, 40, phi=phi)
+    probs.append((_dev(np.random.default_rng(2).uniform(-1, 1, (40, 3000)).astype(np.float32)),
+                  _dev(np.random.default_rng(3).uniform(-1, 1, (3000, 90)).astype(np.float32)),
+                  torch.empty((40, 90), dtype=torch.float32, device="cuda"), False))
+    fma = [(a, b, torch.empty_like(c), acc) for a, b, c, acc in probs]
+    plan = K.Plan(probs, f32_mode=L.PLAN_F32_OZAKI)
+    assert plan.f32_info()[0] == len(probs)
+    plan.run(use_graph=True)
+    ref = K.Plan(fma)
+    ref.run(use_graph=False)
+    torch.cuda.synchronize()
+    for (a, b, c, _), (_, _, cf, _) in zip(probs, fma):
+        A64, B64 = to_np(a).astype(np.float64), to_np(b).astype(np.float64)
+        Cdd, ab = ora.gemm_dd(A64, B64)
+        e = _err(to_np(c).astype(np.float64), Cdd, ab)
+        ef = _err(to_np(cf).astype(np.float64), Cdd, ab)
+        assert e <= 2.0 ** -23 and e <= max(ef, 2.0 ** -24), (a.shape, b.shape, e, ef)
+    plan.close()
+    ref.close()
+
+
+def test_plan_f32_and_f64_on_tensor_cores_together(K, ora):
+    """Both groups in one plan with reductions, a NaN-holding f32 problem on
+    the FMA tiles, replayed from the graph after the inputs change."""
+    p64 = _group_problems(61, 12, hi=300)
+    p32 = _f32_problems(62, 12, hi=300)
+    bad = torch.rand((16, 16), device="cuda")
+    bad[2, 3] = float("nan")
+    p32.append((bad, bad.clone(), torch.empty((16, 16), device="cuda"), False))
+    x = [torch.randn(int(n), device="cuda") for n in (100, 70000)]
+    reds = [(v, L.SUM, torch.empty(1, device="cuda")) for v in x]
+    plan = K.Plan(p64 + p32, reds, f64_mode=L.PLAN_F64_OZAKI, f32_mode=L.PLAN_F32_OZAKI)
+    assert plan.f64_info()[0] == 12 and plan.f32_info()[0] == 12
+    for step in range(2):
+        if step:
+            for a, b, c, _ in p64 + p32[:12]:
+                a.mul_(-0.5)
+                c.fill_(float("nan"))
+        plan.run(use_graph=True)
+        torch.cuda.synchronize()
+        _check_against_dd(ora, K, p64)
+        for a, b, c, _ in p32[:12]:
+            Cdd, ab = ora.gemm_dd(to_np(a).astype(np.float64), to_np(b).astype(np.float64))
+            assert _err(to_np(c).astype(np.float64), Cdd, ab) <= 2.0 ** -23
+        assert torch.isnan(p32[12][2]).any()
+        for v, _, o in reds:
+            assert torch.equal(o.reshape(()), K.sum(v).reshape(()))
+    plan.close()
+
+
 def test_autotune_considers_tensor_core_f64(K, ora):
     probs = _group_problems(47, 80)
     f32 = []
@@ -328,14 +421,18 @@ def test_autotune_considers_tensor_core_f64(K, ora):
         f32.append((torch.rand((m, k), device="cuda"), torch.rand((k, n), device="cuda"),
                     torch.empty((m, n), device="cuda"), False))
     K.tuner_clear()
-    rep = K.autotune_plan(probs + f32, (), max_trials=8, reps=3, f64_ozaki=True)
+    rep = K.autotune_plan(probs + f32, (), max_trials=8, reps=3, f64_ozaki=True, f32_ozaki=True)
     assert rep["final_ms"] <= rep["untuned_ms"]
-    assert rep["ozaki_ms"] > 0
-    for a, b, c, _ in probs:
+    assert rep["ozaki_ms"] > 0 and rep["ozaki_f32_ms"] > 0
+    assert set(rep["plan_kwargs"]) == {"f64_mode", "f64_slices", "f64_digit_bits", "f32_mode"}
+    for a, b, c, _ in probs + f32:
         c.fill_(float("nan"))
     plan = K.Plan(probs + f32, (), **rep["plan_kwargs"])
     plan.run(use_graph=True)
     torch.cuda.synchronize()
     _check_against_dd(ora, K, probs[:20])
+    for a, b, c, _ in f32[:10]:
+        Cdd, ab = ora.gemm_dd(to_np(a).astype(np.float64), to_np(b).astype(np.float64))
+        assert _err(to_np(c).astype(np.float64), Cdd, ab) <= 1e-5
     plan.close()
     K.tuner_clear()
