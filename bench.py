@@ -507,11 +507,12 @@ def grouped_section(K, L, seed: int = 7, cpu: bool = True, peaks=None):
     and 4096 row reductions (length log-uniform in [64, 65536]) in one
     persistent launch replayed from a CUDA graph: untuned, with the f64
     GEMMs on the tensor cores, as chosen by the plan-level autotuner
-    (nrs_plan_autotune), and launched one by one. Roofline: the time the
-    group needs at the measured rates (f64 flops at the DMMA rate, or as BF16
-    slice products at the BF16 rate when the plan puts them on the tensor
-    cores; f32 flops at the FMA rate; reduction bytes at the HBM copy rate)
-    over the measured time."""
+    (nrs_plan_autotune, which also tries the f32 GEMMs on the tensor cores),
+    and launched one by one. Roofline: the time the group needs at the
+    measured rates (f64 and f32 flops at the DMMA / FMA rates, or as BF16
+    slice products at the BF16 rate for the GEMMs the plan puts on the
+    tensor cores; reduction bytes at the HBM copy rate) over the measured
+    time."""
     import numpy as np
     import torch
     r = np.random.default_rng(seed)
@@ -548,11 +549,12 @@ def grouped_section(K, L, seed: int = 7, cpu: bool = True, peaks=None):
     ms_o = _event_median_ms(lambda: plan_o.run(use_graph=True), 5, stream)
     plan_o.close()
     t_tune = time.perf_counter()
-    rep = K.autotune_plan(gemms, reds, max_trials=48, reps=3, f64_ozaki=True)
+    rep = K.autotune_plan(gemms, reds, max_trials=48, reps=3, f64_ozaki=True, f32_ozaki=True)
     tune_s = time.perf_counter() - t_tune
     plan = K.Plan(gemms, reds, **rep["plan_kwargs"])
     st = plan.stats()
     n_tc_final, s_final, b_final = plan.f64_info()
+    n32_final, s32_final, _ = plan.f32_info()
     ms_g = _event_median_ms(lambda: plan.run(use_graph=True), 5, stream)
     K.tuner_clear()
 
@@ -567,23 +569,32 @@ def grouped_section(K, L, seed: int = 7, cpu: bool = True, peaks=None):
            "grouped_graph_ms": round(ms_g, 3), "untuned_graph_ms": round(ms_h, 3),
            "f64_on_tensor_cores_untuned_ms": round(ms_o, 3),
            "f64_tensor_core_gemms": n_tc_final, "f64_slices": s_final, "f64_digit_bits": b_final,
+           "f32_tensor_core_gemms": n32_final, "f32_slices": s32_final,
            "f64_tensor_core_gemms_auto": n_tc, "f64_slices_auto": oz_s,
            "one_by_one_ms": round(ms_1, 3), "speedup_vs_one_by_one": round(ms_1 / ms_g, 2),
            "gflops": round(flops / ms_g / 1e6, 1), "f64_share_of_flops": round(f64_flops / flops, 3),
            "reduce_bytes": rbytes,
            "autotune": {"seconds": round(tune_s, 2), "buckets": rep["buckets"], "trials": rep["trials"],
                         "untuned_ms": round(rep["untuned_ms"], 3), "isolated_buckets_ms": round(rep["isolated_ms"], 3),
-                        "ozaki_mode_ms": round(rep["ozaki_ms"], 3), "final_ms": round(rep["final_ms"], 3),
+                        "ozaki_mode_ms": round(rep["ozaki_ms"], 3),
+                        "ozaki_f32_mode_ms": round(rep["ozaki_f32_ms"], 3), "final_ms": round(rep["final_ms"], 3),
                         "chosen": rep["plan_kwargs"]}}
     if peaks:
-        f32_t = f32_flops / (peaks["fp32_fma_tflops"] * 1e12)
+        # each part at its measured rate: f64 on DMMA or as BF16 slice
+        # products, f32 on FMA or as BF16 slice products, reductions at HBM
+        if n32_final:
+            f32_t = f32_flops * s32_final * (s32_final + 1) / 2 / (_bf16_peak() * 1e12)
+            f32_part = "f32 as BF16 slice products"
+        else:
+            f32_t = f32_flops / (peaks["fp32_fma_tflops"] * 1e12)
+            f32_part = "f32 FMA"
         red_t = rbytes / (_peaks()[0] * 1e9)
         dmma_t = f64_flops / (peaks["fp64_dmma_tflops"] * 1e12)
         if n_tc_final:
             bf16_t = f64_flops * s_final * (s_final + 1) / 2 / (_bf16_peak() * 1e12)
-            t_lb, bound = (bf16_t + f32_t + red_t) * 1e3, "mixed: f64 as BF16 slice products + f32 FMA + HBM"
+            t_lb, bound = (bf16_t + f32_t + red_t) * 1e3, f"mixed: f64 as BF16 slice products + {f32_part} + HBM"
         else:
-            t_lb, bound = (dmma_t + f32_t + red_t) * 1e3, "mixed: f64 DMMA + f32 FMA + HBM"
+            t_lb, bound = (dmma_t + f32_t + red_t) * 1e3, f"mixed: f64 DMMA + {f32_part} + HBM"
         out["roofline"] = {"bound": bound, "kernel": "ozaki_tc_kernel (grouped) + grouped_kernel",
                            "lower_bound_ms": round(t_lb, 3), "achieved_ms": round(ms_g, 3),
                            "frac": round(t_lb / ms_g, 4), "unit": "ms",

@@ -44,6 +44,8 @@ CASES = {
     "add_decode_f32": ("f32", None, None),
     "selector_train": (None, None, None),
     "grouped_ozaki": (None, None, None),
+    "c4_f64_ozaki": (None, None, None),
+    "c4_f32_ozaki": (None, None, None),
 }
 
 
@@ -132,6 +134,23 @@ def main():
         ms = torch.ones_like(ts)
         sel = K.Selector()
         fn = lambda: sel.train(xs, ts, ms, epochs=1)  # noqa: E731
+    elif a.case in ("c4_f64_ozaki", "c4_f32_ozaki"):
+        # bench.py's C4 group (seed 7: 4096 GEMMs, M, N, K log-uniform in
+        # [16, 512], even indices f32, odd f64), only its f64 (or f32) GEMMs,
+        # as one plan with them on the tensor cores, replayed from its graph
+        import numpy as np
+        r = np.random.default_rng(7)
+        lu = lambda lo, hi, k: np.exp(r.uniform(np.log(lo), np.log(hi), k)).astype(np.int64)  # noqa: E731
+        M, N, Kd = lu(16, 512, 4096), lu(16, 512, 4096), lu(16, 512, 4096)
+        f64 = a.case == "c4_f64_ozaki"
+        t = torch.float64 if f64 else torch.float32
+        gemms = []
+        for i in range(1 if f64 else 0, 4096, 2):
+            gemms.append((torch.empty((int(M[i]), int(Kd[i])), dtype=t, device="cuda").uniform_(-1, 1),
+                          torch.empty((int(Kd[i]), int(N[i])), dtype=t, device="cuda").uniform_(-1, 1),
+                          torch.empty((int(M[i]), int(N[i])), dtype=t, device="cuda"), False))
+        plan = K.Plan(gemms, f64_mode=L.PLAN_F64_OZAKI) if f64 else K.Plan(gemms, f32_mode=L.PLAN_F32_OZAKI)
+        fn = lambda: plan.run(use_graph=True)  # noqa: E731
     else:
         import numpy as np
         r = np.random.default_rng(7)
