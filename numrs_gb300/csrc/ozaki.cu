@@ -21,10 +21,12 @@
 //    every partial sum of a K <= 2^(26-2b) chunk (4096 for b = 7) is an
 //    integer of at most 2^24: the FP32 accumulation is EXACT.
 // 4. Cross-slice accumulation: the exact products of one diagonal
-//    (s + t = d) are summed as int32, then added once per diagonal into a
-//    per-element 128-bit integer at weight 2^(b(S-1-d)) -- exact, no FP64
-//    op -- and the most significant diagonal converts the total once to f64
-//    and applies 2^(e_a[i] + e_b[j] + 2 - 2b - b(S-1)).
+//    (s + t = d) are summed as int32 and carried, from d = S-1 up to d = 0,
+//    in one int32 per element: R <- floor(R / 2^b) + D_d, the low b bits of
+//    the old R being final (digit S-2-d). After d = 0 the exact total is
+//    T = R 2^(b(S-1)) + sum_t digit_t 2^(bt), rounded once to f64 with
+//    integer operations (no FP64 op) and scaled by
+//    2^(e_a[i] + e_b[j] + 2 - 2b - b(S-1)).
 //
 // The tensor-core kernel is persistent (one CTA per SM) and warp-specialised:
 //   warp 0      : TMA producer, 4-stage ring of A (128x64) + B (256x64) bf16
@@ -34,14 +36,13 @@
 //   warps 2..9  : epilogue (one TMEM lane = one tile row per thread, two warps
 //                 per lane quarter splitting the 256 columns): copy the
 //                 finished accumulator to registers, hand it back to the MMA
-//                 warp at once, fold the copy into the int32 diagonal sums
-//                 kept in TMEM columns 256..511, and add each finished
-//                 diagonal into an m x n array of int128 accumulators.
+//                 warp at once, fold the copy into the carried int32 sums R
+//                 kept in TMEM columns 256..511, write each retired digit as
+//                 a byte of the element's record in a per-CTA slot, and
+//                 round every element's exact total once after d = 0.
 // Grouped launches (many small problems, one tile list) use 128 x 128 tiles,
-// a 6-stage ring and two accumulators in turn, and replace the per-diagonal
-// int128 read-modify-write by carried int32 sums that retire one b-bit digit
-// per diagonal into a write-only per-CTA slot, combined once per tile (the
-// grouped epilogue below describes it).
+// a 6-stage ring and two accumulators in turn, and keep the digits in TMEM
+// and registers (the grouped epilogue below describes it).
 // Measured at 8192^3 (clock counters per warp): the MMA warp waits for TMA
 // data ~29% of its time and for the epilogue ~8%.
 // Every mbarrier wait is bounded; on give-up the kernel records an error
@@ -209,7 +210,7 @@ struct OzParams {
   int group_m;     // tile rasterisation group height
   const int* ea;   // row exponents of A
   const int* eb;   // column exponents of B
-  __int128* acc;   // exact accumulators: m x n (one problem) or a slot per CTA (grouped)
+  __int128* acc;   // per-CTA digit slots (16-byte aligned)
   double* C;
   int64_t ldc;
   int final_shift; // 2 - 2b - b(S-1) for b-bit digits
@@ -806,19 +807,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   } else {
     // ---------------- epilogue (warps 2..9) ----------------
     // Warp w reads TMEM lane quarter w % 4 (one tile row per thread) and
-    // column half (w - 2) / 4. The exact pair products of one diagonal
-    // (s + t = d, every K chunk) are summed as int32 in TMEM columns
-    // 256..511 (|sum| < 2^31 by the K limit checked on the host): per unit,
-    // load the accumulator, add it into the diagonal sums, store them back,
-    // and hand the accumulator to the MMA warp. Global memory is touched once
-    // per diagonal: the int128 accumulator gets D_d << 6(S-1-d), and the most
-    // significant diagonal converts the total to f64 into C.
+    // column half (w - 2) / 4 (128 columns). As in the grouped epilogue, one
+    // int32 per element, R (TMEM columns 256..511), carries the exact
+    // diagonal sums from d = S-1 to d = 0 (R <- floor(R / 2^b) + D_d) and
+    // the low b bits retire as digit S-2-d, here as a byte of the element's
+    // 16-byte record in this CTA's slot (column-major 128 x 256; written once
+    // per diagonal, read once).
+    // No global read-modify-write per diagonal; after d = 0 each element's
+    // exact total R 2^(b(S-1)) + sum_t digit_t 2^(bt) is rounded once to
+    // f64. Per group: copy the accumulator to registers, hand it back to the
+    // MMA warp at once, fold the copy into R.
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
     const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + half * (OZ_BN / 2);
     const uint32_t acc_t = lane_base;           // accumulator columns
-    const uint32_t dsum_t = lane_base + OZ_BN;  // diagonal-sum columns
+    const uint32_t dsum_t = lane_base + OZ_BN;  // R
+    const int b = P.digit_bits, S = P.slices, nd = S - 1;
+    const uint32_t dmask = (1u << b) - 1;
+    constexpr size_t pitch = (size_t)OZ_BM * 16;  // record bytes between tile columns
+    uint8_t* const slot = reinterpret_cast<uint8_t*>(P.acc) + (size_t)blockIdx.x * (OZ_BM * OZ_BN * 16) +
+                          (size_t)(half * (OZ_BN / 2)) * pitch + (size_t)row_in_tile * 16;
     uint32_t ai = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
@@ -826,14 +835,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int64_t row = tc.row0 + row_in_tile;
       const bool row_ok = row < tc.m;
       const int64_t col0 = tc.col0 + half * (OZ_BN / 2);
+      const int ncols = (int)(tc.n - col0 < OZ_BN / 2 ? (tc.n - col0 > 0 ? tc.n - col0 : 0) : OZ_BN / 2);
+      const int ecol_base = row_ok ? tc.ea[row] + P.final_shift : 0;
       const int gm = merge_count(tc, P, false);
       PairIter pr;
-      pr.start(P.slices);
-      for (int u = 0; u < tc.n_pairs; ++ai) {
+      pr.start(S);
+      for (int u = 0; u < tc.n_pairs && ok; ++ai) {
         const int g = group_size(pr, gm, tc.kchunks);
         const int d = pr.d;
         const bool diag_start = pr.diag_first();
-        const bool diag_end = g == pr.left(tc.kchunks);  // the group closes its diagonal
+        const bool tile_first = u == 0;
         u += g;
         for (int j = 0; j < g; ++j) pr.next(tc.kchunks);
         const uint32_t aph = ai & 1;
@@ -841,7 +852,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_after();
         // Copy this warp's 128 accumulator columns to registers (eight loads,
         // one wait) and hand the accumulator back at once, so the next unit's
-        // MMAs run while the copy is folded into the diagonal sums.
+        // MMAs run while the copy is folded into R.
         uint32_t v[OZ_BN / 2];
 #pragma unroll
         for (int c = 0; c < OZ_BN / 32; ++c) tmem_ld16_nowait(acc_t + c * 16, v + c * 16);
@@ -849,59 +860,56 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acce[0]);
+        const int dig_i = nd - 1 - d;  // digit index of diagonal d + 1
 #pragma unroll
-        for (int c = 0; c < OZ_BN / 32; c += 2) {
-          uint32_t w[32];
-          if (!diag_start) {
-            tmem_ld16_nowait(dsum_t + c * 16, w);
-            tmem_ld16_nowait(dsum_t + (c + 1) * 16, w + 16);
-            tmem_wait_ld();
+        for (int c = 0; c < OZ_BN / 32; ++c) {
+          uint32_t w[16];
+          if (tile_first) {
 #pragma unroll
-            for (int e = 0; e < 32; ++e)
-              w[e] = (uint32_t)((int32_t)w[e] + __float2int_rn(__uint_as_float(v[c * 16 + e])));
+            for (int e = 0; e < 16; ++e) w[e] = (uint32_t)__float2int_rn(__uint_as_float(v[c * 16 + e]));
           } else {
+            tmem_ld16(dsum_t + c * 16, w);
+            if (diag_start) {
+              uint8_t* sp = slot + (size_t)(c * 16) * pitch + dig_i;
+              const int nv = row_ok ? ncols - c * 16 : 0;  // columns of this chunk inside the problem
 #pragma unroll
-            for (int e = 0; e < 32; ++e) w[e] = (uint32_t)__float2int_rn(__uint_as_float(v[c * 16 + e]));
+              for (int e = 0; e < 16; ++e) {
+                const int32_t r = (int32_t)w[e];
+                if (e < nv) sp[(size_t)e * pitch] = (uint8_t)((uint32_t)r & dmask);
+                w[e] = (uint32_t)((r >> b) + __float2int_rn(__uint_as_float(v[c * 16 + e])));
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e)
+                w[e] = (uint32_t)((int32_t)w[e] + __float2int_rn(__uint_as_float(v[c * 16 + e])));
+            }
           }
-          tmem_st16(dsum_t + c * 16, *reinterpret_cast<const uint32_t(*)[16]>(w));
-          tmem_st16(dsum_t + (c + 1) * 16, *reinterpret_cast<const uint32_t(*)[16]>(w + 16));
+          tmem_st16(dsum_t + c * 16, w);
         }
         tmem_wait_st();
         tc_fence_before();
         __syncwarp();
-        if (!diag_end) continue;
-        const bool first = (d == P.slices - 1), last = (d == 0);
-        const int shift = P.digit_bits * (P.slices - 1 - d);
-        const int ecol_base = (last && row_ok) ? tc.ea[row] + P.final_shift : 0;
-        // The int128 accumulators: an m x n row-major array (measured 5%
-        // faster at 8192^3 than per-CTA slots, whose 78 MB compete in L2 with
-        // the slice panels the tensor cores stream).
-        __int128* const accp = P.acc + (row_ok ? row : 0) * tc.n + col0;
+      }
+      if (!ok) break;
+      // After the last group of d = 0: R and the records of 8 columns at a
+      // time (loads in flight together), rounded once, written to C.
 #pragma unroll 1
-        for (int c = 0; c < OZ_BN / 32; ++c) {
-          uint32_t w[16];
-          tmem_ld16(dsum_t + c * 16, w);
-          if (!row_ok) continue;
+      for (int c8 = 0; c8 < OZ_BN / 2; c8 += 8) {
+        if (c8 >= ncols) break;  // warp-uniform
+        uint32_t w[8], lw[8], hw[8];
+        tmem_ld8_nowait(dsum_t + c8, w);
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            const int j = c * 16 + e;
-            const int64_t col = col0 + j;
-            if (col >= tc.n) continue;
-            const __int128 contrib = ((__int128)(int32_t)w[e]) << shift;
-            __int128* ap = accp + j;
-            const __int128 sum = first ? contrib : (*ap + contrib);
-            if (!last) {
-              *ap = sum;
-            } else {
-              // |sum| < 2^127: rounded once to f64.
-              const bool neg = sum < 0;
-              const unsigned __int128 mag = neg ? (unsigned __int128)(-sum) : (unsigned __int128)sum;
-              const double r = int128_to_f64(neg, (uint64_t)(mag >> 64), (uint64_t)mag, ecol_base + tc.eb[col]);
-              double* cp = (double*)tc.C + row * tc.ldc + col;
-              *cp = tc.accumulate ? *cp + r : r;
-            }
-          }
+        for (int e = 0; e < 8; ++e) {
+          uint64_t r = 0;
+          if (row_ok && c8 + e < ncols)
+            r = __ldcg(reinterpret_cast<const unsigned long long*>(slot + (size_t)(c8 + e) * pitch));
+          lw[e] = (uint32_t)r;
+          hw[e] = (uint32_t)(r >> 32);
         }
+        tmem_wait_ld();
+        if (!row_ok) continue;
+        retire8<false>(w, lw, hw, slot + (size_t)c8 * pitch + 8, pitch, tc.eb + col0 + c8, ncols - c8, b, S,
+                       ecol_base, tc.C, row * tc.ldc + col0 + c8, tc.accumulate);
       }
     }
   }
@@ -1488,11 +1496,14 @@ int spread_estimate(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int6
 int ozaki_run(nrs_handle* h, const OzOperand& a, const OzOperand& bT, int64_t m, int64_t n, int64_t k,
               int64_t kpad, int b, int S, int kchunks, double* C, int64_t ldc, bool accumulate) {
   auto al = [](size_t v) { return (v + 1023) & ~size_t(1023); };
-  // Workspace: exponents | A slices | B slices | int128 accumulators (the
-  // column maxima of a column-major operand go through the accumulators).
+  // Workspace: exponents | A slices | B slices | digit slots, one 128 x 256
+  // x 16-byte slot per CTA (the column maxima of a column-major operand go
+  // through the slots first).
   const size_t ea_b = al((size_t)m * 4), eb_b = al((size_t)n * 4);
   const size_t sa_b = al((size_t)S * m * kpad * 2), sb_b = al((size_t)S * n * kpad * 2);
-  const size_t acc_b = al(std::max((size_t)m * n * 16, (size_t)std::max(m, n) * 8));
+  const int64_t tiles = ((m + OZ_BM - 1) / OZ_BM) * ((n + OZ_BN - 1) / OZ_BN);
+  const int64_t ctas = std::min<int64_t>(tiles, h->hw_sms);
+  const size_t acc_b = al(std::max((size_t)ctas * OZ_BM * OZ_BN * 16, (size_t)std::max(m, n) * 8));
   int st;
   uint8_t* ws = (uint8_t*)nrs_workspace(h, ea_b + eb_b + sa_b + sb_b + acc_b, &st);
   if (!ws) return st;
