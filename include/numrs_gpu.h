@@ -381,7 +381,8 @@ typedef struct nrs_ozaki_info {
 /* C := A*B (or C += A*B with NRS_GEMM_ACCUMULATE) in f64 accuracy from BF16
  * slice products on tcgen05 tensor cores with per-row (A) / per-column (B)
  * power-of-two scaling, exact fp32 accumulation inside K blocks, exact int32
- * cross-block and int128 cross-slice accumulation, one conversion to f64.
+ * sums carried across the slice diagonals (one retired digit per diagonal),
+ * one exactly rounded conversion to f64 per element.
  * No reference counterpart: replaces the f64 tier of gemm_2d
  * (src/kernels/gemm.rs:290) for large problems. Operands as in nrs_gemm
  * (row-major, NRS_GEMM_TRANS_A / _TRANS_B for transposed views); operands
