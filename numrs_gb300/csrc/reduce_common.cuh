@@ -161,6 +161,12 @@ struct RunFold {
     if constexpr (OP == NRS_MAX) return v > a ? v : a;
     else return v < a ? v : a;
   }
+  // pick for operands that are neither NaN nor zero: one max / min
+  // instruction (equal operands then have equal bits).
+  static __device__ __forceinline__ T pick_plain(T a, T v) {
+    if constexpr (OP == NRS_MAX) return fmax(a, v);
+    else return fmin(a, v);
+  }
 
   template <int N, typename Get>
   static __device__ __forceinline__ T run(T acc, Get get) {
@@ -180,8 +186,8 @@ struct RunFold {
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         const T v = get(i);
-        special |= (v != v) | (v == T(0));
-        a[i & 3] = pick(a[i & 3], v);
+        special |= !(fabs(v) > T(0));  // NaN or a zero
+        a[i & 3] = pick_plain(a[i & 3], v);
       }
       if (!special) return pick(pick(a[0], a[1]), pick(a[2], a[3]));
 #pragma unroll
