@@ -173,3 +173,69 @@ NRS_HD void ozaki_exact_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S,
   mlo = neg ? ~tl + 1 : tl;
   mhi = neg ? ~th + (tl == 0 ? 1 : 0) : th;
 }
+
+// ---------------------------------------------------------------------------
+// Slicing with 64-bit integers when b S <= 64
+// ---------------------------------------------------------------------------
+// The slicers round X = x 2^(126-e) (exact for |x| < 2^e) to a multiple of
+// 2^p, p = 127 - bS (ties up), and read S signed b-bit digits off
+// Z = X + 2^(p-1) + h sum_t 2^(p_t) (h = 2^(b-1), p_t = 127 - b - bt). With
+// b S <= 64 the same digits come from 64-bit arithmetic:
+//   Y = floor((X + 2^(p-1)) / 2^p) = round-half-up(x 2^(bS-1-e)), |Y| < 2^63,
+//   Z' = Y + h sum_t 2^(b(S-1-t)) = Z >> p  (0 <= Z' < 2^(bS+1)),
+// digit t = field t of Z' minus h; the top field can need a ninth bit (bit
+// bS of Z', or for b S = 64 the carry-out of the add).
+NRS_HD int64_t ozaki_round_y(double x, int e, int bS) {
+  uint64_t bits;
+  memcpy(&bits, &x, sizeof bits);
+  const bool neg = bits >> 63;
+  const int biased = (int)((bits >> 52) & 0x7FF);
+  uint64_t mant = bits & 0xFFFFFFFFFFFFFull;
+  int E;
+  if (biased == 0) {
+    E = -1074;
+  } else {
+    mant |= 1ull << 52;
+    E = biased - 1075;  // x = mant 2^E
+  }
+  if (mant == 0) return 0;
+  const int sh = E + bS - 1 - e;
+  if (sh >= 0) {  // exact; below 2^63 because |x| < 2^e
+    const int64_t m = (int64_t)(mant << sh);
+    return neg ? -m : m;
+  }
+  const int k = -sh;
+  if (k >= 64) return 0;  // |x 2^(bS-1-e)| < 2^-11
+  const uint64_t half = 1ull << (k - 1);
+  // floor((+-mant 2^-k) + 1/2): up for a positive half, toward zero for a negative one
+  return neg ? -(int64_t)((mant + half - 1) >> k) : (int64_t)((mant + half) >> k);
+}
+
+NRS_HD uint64_t ozaki_offset64(int S, int b) {
+  uint64_t c = 0;
+  for (int t = 0; t < S; ++t) c += (uint64_t)1 << (b - 1) << (b * (S - 1 - t));
+  return c;
+}
+
+// Z' left-aligned (digit t in bits [64 - b(t+1), 64 - bt)) and the carry-out
+// of Y + offset, from which ozaki_digit64 reads digit t.
+struct OzakiZ64 {
+  uint64_t z;
+  uint32_t carry;
+};
+NRS_HD OzakiZ64 ozaki_z64(double x, int e, int b, int S, uint64_t offset) {
+  const int bS = b * S;
+  const int64_t Y = ozaki_round_y(x, e, bS);
+  const uint64_t z = (uint64_t)Y + offset;
+  OzakiZ64 r;
+  // the top field's ninth bit: bit bS of Z' (below 2^(bS+1)), or for
+  // b S = 64 the carry-out of the 64-bit add
+  r.carry = bS < 64 ? (uint32_t)((z >> bS) & 1) : (uint32_t)((Y >= 0) && (z < offset));
+  r.z = bS < 64 ? z << (64 - bS) : z;
+  return r;
+}
+template <int B>
+NRS_HD int ozaki_digit64(const OzakiZ64& z, int t) {
+  const int f = (int)(uint32_t)(z.z >> (64 - B * (t + 1)));
+  return (t == 0 ? (f | (int)(z.carry << B)) : (f & ((1 << B) - 1))) - (1 << (B - 1));
+}

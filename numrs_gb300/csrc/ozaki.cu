@@ -1036,13 +1036,15 @@ __device__ __forceinline__ uint32_t bf16_of_int(int v) {
 // A (m x k) -> slices [S][m][kpad], K-major; zero beyond k. A thread takes 8
 // consecutive k of one row (kpad is a multiple of 8; four 16-byte loads when
 // aligned) and writes one 16-byte vector per slice.
-template <int b, bool VEC>
+// SMALL (b S <= 64): the same digits from 64-bit arithmetic (ozaki_z64).
+template <int b, bool VEC, bool SMALL>
 __global__ void __launch_bounds__(256)
     slice_rows(const double* __restrict__ A, int64_t m, int64_t k, int64_t lda, int64_t kpad,
                const int* __restrict__ ea, int S, uint16_t* __restrict__ out) {
   const int64_t gpr = kpad / 8;
   const int64_t total = m * gpr;
   const unsigned __int128 C = digit_offset(S, b);
+  const uint64_t C64 = ozaki_offset64(S, b);
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = g / gpr, j0 = (g - i * gpr) * 8;
@@ -1062,18 +1064,35 @@ __global__ void __launch_bounds__(256)
     }
     // The eight offset values, then one slice at a time (one 16-byte store
     // each), so only the current slice's packed words are live.
-    unsigned __int128 Z[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) Z[q] = (unsigned __int128)fixed126(x[q], e) + C;
     uint16_t* o = out + i * kpad + j0;
+    if constexpr (SMALL) {
+      OzakiZ64 Z[8];
 #pragma unroll
-    for (int t = 0; t < OZ_MAX_SLICES; ++t) {
-      if (t < S) {
-        uint32_t pk[4];
+      for (int q = 0; q < 8; ++q) Z[q] = ozaki_z64(x[q], e, b, S, C64);
 #pragma unroll
-        for (int h = 0; h < 4; ++h)
-          pk[h] = bf16_of_int(digit_at<b>(Z[2 * h], t)) | (bf16_of_int(digit_at<b>(Z[2 * h + 1], t)) << 16);
-        *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+        if (t < S) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h)
+            pk[h] = bf16_of_int(ozaki_digit64<b>(Z[2 * h], t)) |
+                    (bf16_of_int(ozaki_digit64<b>(Z[2 * h + 1], t)) << 16);
+          *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      }
+    } else {
+      unsigned __int128 Z[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) Z[q] = (unsigned __int128)fixed126(x[q], e) + C;
+#pragma unroll
+      for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+        if (t < S) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h)
+            pk[h] = bf16_of_int(digit_at<b>(Z[2 * h], t)) | (bf16_of_int(digit_at<b>(Z[2 * h + 1], t)) << 16);
+          *reinterpret_cast<uint4*>(o + (int64_t)t * m * kpad) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
       }
     }
   }
@@ -1085,7 +1104,7 @@ __global__ void __launch_bounds__(256)
 // words] (the pad word keeps both phases free of bank conflicts), then every
 // thread writes one 16-byte vector (8 k of one n row) per slice.
 constexpr int kSliceColK = 64, kSliceColN = 32, kSliceColPitch = kSliceColK / 2 + 1;
-template <int b>
+template <int b, bool SMALL>
 __global__ void __launch_bounds__(256)
     slice_cols(const double* __restrict__ B, int64_t k, int64_t n, int64_t ldb, int64_t kpad,
                const int* __restrict__ eb, int S, uint16_t* __restrict__ out) {
@@ -1093,6 +1112,7 @@ __global__ void __launch_bounds__(256)
   const int64_t k0 = (int64_t)blockIdx.y * kSliceColK, n0 = (int64_t)blockIdx.x * kSliceColN;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const unsigned __int128 C = digit_offset(S, b);
+  const uint64_t C64 = ozaki_offset64(S, b);
   {
     const int64_t nn = n0 + tx;
     const int e = nn < n ? eb[nn] : 0;
@@ -1100,15 +1120,24 @@ __global__ void __launch_bounds__(256)
     for (int r = 0; r < kSliceColK / 16; ++r) {  // word column w = ty + 8r: k rows 2w, 2w+1
       const int w = ty + 8 * r;
       const int64_t kk = k0 + 2 * w;
-      const unsigned __int128 Z0 =
-          (unsigned __int128)(kk < k && nn < n ? fixed126(B[kk * ldb + nn], e) : (__int128)0) + C;
-      const unsigned __int128 Z1 =
-          (unsigned __int128)(kk + 1 < k && nn < n ? fixed126(B[(kk + 1) * ldb + nn], e) : (__int128)0) + C;
+      const double x0 = kk < k && nn < n ? B[kk * ldb + nn] : 0.0;
+      const double x1 = kk + 1 < k && nn < n ? B[(kk + 1) * ldb + nn] : 0.0;
+      if constexpr (SMALL) {
+        const OzakiZ64 Z0 = ozaki_z64(x0, e, b, S, C64), Z1 = ozaki_z64(x1, e, b, S, C64);
 #pragma unroll
-      for (int t = 0; t < OZ_MAX_SLICES; ++t)
-        if (t < S)
-          tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
-              bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
+        for (int t = 0; t < OZ_MAX_SLICES; ++t)
+          if (t < S)
+            tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+                bf16_of_int(ozaki_digit64<b>(Z0, t)) | (bf16_of_int(ozaki_digit64<b>(Z1, t)) << 16);
+      } else {
+        const unsigned __int128 Z0 = (unsigned __int128)fixed126(x0, e) + C;
+        const unsigned __int128 Z1 = (unsigned __int128)fixed126(x1, e) + C;
+#pragma unroll
+        for (int t = 0; t < OZ_MAX_SLICES; ++t)
+          if (t < S)
+            tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+                bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
+      }
     }
   }
   __syncthreads();
@@ -1310,28 +1339,36 @@ int launch_exponents(nrs_handle* h, const OzOperand& o, int64_t k, int* e,
   return nrs_after_launch(h, "ozaki exponents");
 }
 
-template <int b>
-int launch_slices_b(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int S,
-                    uint16_t* out) {
+template <int b, bool SMALL>
+int launch_slices_bs(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int S,
+                     uint16_t* out) {
   cudaStream_t s = h->stream;
   if (o.rows_contig) {
     const int64_t groups = o.rows * (kpad / 8);
     const int grid = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)h->num_sms * 8);
     // 16-byte row loads when every row start is 16-byte aligned.
     if (((reinterpret_cast<uintptr_t>(o.p) & 15) == 0) && (o.ld % 2 == 0))
-      slice_rows<b, true><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
+      slice_rows<b, true, SMALL><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
     else
-      slice_rows<b, false><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
+      slice_rows<b, false, SMALL><<<grid, 256, 0, s>>>(o.d(), o.rows, k, o.ld, kpad, e, S, out);
   } else {
     const int smem = (int)((size_t)S * kSliceColN * kSliceColPitch * 4);
-    int st = nrs_cuda_check(h, cudaFuncSetAttribute(slice_cols<b>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    smem),
+    int st = nrs_cuda_check(h,
+                            cudaFuncSetAttribute(slice_cols<b, SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 smem),
                             "cudaFuncSetAttribute(slice_cols)");
     if (st) return st;
     dim3 g((unsigned)((o.rows + kSliceColN - 1) / kSliceColN), (unsigned)((kpad + kSliceColK - 1) / kSliceColK));
-    slice_cols<b><<<g, 256, smem, s>>>(o.d(), k, o.rows, o.ld, kpad, e, S, out);
+    slice_cols<b, SMALL><<<g, 256, smem, s>>>(o.d(), k, o.rows, o.ld, kpad, e, S, out);
   }
   return nrs_after_launch(h, "ozaki slicing");
+}
+// b S <= 64: the 64-bit digit path (the same digits, fewer integer operations)
+template <int b>
+int launch_slices_b(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int S,
+                    uint16_t* out) {
+  return b * S <= 64 ? launch_slices_bs<b, true>(h, o, k, kpad, e, S, out)
+                     : launch_slices_bs<b, false>(h, o, k, kpad, e, S, out);
 }
 
 int launch_slices(nrs_handle* h, const OzOperand& o, int64_t k, int64_t kpad, const int* e, int b, int S,
@@ -1599,7 +1636,7 @@ __global__ void __launch_bounds__(256)
 
 // A slices of every problem: a block takes 8 rows of one problem, a thread 8
 // consecutive k of one row (zero beyond k, up to the problem's kpad).
-template <typename T, int b>
+template <typename T, int b, bool SMALL>
 __global__ void __launch_bounds__(256)
     g_slice_rows(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ ea, int S,
                  int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
@@ -1607,30 +1644,48 @@ __global__ void __launch_bounds__(256)
   const OzIn q = in[c.prob];
   const int64_t groups = q.kpad / 8;
   const unsigned __int128 C = digit_offset(S, b);
+  const uint64_t C64 = ozaki_offset64(S, b);
   for (int64_t w = threadIdx.x; w < 8 * groups; w += blockDim.x) {
     const int64_t row = (int64_t)c.r0 + w / groups, j0 = (w % groups) * 8;
     if (row >= q.m) break;  // w only grows: every later item is beyond m too
     const int e = ea[q.rowoff + row];
     const T* src = static_cast<const T*>(q.A) + row * q.lda + j0;
-    unsigned __int128 Z[8];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) Z[t] = (unsigned __int128)fixed126(j0 + t < q.k ? (double)src[t] : 0.0, e) + C;
     uint16_t* o = out + (q.rowoff + row) * pitch + j0;
+    if constexpr (SMALL) {
+      OzakiZ64 Z[8];
 #pragma unroll
-    for (int t = 0; t < OZ_MAX_SLICES; ++t) {
-      if (t < S) {
-        uint32_t pk[4];
+      for (int t = 0; t < 8; ++t) Z[t] = ozaki_z64(j0 + t < q.k ? (double)src[t] : 0.0, e, b, S, C64);
 #pragma unroll
-        for (int hh = 0; hh < 4; ++hh)
-          pk[hh] = bf16_of_int(digit_at<b>(Z[2 * hh], t)) | (bf16_of_int(digit_at<b>(Z[2 * hh + 1], t)) << 16);
-        *reinterpret_cast<uint4*>(o + (int64_t)t * plane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+        if (t < S) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int hh = 0; hh < 4; ++hh)
+            pk[hh] = bf16_of_int(ozaki_digit64<b>(Z[2 * hh], t)) |
+                     (bf16_of_int(ozaki_digit64<b>(Z[2 * hh + 1], t)) << 16);
+          *reinterpret_cast<uint4*>(o + (int64_t)t * plane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      }
+    } else {
+      unsigned __int128 Z[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) Z[t] = (unsigned __int128)fixed126(j0 + t < q.k ? (double)src[t] : 0.0, e) + C;
+#pragma unroll
+      for (int t = 0; t < OZ_MAX_SLICES; ++t) {
+        if (t < S) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int hh = 0; hh < 4; ++hh)
+            pk[hh] = bf16_of_int(digit_at<b>(Z[2 * hh], t)) | (bf16_of_int(digit_at<b>(Z[2 * hh + 1], t)) << 16);
+          *reinterpret_cast<uint4*>(o + (int64_t)t * plane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
       }
     }
   }
 }
 
 // B^T slices of every problem: slice_cols' 64 k x 32 n transposing tile.
-template <typename T, int b>
+template <typename T, int b, bool SMALL>
 __global__ void __launch_bounds__(256)
     g_slice_cols(const OzIn* __restrict__ in, const OzChunk* __restrict__ ch, const int* __restrict__ eb, int S,
                  int64_t pitch, int64_t plane, uint16_t* __restrict__ out) {
@@ -1640,6 +1695,7 @@ __global__ void __launch_bounds__(256)
   const int64_t k0 = c.k0, n0 = c.r0;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const unsigned __int128 C = digit_offset(S, b);
+  const uint64_t C64 = ozaki_offset64(S, b);
   const T* const Bq = static_cast<const T*>(q.B);
   {
     const int64_t nn = n0 + tx;
@@ -1648,15 +1704,24 @@ __global__ void __launch_bounds__(256)
     for (int r = 0; r < kSliceColK / 16; ++r) {
       const int w = ty + 8 * r;
       const int64_t kk = k0 + 2 * w;
-      const unsigned __int128 Z0 =
-          (unsigned __int128)(kk < q.k && nn < q.n ? fixed126((double)Bq[kk * q.ldb + nn], e) : (__int128)0) + C;
-      const unsigned __int128 Z1 =
-          (unsigned __int128)(kk + 1 < q.k && nn < q.n ? fixed126((double)Bq[(kk + 1) * q.ldb + nn], e) : (__int128)0) + C;
+      const double x0 = kk < q.k && nn < q.n ? (double)Bq[kk * q.ldb + nn] : 0.0;
+      const double x1 = kk + 1 < q.k && nn < q.n ? (double)Bq[(kk + 1) * q.ldb + nn] : 0.0;
+      if constexpr (SMALL) {
+        const OzakiZ64 Z0 = ozaki_z64(x0, e, b, S, C64), Z1 = ozaki_z64(x1, e, b, S, C64);
 #pragma unroll
-      for (int t = 0; t < OZ_MAX_SLICES; ++t)
-        if (t < S)
-          tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
-              bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
+        for (int t = 0; t < OZ_MAX_SLICES; ++t)
+          if (t < S)
+            tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+                bf16_of_int(ozaki_digit64<b>(Z0, t)) | (bf16_of_int(ozaki_digit64<b>(Z1, t)) << 16);
+      } else {
+        const unsigned __int128 Z0 = (unsigned __int128)fixed126(x0, e) + C;
+        const unsigned __int128 Z1 = (unsigned __int128)fixed126(x1, e) + C;
+#pragma unroll
+        for (int t = 0; t < OZ_MAX_SLICES; ++t)
+          if (t < S)
+            tile[(t * kSliceColN + tx) * kSliceColPitch + w] =
+                bf16_of_int(digit_at<b>(Z0, t)) | (bf16_of_int(digit_at<b>(Z1, t)) << 16);
+      }
     }
   }
   __syncthreads();
@@ -1968,19 +2033,23 @@ int nrs_ozaki_group_build(nrs_handle* h, int64_t count, const nrs_gemm_desc* d, 
   return NRS_OK;
 }
 
+template <typename T, int b, bool SMALL>
+int group_slices_s(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
+  const int64_t plane_a = G->rows_a * G->pitch, plane_b = G->rows_b * G->pitch;
+  g_slice_rows<T, b, SMALL><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea, G->S, G->pitch,
+                                                                 plane_a, G->d_sa);
+  const int smem = (int)((size_t)G->S * kSliceColN * kSliceColPitch * 4);
+  int st = nrs_cuda_check(
+      h, cudaFuncSetAttribute(g_slice_cols<T, b, SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+      "cudaFuncSetAttribute(g_slice_cols)");
+  if (st) return st;
+  g_slice_cols<T, b, SMALL><<<(unsigned)G->n_slcol, 256, smem, s>>>(G->d_in, G->d_slcol, G->d_eb, G->S, G->pitch,
+                                                                   plane_b, G->d_sb);
+  return nrs_after_launch(h, "grouped ozaki slicing");
+}
 template <typename T, int b>
 int group_slices(nrs_handle* h, nrs_ozaki_group* G, cudaStream_t s) {
-  const int64_t plane_a = G->rows_a * G->pitch, plane_b = G->rows_b * G->pitch;
-  g_slice_rows<T, b><<<(unsigned)G->n_rowch, 256, 0, s>>>(G->d_in, G->d_rowch, G->d_ea, G->S, G->pitch, plane_a,
-                                                          G->d_sa);
-  const int smem = (int)((size_t)G->S * kSliceColN * kSliceColPitch * 4);
-  int st = nrs_cuda_check(h,
-                          cudaFuncSetAttribute(g_slice_cols<T, b>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-                          "cudaFuncSetAttribute(g_slice_cols)");
-  if (st) return st;
-  g_slice_cols<T, b><<<(unsigned)G->n_slcol, 256, smem, s>>>(G->d_in, G->d_slcol, G->d_eb, G->S, G->pitch, plane_b,
-                                                            G->d_sb);
-  return nrs_after_launch(h, "grouped ozaki slicing");
+  return b * G->S <= 64 ? group_slices_s<T, b, true>(h, G, s) : group_slices_s<T, b, false>(h, G, s);
 }
 
 template <typename T>

@@ -40,6 +40,11 @@ extern "C" uint32_t nrs_test_f32(uint64_t hi, uint64_t lo, int e, int neg, int f
   *special = sp;
   return (uint32_t)r;
 }
+extern "C" void nrs_test_digits64(double x, int e, int b, int S, int* out) {
+  const OzakiZ64 z = ozaki_z64(x, e, b, S, ozaki_offset64(S, b));
+  for (int t = 0; t < S; ++t)
+    out[t] = b == 8 ? ozaki_digit64<8>(z, t) : b == 7 ? ozaki_digit64<7>(z, t) : ozaki_digit64<6>(z, t);
+}
 extern "C" void nrs_test_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int* neg, uint64_t* mhi,
                                uint64_t* mlo) {
   bool n = false;
@@ -200,3 +205,40 @@ def test_int128_to_f32_exact_and_fast(lib):
             n_fast += 1
             assert got == want, ("fast", hex(m), e, neg, hex(got), hex(want))
     assert n_fast > 10000
+
+
+def _digits128(x, e, b, S):
+    """The slicers' 128-bit digits: X = x 2^(126-e), Z = X + 2^(p-1) +
+    h sum_t 2^(p_t), digit t = field t of Z minus h (p_t = 127 - b - bt)."""
+    X = int(Fraction(x) * Fraction(2) ** (126 - e))  # exact for |x| < 2^e
+    h = 1 << (b - 1)
+    p = [127 - b - b * t for t in range(S)]
+    Z = X + (1 << (p[S - 1] - 1)) + sum(h << pt for pt in p)
+    return [((Z >> p[t]) if t == 0 else ((Z >> p[t]) & ((1 << b) - 1))) - h for t in range(S)]
+
+
+@pytest.mark.parametrize("b", [8, 7, 6])
+def test_slice_digits64_equal_the_128bit_digits(lib, b):
+    """The 64-bit slicing form gives the 128-bit form's digits for every
+    b S <= 64: random doubles of every magnitude below 2^e (subnormals and
+    zeros included), rounding ties, and values next to the row maximum."""
+    import math
+    f = lib.nrs_test_digits64
+    f.restype = None
+    f.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    out = (ctypes.c_int * 16)()
+    r = random.Random(100 + b)
+    for S in range(1, 17):
+        if b * S > 64:
+            continue
+        xs = []
+        for _ in range(300):
+            e = r.randint(-1060, 1000)
+            xs.append((r.uniform(-1, 1) * 2.0 ** (e - r.choice([0, 0, 1, 5, 20, 60])), e))
+        xs += [(0.0, 3), (-0.0, 3), (5e-324, -1021), (-5e-324, -1021), (math.ldexp(1 - 2 ** -53, 7), 7),
+               (-math.ldexp(1 - 2 ** -53, 7), 7), (math.ldexp(1, -b * S), 1), (-math.ldexp(1, -b * S), 1),
+               (math.ldexp(3, -b * S - 1), 1), (-math.ldexp(3, -b * S - 1), 1)]
+        for x, e in xs:
+            assert abs(x) < 2.0 ** e
+            f(x, e, b, S, out)
+            assert list(out[:S]) == _digits128(x, e, b, S), (x, e, b, S)
