@@ -168,6 +168,31 @@ NRS_DEV int swz(int r, int j) { return r * 128 + ((j ^ (r & 7)) << 4); }
 // the canonical NaN), so the value chain is one compare and select (ties keep
 // the later operand, as apply does).
 template <typename T, int OP, int N>
+NRS_DEV T run_block(T (&v)[N], bool first, T acc);
+
+// The same fold's result without the prefixes (reductions). Float maximum /
+// minimum are order-free over values that hold no NaN and no zero (equal
+// values then have equal bits), so such blocks fold as four independent
+// fmax / fmin chains; a block with a NaN or a zero, or a NaN accumulator,
+// takes the sequential chain. Other ops: the sequential chain.
+template <typename T, int OP, int N>
+NRS_DEV T reduce_block(T (&v)[N], bool first, T acc) {
+  if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
+    bool special = !first && acc != acc;
+#pragma unroll
+    for (int e = 0; e < N; ++e) special |= !(fabs(v[e]) > T(0));
+    if (!special) {
+      T a[4] = {first ? v[0] : acc, v[1], v[2], v[3]};
+      if (!first) a[0] = OP == NRS_OP_MAX ? fmax(a[0], v[0]) : fmin(a[0], v[0]);
+#pragma unroll
+      for (int e = 4; e < N; ++e) a[e & 3] = OP == NRS_OP_MAX ? fmax(a[e & 3], v[e]) : fmin(a[e & 3], v[e]);
+      return OP == NRS_OP_MAX ? fmax(fmax(a[0], a[1]), fmax(a[2], a[3])) : fmin(fmin(a[0], a[1]), fmin(a[2], a[3]));
+    }
+  }
+  return run_block<T, OP, N>(v, first, acc);
+}
+
+template <typename T, int OP, int N>
 NRS_DEV T run_block(T (&v)[N], bool first, T acc) {
   if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN)) {
     bool nanf = acc != acc;
@@ -203,7 +228,7 @@ NRS_DEV T fold_col(T* tile, int t, int cnt, bool first, T acc) {
     T v[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) v[r] = tile[r * LW + t];
-    acc = run_block<T, OP, RB>(v, first, acc);
+    acc = WRITE ? run_block<T, OP, RB>(v, first, acc) : reduce_block<T, OP, RB>(v, first, acc);
     if (WRITE) {
 #pragma unroll
       for (int r = 0; r < RB; ++r) tile[r * LW + t] = v[r];
@@ -226,7 +251,7 @@ NRS_DEV T fold_row(uint8_t* tile, int t, int cnt, bool first, T acc) {
     T v[XB];
 #pragma unroll
     for (int j = 0; j < 8; ++j) lds16(&v[j * PER16], tile + swz(t, j));
-    acc = run_block<T, OP, XB>(v, first, acc);
+    acc = WRITE ? run_block<T, OP, XB>(v, first, acc) : reduce_block<T, OP, XB>(v, first, acc);
     if (WRITE) {
 #pragma unroll
       for (int j = 0; j < 8; ++j) sts16(tile + swz(t, j), &v[j * PER16]);
