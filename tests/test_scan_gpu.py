@@ -201,6 +201,37 @@ def test_flat_reduce(K, ora, n, dtype, offset):
             assert np.isnan(to_np(K.ufunc_reduce(op, _dev(x)))[0])
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int64])
+def test_flat_accumulate_long(K, ora, dtype):
+    """Flattened scans of ~100 MB (more than the L2 holds, 300+ segments of
+    many tiles each) with a ragged tail: every order-free op exact against the
+    oracle (maximum / minimum with NaNs and signed zeros at segment-scale
+    offsets), float add within the reassociation tolerance, and two runs bit
+    for bit the same."""
+    step = 304 * 3 * (32768 // np.dtype(dtype).itemsize)
+    n = int(step * 3.4) + 3
+    r = np.random.default_rng(77)
+    for op in ("add", "maximum", "minimum", "multiply"):
+        x = _data(r, (n,), dtype, op)
+        if np.dtype(dtype).kind == "f" and op in ("maximum", "minimum"):
+            for e in (step - 1, step, 2 * step + 5):
+                x[e] = -0.0 if e % 2 else 0.0
+            x[int(step * 2.7)] = np.nan
+        xd = _dev(x)
+        got = to_np(K.ufunc_accumulate(op, xd))
+        again = to_np(K.ufunc_accumulate(op, xd))
+        np.testing.assert_array_equal(got.view(np.uint8), again.view(np.uint8))
+        if np.dtype(dtype).kind == "f" and op in ("add", "multiply"):
+            if op == "add":
+                ref = np.cumsum(x.astype(np.float64))
+                tol = (4e-6 if dtype == np.float32 else 1e-14) * np.cumsum(np.abs(x.astype(np.float64)))
+                assert np.all(np.abs(got.astype(np.float64) - ref) <= tol + 1e-30)
+            continue  # long float products reach the subnormal floor: covered above
+        _same(got, ora.accumulate(OPS[op], x))
+        del xd
+    torch.cuda.empty_cache()
+
+
 def test_full_size_properties(K):
     """16384 x 16384 f32 (the reduction benchmark's array): the last row of
     cumsum(axis=0) is sum(axis=0) bit for bit (both are the zero-seeded
