@@ -14,7 +14,9 @@ the 129 MB L2), so no L2 flush is needed between steps.
 Printed JSON (one line, rank 0): value = device-resident GB/s of the whole
 step; e2e = the same bytes through the C ABI with pinned HOST buffers (host
 -> device copies of both arrays and device -> host copies of every result
-inside the timed region); roofline = the dominant kernel class against the
+inside the timed region), with e2e.link = the pinned copy rates measured in
+the same run and the step's floor at that H2D rate (frac = floor / step);
+roofline = the dominant kernel class against the
 measured HBM peak; cpu_baseline = the CPU oracle (numrs2 restatement) on a
 bounded row slab of the same workload, all host threads.
 """
@@ -856,6 +858,20 @@ def main():
                 L.check(lib.nrs_synchronize(hh), hh)
             return d2h
 
+        # The host link alone: the best of three 1 GiB pinned copies each way
+        # (H2D and D2H), on the copy streams the step uses; the step cannot
+        # beat its H2D bytes at the H2D rate.
+        def link_gbs(fn, nbytes):
+            best = float("inf")
+            for _ in range(3):
+                t0 = time.perf_counter()
+                fn()
+                best = min(best, time.perf_counter() - t0)
+            return nbytes / best / 1e9
+        h2d_gbs = link_gbs(lambda: (L.check(lib.nrs_memcpy_h2d(h_in, C.c_void_p(x32.data_ptr()), hp32, nb32), h_in),
+                                    L.check(lib.nrs_synchronize(h_in), h_in)), nb32)
+        d2h_gbs = link_gbs(lambda: (L.check(lib.nrs_memcpy_d2h(h_out, hy, C.c_void_p(x32.data_ptr()), nb32), h_out),
+                                    L.check(lib.nrs_synchronize(h_out), h_out)), nb32)
         e2e_step()
         # the blocked i64 reductions give the whole-array results bit for bit
         for j, (vn, code, axis, _) in enumerate(i64_red):
@@ -881,7 +897,10 @@ def main():
                       "h2d_bytes_per_step": nb32 + nb64, "d2h_bytes_per_step": d2h,
                       "ms_per_step": round(dt * 1e3, 3), "steps": e_steps, "stat": "median",
                       "ms_per_step_mean": round(sum(times) / len(times) * 1e3, 3),
-                      "ms_per_step_max": round(max(times) * 1e3, 3)}
+                      "ms_per_step_max": round(max(times) * 1e3, 3),
+                      "link": {"h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1),
+                               "h2d_bound_ms": round((nb32 + nb64) / h2d_gbs / 1e6, 3),
+                               "frac": round((nb32 + nb64) / h2d_gbs / 1e6 / (dt * 1e3), 3)}}
         for p in (hp32, hp64, hy):
             lib.nrs_host_free(h, p)
         for hh in (h_in, h_out, *hx[1:]):
