@@ -168,6 +168,15 @@ struct RunFold {
     else return fmin(a, v);
   }
 
+  // max / min that return NaN when either operand is NaN (f32 only: the
+  // instruction has no f64 form).
+  static __device__ __forceinline__ float pick_nan(float a, float v) {
+    float d;
+    if constexpr (OP == NRS_MAX) asm("max.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(v));
+    else asm("min.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(v));
+    return d;
+  }
+
   template <int N, typename Get>
   static __device__ __forceinline__ T run(T acc, Get get) {
     if constexpr (!kChains) {
@@ -179,6 +188,25 @@ struct RunFold {
 #pragma unroll
       for (int i = 0; i < N; ++i) a[i & 3] = Fold<T, OP>::step(a[i & 3], get(i));
       return Fold<T, OP>::step(Fold<T, OP>::step(a[0], a[1]), Fold<T, OP>::step(a[2], a[3]));
+    } else if constexpr (std::is_same<T, float>::value) {
+      // Four NaN-propagating chains, one instruction per element. A result
+      // that is neither NaN nor zero is the ordered fold's bit for bit (equal
+      // nonzero values have equal bits); a NaN (whose first payload the
+      // ordered fold keeps) or a zero (where -0 and +0 tie) re-folds the
+      // block in order.
+      static_assert(N % 4 == 0, "blocks of four");
+      if (acc != acc) return acc;  // the lane already holds its first NaN
+      float v[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] = get(i);
+      float a[4] = {pick_nan(acc, v[0]), v[1], v[2], v[3]};
+#pragma unroll
+      for (int i = 4; i < N; ++i) a[i & 3] = pick_nan(a[i & 3], v[i]);
+      const float r = pick_nan(pick_nan(a[0], a[1]), pick_nan(a[2], a[3]));
+      if (r == r && r != 0.0f) return r;
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc = Fold<T, OP>::step(acc, v[i]);
+      return acc;
     } else {
       if (acc != acc) return acc;  // the lane already holds its first NaN
       T a[4] = {acc, Fold<T, OP>::init(), Fold<T, OP>::init(), Fold<T, OP>::init()};

@@ -170,14 +170,38 @@ NRS_DEV int swz(int r, int j) { return r * 128 + ((j ^ (r & 7)) << 4); }
 template <typename T, int OP, int N>
 NRS_DEV T run_block(T (&v)[N], bool first, T acc);
 
+// f32 maximum / minimum returning NaN when either operand is NaN (the
+// instruction has no f64 form).
+template <int OP>
+NRS_DEV float nan_pick(float a, float b) {
+  float d;
+  if constexpr (OP == NRS_OP_MAX) asm("max.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+  else asm("min.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+  return d;
+}
+
 // The same fold's result without the prefixes (reductions). Float maximum /
 // minimum are order-free over values that hold no NaN and no zero (equal
-// values then have equal bits), so such blocks fold as four independent
-// fmax / fmin chains; a block with a NaN or a zero, or a NaN accumulator,
-// takes the sequential chain. Other ops: the sequential chain.
+// values then have equal bits), so blocks fold as four independent chains:
+// f32 with NaN-propagating max / min and one test of the result, f64 with
+// fmax / fmin after a per-element NaN-or-zero test; a block with a NaN or
+// a zero, or a NaN accumulator, takes the sequential chain. Other ops: the
+// sequential chain.
 template <typename T, int OP, int N>
 NRS_DEV T reduce_block(T (&v)[N], bool first, T acc) {
-  if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
+  if constexpr (std::is_same<T, float>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
+    // Four NaN-propagating chains, one instruction per element: a result
+    // that is neither NaN nor zero is apply's fold bit for bit (equal nonzero
+    // values have equal bits); a NaN (canonical in apply) or a zero (-0 and
+    // +0 tie, the later wins) takes the ordered chain.
+    if (first || acc == acc) {
+      float a[4] = {first ? v[0] : nan_pick<OP>(acc, v[0]), v[1], v[2], v[3]};
+#pragma unroll
+      for (int e = 4; e < N; ++e) a[e & 3] = nan_pick<OP>(a[e & 3], v[e]);
+      const float r = nan_pick<OP>(nan_pick<OP>(a[0], a[1]), nan_pick<OP>(a[2], a[3]));
+      if (r == r && r != 0.0f) return r;
+    }
+  } else if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
     bool special = !first && acc != acc;
 #pragma unroll
     for (int e = 0; e < N; ++e) special |= !(fabs(v[e]) > T(0));
