@@ -130,8 +130,29 @@ __device__ void row_reduce_t(const T* __restrict__ x, int64_t len, void* out, ui
         acc = Fold<T, OP>::step(acc, v);
       }
     }
-    const T r = block_combine<T, OP>(acc, sh);
+    T r = block_combine<T, OP>(acc, sh);
     const int anynan = __syncthreads_or(tn);
+    if constexpr (std::is_floating_point<T>::value && (OP == NRS_MAX || OP == NRS_MIN)) {
+      // An extreme of zero: the left-to-right fold keeps the chunk's first
+      // zero (-0.0 and +0.0 tie), which the striped tree does not track.
+      __shared__ int zflag;
+      __shared__ unsigned long long fzs;
+      if (threadIdx.x == 0) {
+        zflag = r == T(0);
+        fzs = (unsigned long long)clen;
+      }
+      __syncthreads();
+      if (zflag) {
+        for (int64_t i = threadIdx.x; i < clen; i += kThreads)
+          if (x[c0 + i] == T(0)) {
+            atomicMin(&fzs, (unsigned long long)i);
+            break;
+          }
+        __syncthreads();
+        if (threadIdx.x == 0) r = x[c0 + (int64_t)fzs];
+      }
+      __syncthreads();  // zflag / fzs are free for the next chunk
+    }
     if (threadIdx.x == 0) {
       total = Fold<T, OP>::step(total, Fold<T, OP>::step(Fold<T, OP>::init(), r));
       nan |= anynan;

@@ -294,7 +294,16 @@ __global__ void __launch_bounds__(kColLanes)
       tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
     }
   }
-  const T m = (lane_mean && l0 + t < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + t] : T(0);
+  // A thread past the last lane folds lane 0's column (and discards it)
+  // rather than the box's zero fill, whose zeros would send the max / min
+  // chains to the ordered path on every tile and make this CTA the
+  // launch's straggler (f64: 2.3x the launch time at 11586^2). f32 max /
+  // min keep their own column: their ordered path is cheap, and the
+  // substitution measured 14% slower for them.
+  constexpr bool kSubst = !(std::is_same<T, float>::value && (OP == NRS_MAX || OP == NRS_MIN));
+  const bool live = l0 + t < lanes;
+  const int tl = (kSubst && !live) ? 0 : t;
+  const T m = (lane_mean && l0 + tl < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + tl] : T(0);
   T acc = Fold<T, OP>::init();
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
@@ -308,9 +317,9 @@ __global__ void __launch_bounds__(kColLanes)
     const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
     if (cnt == RB) {
       acc = RunFold<T, OP>::template run<RB>(
-          acc, [&](int r) { return lane_xform<T, OP>(tile[r * LW + t], m); });
+          acc, [&](int r) { return lane_xform<T, OP>(tile[r * LW + tl], m); });
     } else {
-      for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, lane_xform<T, OP>(tile[r * LW + t], m));
+      for (int r = 0; r < cnt; ++r) acc = Fold<T, OP>::step(acc, lane_xform<T, OP>(tile[r * LW + tl], m));
     }
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + STAGES < n_tiles) {
@@ -370,9 +379,12 @@ __global__ void __launch_bounds__(64)
       tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
     }
   }
-  const T m = (lane_mean && l0 + t < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + t] : T(0);
+  // A thread past the last row folds row 0 of the tile (and discards it)
+  // rather than the box's zero fill (see fold_cols_tma).
+  const int tl = l0 + t < lanes ? t : 0;
+  const T m = (lane_mean && l0 + tl < lanes) ? lane_mean[(int64_t)batch * lanes + l0 + tl] : T(0);
   T acc = Fold<T, OP>::init();
-  const int sw = t & 7;
+  const int sw = tl & 7;
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
     const int s = (int)(it % STAGES);
@@ -380,7 +392,7 @@ __global__ void __launch_bounds__(64)
     if (!mbar_wait_bounded(&full[s], phase, NRS_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     if (abort_flag) break;
-    const uint8_t* row = smem + s * TILE + t * 128;
+    const uint8_t* row = smem + s * TILE + tl * 128;
     const int64_t x0 = it * XB;
     const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
     if (cnt == XB) {
@@ -423,6 +435,30 @@ __global__ void __launch_bounds__(64)
   if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
+// The comparison argmax / argmin runs on: the value itself, except for f64,
+// whose values map to int64 keys (integer pipe; GB300's FP64 pipe retires a
+// few operations per clock per SM): the magnitude bits of negatives flipped,
+// -0 folded onto +0 (equal values tie, the first index stays), a NaN element
+// the key that never wins, and a lane that starts with NaN the key nothing
+// beats.
+template <typename T, bool MAX>
+struct ArgOrd {
+  using K = T;
+  static __device__ __forceinline__ K key(T v) { return v; }
+  static __device__ __forceinline__ K start(T v) { return v; }
+};
+template <bool MAX>
+struct ArgOrd<double, MAX> {
+  using K = int64_t;
+  static __device__ __forceinline__ K key(double v) {
+    const uint64_t u = (uint64_t)__double_as_longlong(v);
+    if ((u & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return MAX ? INT64_MIN : INT64_MAX;
+    if ((u << 1) == 0) return 0;
+    return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1));
+  }
+  static __device__ __forceinline__ K start(double v) { return v != v ? (MAX ? INT64_MAX : INT64_MIN) : key(v); }
+};
+
 // argmax / argmin along lanes through the same TMA pipelines: each thread
 // scans its lane in order keeping (best, index) -- the first element starts
 // the lane, a later one replaces it only if strictly greater (smaller), so
@@ -459,7 +495,8 @@ __global__ void __launch_bounds__(64)
   __syncthreads();
   if (t == 0)
     for (int s = 0; s < STAGES && s < n_tiles; ++s) load(s, s);
-  T best = T(0);
+  using Ord = ArgOrd<T, MAX>;
+  typename Ord::K best = typename Ord::K(0);
   int bt = 0, be = 0;  // tile and position of the best so far (32-bit selects)
   const int sw = t & 7;
   int64_t it = 0;
@@ -485,21 +522,23 @@ __global__ void __launch_bounds__(64)
     // The lane's first element starts it (comparing it with itself then
     // changes nothing, NaN included), so full tiles need no per-element
     // checks beyond the compare.
-    if (it == 0) best = v[0];
+    if (it == 0) best = Ord::start(v[0]);
     int bet = -1;  // position of this tile's improvement, if any
     if (cnt == TB) {
 #pragma unroll
       for (int e = 0; e < TB; ++e) {
-        if (MAX ? (v[e] > best) : (v[e] < best)) {
-          best = v[e];
+        const typename Ord::K k = Ord::key(v[e]);
+        if (MAX ? (k > best) : (k < best)) {
+          best = k;
           bet = e;
         }
       }
     } else {
 #pragma unroll
       for (int e = 0; e < TB; ++e) {
-        if (e < cnt && (MAX ? (v[e] > best) : (v[e] < best))) {
-          best = v[e];
+        const typename Ord::K k = Ord::key(v[e]);
+        if (e < cnt && (MAX ? (k > best) : (k < best))) {
+          best = k;
           bet = e;
         }
       }
@@ -586,6 +625,48 @@ __global__ void __launch_bounds__(256, kFlatBlocksPerSM)
     const int64_t lo = c * chunk;
     const int64_t len = (n - lo) < chunk ? (n - lo) : chunk;
     const T* p = x + lo + LPT * t;
+    if constexpr (std::is_same<T, double>::value && (OP == NRS_MAX || OP == NRS_MIN) && !SSD) {
+      // f64 max / min on int64 keys (no FP64 instruction per element): the
+      // chunk's extreme when it holds no NaN and no zero (the extreme is then
+      // unique in bits and the order is free); otherwise the chunk is folded
+      // again below with the ordered steps.
+      using RF = RunFold<double, OP>;
+      const int64_t k0 = RF::key64((uint64_t)__double_as_longlong(Fold<double, OP>::init()));
+      int64_t kacc[LPT];
+#pragma unroll
+      for (int j = 0; j < LPT; ++j) kacc[j] = k0;
+      bool odd = false;
+      auto kfold = [&](int64_t& a, double v) {
+        const uint64_t u = (uint64_t)__double_as_longlong(v);
+        odd |= RF::nan_or_zero64(u);
+        const int64_t k = RF::key64(u);
+        a = (OP == NRS_MAX ? (k > a) : (k < a)) ? k : a;
+      };
+      const int64_t full = len / 256;
+#pragma unroll UNROLL
+      for (int64_t k = 0; k < full; ++k) {
+        T v[LPT];
+        load_lanes<T, VEC>(p + 256 * k, v);
+#pragma unroll
+        for (int j = 0; j < LPT; ++j) kfold(kacc[j], v[j]);
+      }
+      const int64_t rest = len - 256 * full;
+#pragma unroll
+      for (int j = 0; j < LPT; ++j)
+        if (LPT * t + j < rest) kfold(kacc[j], p[256 * full + j]);
+      if (!__any_sync(0xffffffffu, odd)) {
+        int64_t b = kacc[0];
+#pragma unroll
+        for (int j = 1; j < LPT; ++j) b = (OP == NRS_MAX ? (kacc[j] > b) : (kacc[j] < b)) ? kacc[j] : b;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const int64_t o = __shfl_xor_sync(0xffffffffu, b, off);
+          b = (OP == NRS_MAX ? (o > b) : (o < b)) ? o : b;
+        }
+        if (t == 0) part[c] = Partial<T>{__longlong_as_double((long long)RF::key64((uint64_t)b)), 0};
+        continue;
+      }
+    }
     T acc[LPT];
 #pragma unroll
     for (int j = 0; j < LPT; ++j) acc[j] = Fold<T, OP>::init();
@@ -615,6 +696,25 @@ __global__ void __launch_bounds__(256, kFlatBlocksPerSM)
     T r = __shfl_sync(0xffffffffu, acc[0], 0);
 #pragma unroll
     for (int g = 1; g < 8; ++g) r = Fold<T, OP>::step(r, __shfl_sync(0xffffffffu, acc[0], 4 * g));
+    if constexpr (std::is_floating_point<T>::value && (OP == NRS_MAX || OP == NRS_MIN) && !SSD) {
+      // An extreme of zero: the left-to-right fold keeps the chunk's first
+      // zero (-0.0 and +0.0 tie), which the lane order above does not
+      // track; the warp looks it up (lane l checks l, l + 32, ...).
+      if (r == T(0)) {
+        int64_t fz = len;
+        for (int64_t i = t; i < len; i += 32)
+          if (x[lo + i] == T(0)) {
+            fz = i;
+            break;
+          }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const int64_t o = __shfl_xor_sync(0xffffffffu, fz, off);
+          fz = o < fz ? o : fz;
+        }
+        r = x[lo + fz];
+      }
+    }
     const int anynan = __any_sync(0xffffffffu, nan);
     if (t == 0) part[c] = Partial<T>{r, anynan};
   }
@@ -669,11 +769,47 @@ __global__ void __launch_bounds__(1024)
   int anynan = 0;
   if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
     // The partials hold no NaN (a flag carries it), and without NaNs max/min
-    // do not depend on the grouping (only which of two equal zeros is kept),
-    // so the runs combine as a tree rather than a 1024-step chain.
-    r = block_combine<T, OP>(acc, run);
+    // depend on the grouping only in which of two equal zeros is kept: the
+    // runs combine as a tree of (value, first chunk) pairs, equal values
+    // keeping the smaller chunk, so the result is the left-to-right fold's.
+    int64_t ai = nchunks;  // chunk of acc's value (none yet)
+    {
+      T a2 = Fold<T, OP>::init();
+      for (int64_t i = t; i < nchunks; i += 1024) {
+        const T v = part[i].v;
+        if (OP == NRS_MAX ? (v > a2) : (v < a2)) {
+          a2 = v;
+          ai = i;
+        }
+      }
+      acc = a2;
+    }
+    auto take = [](T v, int64_t i, T w, int64_t j) {
+      return (OP == NRS_MAX ? (v > w) : (v < w)) || (v == w && i < j);
+    };
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, acc, off);
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, ai, off);
+      if (take(ov, oi, acc, ai)) {
+        acc = ov;
+        ai = oi;
+      }
+    }
+    __shared__ int64_t runi[32];
+    if ((t & 31) == 0) {
+      run[t >> 5] = acc;
+      runi[t >> 5] = ai;
+    }
     anynan = __syncthreads_or(nan);
     if (t != 0) return;
+    r = run[0];
+    int64_t ri = runi[0];
+    for (int w = 1; w < 32; ++w)
+      if (take(run[w], runi[w], r, ri)) {
+        r = run[w];
+        ri = runi[w];
+      }
   } else {
     run[t] = acc;
     runnan[t] = nan;
@@ -940,8 +1076,8 @@ int dispatch_axis_ops(nrs_handle* h, const AxisProblem& p) {
 template <typename T>
 int flat_reduce(nrs_handle* h, int op, int64_t n, int64_t ddof, const T* x, void* out) {
   // Tiering (src/kernels/reduce.rs): SUM/MEAN one simd_sum below 10k, else
-  // 8192 chunks; VAR below 40k one pass each, else chunks; MIN/MAX and PROD
-  // chunking does not change their result, so they always use 8192 chunks.
+  // 8192 chunks; VAR below 40k one pass each, else chunks; MIN/MAX (whose
+  // partials keep the first of equal zeros) and PROD always use 8192 chunks.
   int64_t chunk;
   if (op == NRS_VAR || op == NRS_STD)
     chunk = (n < kVarParallelMin) ? (n > 0 ? n : 1) : kChunk;

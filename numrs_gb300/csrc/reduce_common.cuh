@@ -177,6 +177,18 @@ struct RunFold {
     return d;
   }
 
+  // f64 order on the integer pipe: for values that are neither NaN nor zero,
+  // a < b as doubles exactly when key(a) < key(b) as int64 (the magnitude
+  // bits of negatives flipped); the key maps back by the same operation.
+  static __device__ __forceinline__ int64_t key64(uint64_t u) {
+    return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1));
+  }
+  // NaN or a zero: the magnitude bits minus one, unsigned, reach the
+  // infinity pattern (zero wraps around).
+  static __device__ __forceinline__ bool nan_or_zero64(uint64_t u) {
+    return ((u & 0x7FFFFFFFFFFFFFFFull) - 1u) >= 0x7FF0000000000000ull;
+  }
+
   template <int N, typename Get>
   static __device__ __forceinline__ T run(T acc, Get get) {
     if constexpr (!kChains) {
@@ -204,6 +216,35 @@ struct RunFold {
       for (int i = 4; i < N; ++i) a[i & 3] = pick_nan(a[i & 3], v[i]);
       const float r = pick_nan(pick_nan(a[0], a[1]), pick_nan(a[2], a[3]));
       if (r == r && r != 0.0f) return r;
+#pragma unroll
+      for (int i = 0; i < N; ++i) acc = Fold<T, OP>::step(acc, v[i]);
+      return acc;
+    } else if constexpr (std::is_same<T, double>::value) {
+      // Four chains of int64 keys (no FP64 instruction per element): exact
+      // when the block and the accumulator hold no NaN and no zero; else the
+      // block re-folds in order.
+      static_assert(N % 4 == 0, "blocks of four");
+      const uint64_t ua = (uint64_t)__double_as_longlong(acc);
+      if ((ua & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return acc;  // the lane's first NaN
+      double v[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] = get(i);
+      bool special = nan_or_zero64(ua);
+      const int64_t k0 = key64((uint64_t)__double_as_longlong(Fold<T, OP>::init()));
+      int64_t a[4] = {key64(ua), k0, k0, k0};
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const uint64_t u = (uint64_t)__double_as_longlong(v[i]);
+        special |= nan_or_zero64(u);
+        const int64_t k = key64(u);
+        a[i & 3] = (OP == NRS_MAX ? (k > a[i & 3]) : (k < a[i & 3])) ? k : a[i & 3];
+      }
+      if (!special) {
+        const int64_t b0 = (OP == NRS_MAX ? (a[1] > a[0]) : (a[1] < a[0])) ? a[1] : a[0];
+        const int64_t b1 = (OP == NRS_MAX ? (a[3] > a[2]) : (a[3] < a[2])) ? a[3] : a[2];
+        const int64_t b = (OP == NRS_MAX ? (b1 > b0) : (b1 < b0)) ? b1 : b0;
+        return __longlong_as_double((long long)key64((uint64_t)b));
+      }
 #pragma unroll
       for (int i = 0; i < N; ++i) acc = Fold<T, OP>::step(acc, v[i]);
       return acc;

@@ -201,16 +201,27 @@ NRS_DEV T reduce_block(T (&v)[N], bool first, T acc) {
       const float r = nan_pick<OP>(nan_pick<OP>(a[0], a[1]), nan_pick<OP>(a[2], a[3]));
       if (r == r && r != 0.0f) return r;
     }
-  } else if constexpr (std::is_floating_point<T>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
-    bool special = !first && acc != acc;
+  } else if constexpr (std::is_same<T, double>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
+    // int64 keys (the magnitude bits of negatives flipped) order non-NaN,
+    // nonzero doubles exactly, with no FP64 instruction per element.
+    auto key = [](uint64_t u) { return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1)); };
+    auto odd = [](uint64_t u) { return ((u & 0x7FFFFFFFFFFFFFFFull) - 1u) >= 0x7FF0000000000000ull; };
+    auto better = [](int64_t k, int64_t a) { return OP == NRS_OP_MAX ? (k > a) : (k < a); };
+    const uint64_t ua = (uint64_t)__double_as_longlong(acc);
+    bool special = !first && odd(ua);
+    int64_t a[4];
 #pragma unroll
-    for (int e = 0; e < N; ++e) special |= !(fabs(v[e]) > T(0));
+    for (int e = 0; e < N; ++e) {
+      const uint64_t u = (uint64_t)__double_as_longlong(v[e]);
+      special |= odd(u);
+      const int64_t k = key(u);
+      if (e < 4) a[e] = (e == 0 && !first) ? (better(k, key(ua)) ? k : key(ua)) : k;
+      else a[e & 3] = better(k, a[e & 3]) ? k : a[e & 3];
+    }
     if (!special) {
-      T a[4] = {first ? v[0] : acc, v[1], v[2], v[3]};
-      if (!first) a[0] = OP == NRS_OP_MAX ? fmax(a[0], v[0]) : fmin(a[0], v[0]);
-#pragma unroll
-      for (int e = 4; e < N; ++e) a[e & 3] = OP == NRS_OP_MAX ? fmax(a[e & 3], v[e]) : fmin(a[e & 3], v[e]);
-      return OP == NRS_OP_MAX ? fmax(fmax(a[0], a[1]), fmax(a[2], a[3])) : fmin(fmin(a[0], a[1]), fmin(a[2], a[3]));
+      const int64_t b0 = better(a[1], a[0]) ? a[1] : a[0];
+      const int64_t b1 = better(a[3], a[2]) ? a[3] : a[2];
+      return __longlong_as_double((long long)key((uint64_t)(better(b1, b0) ? b1 : b0)));
     }
   }
   return run_block<T, OP, N>(v, first, acc);
@@ -307,6 +318,10 @@ __global__ void __launch_bounds__(kLanesPerCta)
 
   const int t = threadIdx.x;
   const int64_t l0 = (int64_t)blockIdx.x * kLanesPerCta;
+  // a thread past the last lane folds lane 0's data (and discards it)
+  // rather than the box's zero fill, which would send the max / min chains
+  // to the ordered path on every tile
+  const int tl = l0 + t < lanes ? t : 0;
   const int32_t batch = blockIdx.y;
   const int64_t n_tiles = (alen + TB - 1) / TB;
   auto load = [&](int s, int64_t tile) {
@@ -336,9 +351,9 @@ __global__ void __launch_bounds__(kLanesPerCta)
     const int cnt = (int)((alen - it * TB) < TB ? (alen - it * TB) : TB);
     const bool first = (it == 0) && seed.first;
     if (COLS)
-      acc = fold_col<T, OP, false>(reinterpret_cast<T*>(smem + s * kTileBytes), t, cnt, first, acc);
+      acc = fold_col<T, OP, false>(reinterpret_cast<T*>(smem + s * kTileBytes), tl, cnt, first, acc);
     else
-      acc = fold_row<T, OP, false>(smem + s * kTileBytes, t, cnt, first, acc);
+      acc = fold_row<T, OP, false>(smem + s * kTileBytes, tl, cnt, first, acc);
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + S < n_tiles) load(s, it + S);
   }

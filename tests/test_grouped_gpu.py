@@ -279,3 +279,32 @@ def test_tuner_and_selector_files_are_keyed(K, tmp_path):
         s3.load(wpath)
     for sel in (s1, s2, s3):
         sel.close()
+
+
+def test_grouped_row_extrema_first_zero(K, ora):
+    """Max / min rows whose extreme is a zero of both signs: the grouped row
+    reductions and nrs_reduce both keep the first zero, as the left-to-right
+    fold does (one chunk, chunk edges, several chunks)."""
+    r = np.random.default_rng(3)
+    a = torch.empty((32, 32), dtype=torch.float64, device="cuda").uniform_(-1, 1)
+    gemms = [(a, a.clone(), torch.empty_like(a), False)]
+    reds, hosts = [], []
+    for n in (100, 8192, 8193, 30000, 70001):
+        for dt in (np.float32, np.float64):
+            for op, sign in ((L.MAX, -1.0), (L.MIN, 1.0)):
+                x = (sign * np.abs(r.standard_normal(n))).astype(dt)
+                z = r.choice(n, 6, replace=False)
+                first = np.sort(z)
+                x[z] = 0.0
+                x[first[0]] = -0.0 if r.random() < 0.5 else 0.0
+                x[first[1:]] = np.where(np.signbit(x[first[0]]), 0.0, -0.0)  # later zeros: the other sign
+                xd = torch.from_numpy(x).cuda()
+                reds.append((xd, op, torch.empty(1, dtype=xd.dtype, device="cuda")))
+                hosts.append(x)
+    plan = K.Plan(gemms, reds)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    for (xd, op, out), x in zip(reds, hosts):
+        want = np.array([ora.flat("max" if op == L.MAX else "min", x)], x.dtype)
+        np.testing.assert_array_equal(bits(to_np(out)), bits(want))
+        np.testing.assert_array_equal(bits(to_np(K.reduce(xd, op))), bits(want))

@@ -240,3 +240,43 @@ def test_large_c2_shape_properties(K):
     m1 = K.max(x, axis=1)
     assert torch.equal(m1, x.max(1).values)
     del x
+
+
+@pytest.mark.parametrize("case", ["negatives", "zeros", "nans", "extremes"])
+def test_f64_extrema_bit_exact(K, ora, case):
+    """f64 max / min run on int64 keys (integer pipe) for blocks with no NaN
+    and no zero and fall back to the ordered fold otherwise: both lane
+    pipelines, the flattened partials and the ufunc reduce against the
+    oracle bit for bit, on all-negative data (the extreme near zero), signed
+    zeros, NaNs, and infinities / subnormals / the largest finite values."""
+    r = np.random.default_rng({"negatives": 1, "zeros": 2, "nans": 3, "extremes": 4}[case])
+    x = -np.abs(r.standard_normal((700, 520)))
+    if case == "zeros":
+        x[r.random(x.shape) < 0.004] = -0.0
+        x[r.random(x.shape) < 0.004] = 0.0
+    elif case == "nans":
+        x[r.random(x.shape) < 0.001] = np.nan
+    elif case == "extremes":
+        for v in (-np.inf, np.inf, 5e-324, -5e-324, 1.7976931348623157e308, -1.7976931348623157e308):
+            x[r.random(x.shape) < 0.002] = v
+    xd = _dev(x)
+    for op in ("max", "min"):
+        for axis in (0, 1):
+            _check_axis(K, ora, x, op, axis)
+            _check_axis(K, ora, x, op, axis, transposed=True)
+        got = to_np(getattr(K, op)(xd))
+        want = np.array([ora.flat(op, x)], np.float64)
+        assert np.isnan(got[0]) == np.isnan(want[0])
+        if not np.isnan(want[0]):
+            np.testing.assert_array_equal(bits(got), bits(want))
+        ufn = "maximum" if op == "max" else "minimum"
+        code = 11 if op == "max" else 12
+        for axis in (0, 1):
+            g = to_np(K.ufunc_reduce(ufn, xd, axis)).ravel()
+            w = ora.ufunc_reduce(code, x, axis)
+            nan = np.isnan(w)
+            np.testing.assert_array_equal(np.isnan(g), nan)
+            np.testing.assert_array_equal(bits(g[~nan]), bits(w[~nan]))
+    for want_max, fn in ((True, K.argmax), (False, K.argmin)):
+        for axis in (0, 1):
+            np.testing.assert_array_equal(to_np(fn(xd, axis=axis)), ora.axis_arg(x, axis, want_max))
