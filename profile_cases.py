@@ -26,6 +26,9 @@ CASES = {
     "flat_sum_f32": ("f32", L.SUM, None),
     "flat_max_f32": ("f32", L.MAX, None),
     "flat_argmax_f32": ("f32", L.ARGMAX, None),
+    "fold_cols_f64_max": ("f64", L.MAX, 0),
+    "fold_rows_f64_max": ("f64", L.MAX, 1),
+    "flat_max_f64": ("f64", L.MAX, None),
     "exp_affine_f32": ("f32", None, None),
     "ozaki_f64": ("f64", None, None),
     "dmma_f64": ("f64", None, None),
@@ -59,8 +62,8 @@ def main():
     dt, op, axis = CASES[a.case]
     n = a.n
     if a.case.startswith("fold") or a.case.startswith("flat"):
-        if dt == "f32":
-            x = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        if dt in ("f32", "f64"):
+            x = torch.empty((n, n), dtype=torch.float32 if dt == "f32" else torch.float64, device="cuda")
             K.fill_random(x, L.RNG_NORMAL, 3, 0.0, 1.0)
         else:
             x = torch.empty((n, n), dtype=torch.int64, device="cuda")
