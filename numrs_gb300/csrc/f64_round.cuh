@@ -1,6 +1,7 @@
 // The grouped Ozaki epilogue's exact total of a C element and its 128-bit
-// integer to f64 / f32 conversion, written for host and device alike so that
-// the CPU tests check the same code the kernels run.
+// integer to f64 / f32 conversion, and the int64 order keys of doubles used
+// by the max / min / argmax kernels, written for host and device alike so
+// that the CPU tests check the same code the kernels run.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -239,3 +240,18 @@ NRS_HD int ozaki_digit64(const OzakiZ64& z, int t) {
   const int f = (int)(uint32_t)(z.z >> (64 - B * (t + 1)));
   return (t == 0 ? (f | (int)(z.carry << B)) : (f & ((1 << B) - 1))) - (1 << (B - 1));
 }
+
+// ---------------------------------------------------------------------------
+// f64 order on the integer pipe
+// ---------------------------------------------------------------------------
+// For doubles that are neither NaN nor zero, a < b exactly when
+// nrs_f64_key(a) < nrs_f64_key(b) as int64 (the magnitude bits of negatives
+// flipped), and equal keys mean equal bits; the key maps back to the bits by
+// the same operation.
+NRS_HD int64_t nrs_f64_key(uint64_t u) { return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1)); }
+// NaN or a zero: the magnitude bits minus one, unsigned, reach the infinity
+// pattern (zero wraps around).
+NRS_HD bool nrs_f64_nan_or_zero(uint64_t u) {
+  return ((u & 0x7FFFFFFFFFFFFFFFull) - 1u) >= 0x7FF0000000000000ull;
+}
+NRS_HD bool nrs_f64_is_nan(uint64_t u) { return (u & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull; }

@@ -452,9 +452,9 @@ struct ArgOrd<double, MAX> {
   using K = int64_t;
   static __device__ __forceinline__ K key(double v) {
     const uint64_t u = (uint64_t)__double_as_longlong(v);
-    if ((u & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return MAX ? INT64_MIN : INT64_MAX;
+    if (nrs_f64_is_nan(u)) return MAX ? INT64_MIN : INT64_MAX;
     if ((u << 1) == 0) return 0;
-    return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1));
+    return nrs_f64_key(u);
   }
   static __device__ __forceinline__ K start(double v) { return v != v ? (MAX ? INT64_MAX : INT64_MIN) : key(v); }
 };

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "f64_round.cuh"
 #include "nrs_internal.cuh"
 
 namespace nrs_red {
@@ -177,17 +178,9 @@ struct RunFold {
     return d;
   }
 
-  // f64 order on the integer pipe: for values that are neither NaN nor zero,
-  // a < b as doubles exactly when key(a) < key(b) as int64 (the magnitude
-  // bits of negatives flipped); the key maps back by the same operation.
-  static __device__ __forceinline__ int64_t key64(uint64_t u) {
-    return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1));
-  }
-  // NaN or a zero: the magnitude bits minus one, unsigned, reach the
-  // infinity pattern (zero wraps around).
-  static __device__ __forceinline__ bool nan_or_zero64(uint64_t u) {
-    return ((u & 0x7FFFFFFFFFFFFFFFull) - 1u) >= 0x7FF0000000000000ull;
-  }
+  // f64 order on the integer pipe (f64_round.cuh)
+  static __device__ __forceinline__ int64_t key64(uint64_t u) { return nrs_f64_key(u); }
+  static __device__ __forceinline__ bool nan_or_zero64(uint64_t u) { return nrs_f64_nan_or_zero(u); }
 
   template <int N, typename Get>
   static __device__ __forceinline__ T run(T acc, Get get) {
@@ -225,7 +218,7 @@ struct RunFold {
       // block re-folds in order.
       static_assert(N % 4 == 0, "blocks of four");
       const uint64_t ua = (uint64_t)__double_as_longlong(acc);
-      if ((ua & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return acc;  // the lane's first NaN
+      if (nrs_f64_is_nan(ua)) return acc;  // the lane already holds its first NaN
       double v[N];
 #pragma unroll
       for (int i = 0; i < N; ++i) v[i] = get(i);

@@ -28,6 +28,7 @@
 #include <string>
 #include <type_traits>
 
+#include "f64_round.cuh"
 #include "nrs_internal.cuh"
 
 namespace {
@@ -204,8 +205,8 @@ NRS_DEV T reduce_block(T (&v)[N], bool first, T acc) {
   } else if constexpr (std::is_same<T, double>::value && (OP == NRS_OP_MAX || OP == NRS_OP_MIN) && N % 4 == 0) {
     // int64 keys (the magnitude bits of negatives flipped) order non-NaN,
     // nonzero doubles exactly, with no FP64 instruction per element.
-    auto key = [](uint64_t u) { return (int64_t)(u ^ ((uint64_t)((int64_t)u >> 63) >> 1)); };
-    auto odd = [](uint64_t u) { return ((u & 0x7FFFFFFFFFFFFFFFull) - 1u) >= 0x7FF0000000000000ull; };
+    auto key = [](uint64_t u) { return nrs_f64_key(u); };
+    auto odd = [](uint64_t u) { return nrs_f64_nan_or_zero(u); };
     auto better = [](int64_t k, int64_t a) { return OP == NRS_OP_MAX ? (k > a) : (k < a); };
     const uint64_t ua = (uint64_t)__double_as_longlong(acc);
     bool special = !first && odd(ua);

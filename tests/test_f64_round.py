@@ -4,7 +4,9 @@ compiled for the host with g++: the exact path and the straight-line fast
 path against exact rational rounding (round to nearest, ties to even) over
 random magnitudes and scales, ties, carries into the next binade, overflow
 to infinity and the subnormal range; the total T = R 2^(b(S-1)) +
-sum_t digit_t 2^(bt) against Python integers for every digit width."""
+sum_t digit_t 2^(bt) against Python integers for every digit width; and
+the int64 order keys of doubles (max / min / argmax kernels) against
+Python's float order."""
 import ctypes
 import os
 import random
@@ -45,6 +47,9 @@ extern "C" void nrs_test_digits64(double x, int e, int b, int S, int* out) {
   for (int t = 0; t < S; ++t)
     out[t] = b == 8 ? ozaki_digit64<8>(z, t) : b == 7 ? ozaki_digit64<7>(z, t) : ozaki_digit64<6>(z, t);
 }
+extern "C" int64_t nrs_test_key(uint64_t u) { return nrs_f64_key(u); }
+extern "C" int nrs_test_nan_or_zero(uint64_t u) { return nrs_f64_nan_or_zero(u); }
+extern "C" int nrs_test_is_nan(uint64_t u) { return nrs_f64_is_nan(u); }
 extern "C" void nrs_test_total(int32_t R, uint64_t lo, uint64_t hi, int b, int S, int* neg, uint64_t* mhi,
                                uint64_t* mlo) {
   bool n = false;
@@ -242,3 +247,36 @@ def test_slice_digits64_equal_the_128bit_digits(lib, b):
             assert abs(x) < 2.0 ** e
             f(x, e, b, S, out)
             assert list(out[:S]) == _digits128(x, e, b, S), (x, e, b, S)
+
+
+def test_f64_order_keys(lib):
+    """nrs_f64_key orders doubles that are neither NaN nor zero exactly as
+    floats, equal keys only for equal bits, and maps back to the bits by the
+    same operation; nrs_f64_nan_or_zero / nrs_f64_is_nan classify every
+    class of double (signed zeros, subnormals, infinities, quiet and
+    signalling NaNs of both signs)."""
+    key, noz, isn = lib.nrs_test_key, lib.nrs_test_nan_or_zero, lib.nrs_test_is_nan
+    key.restype = ctypes.c_int64
+    key.argtypes = [ctypes.c_uint64]
+    for f in (noz, isn):
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_uint64]
+    bits_of = lambda d: struct.unpack("<Q", struct.pack("<d", d))[0]  # noqa: E731
+    r = random.Random(17)
+    vals = [r.uniform(-1, 1) * 2.0 ** r.randint(-1074, 1023) for _ in range(4000)]
+    vals += [5e-324, -5e-324, 2.2250738585072014e-308, -2.2250738585072014e-308, 1.7976931348623157e308,
+             -1.7976931348623157e308, float("inf"), float("-inf"), 1.0, -1.0, 0.5, -0.5]
+    vals = [v for v in vals if v != 0.0]
+    keyed = [(key(bits_of(v)), v) for v in vals]
+    for k, v in keyed:
+        assert key(k & ((1 << 64) - 1)) & ((1 << 64) - 1) == bits_of(v)  # involution
+    keyed.sort()
+    for (k1, v1), (k2, v2) in zip(keyed, keyed[1:]):
+        assert v1 <= v2 and (k1 == k2) == (bits_of(v1) == bits_of(v2))
+    nans = [0x7FF8000000000000, 0xFFF8000000000000, 0x7FF0000000000001, 0xFFF0000000000001, 0x7FFFFFFFFFFFFFFF]
+    for u in nans:
+        assert noz(u) and isn(u)
+    for u in (0, 1 << 63):
+        assert noz(u) and not isn(u)
+    for v in vals:
+        assert not noz(bits_of(v)) and not isn(bits_of(v))
