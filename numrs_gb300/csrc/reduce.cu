@@ -258,7 +258,7 @@ template <typename T, int OP, int STAGES>
 __global__ void __launch_bounds__(kColLanes)
     fold_cols_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
                   typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err,
-                  const T* __restrict__ lane_mean, T div) {
+                  const T* __restrict__ lane_mean, T div, int64_t part_len, int64_t part_stride) {
   constexpr int LW = kColLanes;        // lanes per tile (= threads)
   constexpr int RB = col_rows<T>();    // axis positions per tile (8 KB tiles)
   constexpr int TILE = LW * RB * sizeof(T);
@@ -270,7 +270,11 @@ __global__ void __launch_bounds__(kColLanes)
   const int t = threadIdx.x;
   const int64_t l0 = (int64_t)blockIdx.x * LW;
   const int32_t batch = blockIdx.y;
-  const int64_t n_tiles = (alen + RB - 1) / RB;
+  // axis part blockIdx.z: positions [a0, a0 + plen) (the whole axis unless
+  // max / min split it across CTAs; part_len is a whole number of tiles)
+  const int64_t a0 = (int64_t)blockIdx.z * part_len;
+  const int64_t plen = (alen - a0) < part_len ? (alen - a0) : part_len;
+  const int64_t n_tiles = (plen + RB - 1) / RB;
   // Wait-expiry test hook (nrs_test_expire_next_wait): err[1], when set,
   // makes the first CTA leave stage 0 unloaded, so its first wait is on a
   // barrier nothing completes, bounded to err[1] probes. Other CTAs and all
@@ -282,7 +286,7 @@ __global__ void __launch_bounds__(kColLanes)
     for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
     fence_mbar_init();
     abort_flag = 0;
-    const uint32_t probes = (blockIdx.x == 0 && blockIdx.y == 0) ? atomicExch(&err[1], 0u) : 0u;
+    const uint32_t probes = (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) ? atomicExch(&err[1], 0u) : 0u;
     skip_stage0 = probes != 0;
     wait_limit = probes != 0 ? probes : NRS_WAIT_LIMIT;
   }
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(kColLanes)
     for (int s = 0; s < STAGES && s < n_tiles; ++s) {
       if (s == 0 && skip_stage0) continue;
       mbar_arrive_expect_tx(&full[s], TILE);
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(s * RB), batch);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(a0 + s * RB), batch);
     }
   }
   // A thread past the last lane folds lane 0's column (and discards it)
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(kColLanes)
     if (abort_flag) break;
     const T* tile = reinterpret_cast<const T*>(smem + s * TILE);
     const int64_t y0 = it * RB;
-    const int cnt = (int)((alen - y0) < RB ? (alen - y0) : RB);
+    const int cnt = (int)((plen - y0) < RB ? (plen - y0) : RB);
     if (cnt == RB) {
       acc = RunFold<T, OP>::template run<RB>(
           acc, [&](int r) { return lane_xform<T, OP>(tile[r * LW + tl], m); });
@@ -324,7 +328,7 @@ __global__ void __launch_bounds__(kColLanes)
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + STAGES < n_tiles) {
       mbar_arrive_expect_tx(&full[s], TILE);
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)((it + STAGES) * RB),
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(a0 + (it + STAGES) * RB),
                   batch);
     }
   }
@@ -341,7 +345,7 @@ __global__ void __launch_bounds__(kColLanes)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
+  if (lane < lanes) out[blockIdx.z * part_stride + (int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
 // Lanes contiguous along the axis. Tensor map dims (axis, lanes, batch), box
@@ -351,7 +355,7 @@ template <typename T, int OP, int STAGES>
 __global__ void __launch_bounds__(64)
     fold_rows_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
                   typename OutOf<T, OP>::type* __restrict__ out, uint32_t* err,
-                  const T* __restrict__ lane_mean, T div) {
+                  const T* __restrict__ lane_mean, T div, int64_t part_len, int64_t part_stride) {
   constexpr int LN = 64;                  // lanes per tile (= threads)
   constexpr int XB = 128 / sizeof(T);     // axis elements per tile row
   constexpr int PER16 = 16 / sizeof(T);   // elements per 16-byte chunk
@@ -364,7 +368,10 @@ __global__ void __launch_bounds__(64)
   const int t = threadIdx.x;
   const int64_t l0 = (int64_t)blockIdx.x * LN;
   const int32_t batch = blockIdx.y;
-  const int64_t n_tiles = (alen + XB - 1) / XB;
+  // axis part blockIdx.z: positions [a0, a0 + plen) (see fold_cols_tma)
+  const int64_t a0 = (int64_t)blockIdx.z * part_len;
+  const int64_t plen = (alen - a0) < part_len ? (alen - a0) : part_len;
+  const int64_t n_tiles = (plen + XB - 1) / XB;
 
   if (t == 0) {
     prefetch_tensormap(&map);
@@ -376,7 +383,7 @@ __global__ void __launch_bounds__(64)
   if (t == 0) {
     for (int s = 0; s < STAGES && s < n_tiles; ++s) {
       mbar_arrive_expect_tx(&full[s], TILE);
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(s * XB), (int32_t)l0, batch);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(a0 + s * XB), (int32_t)l0, batch);
     }
   }
   // A thread past the last row folds row 0 of the tile (and discards it)
@@ -394,7 +401,7 @@ __global__ void __launch_bounds__(64)
     if (abort_flag) break;
     const uint8_t* row = smem + s * TILE + tl * 128;
     const int64_t x0 = it * XB;
-    const int cnt = (int)((alen - x0) < XB ? (alen - x0) : XB);
+    const int cnt = (int)((plen - x0) < XB ? (plen - x0) : XB);
     if (cnt == XB) {
       T v[XB];
 #pragma unroll
@@ -419,7 +426,7 @@ __global__ void __launch_bounds__(64)
     __syncthreads();
     if (t == 0 && it + STAGES < n_tiles) {
       mbar_arrive_expect_tx(&full[s], TILE);
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)((it + STAGES) * XB), (int32_t)l0,
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(a0 + (it + STAGES) * XB), (int32_t)l0,
                   batch);
     }
   }
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(64)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
+  if (lane < lanes) out[blockIdx.z * part_stride + (int64_t)batch * lanes + lane] = finish<T, OP>(acc, alen, div);
 }
 
 // The comparison argmax / argmin runs on: the value itself, except for f64,
@@ -874,6 +881,20 @@ __global__ void fill_value(T* out, int64_t n, T v) {
     out[i] = v;
 }
 
+// Max / min split along the axis: the parts' results fold in axis order
+// with the lane fold's own step. The step is a monoid action (a lane's first
+// NaN stays; strict comparisons keep the first of equal values), so the
+// result is the unsplit fold's bit for bit.
+template <typename T, int OP>
+__global__ void __launch_bounds__(256)
+    combine_parts(const T* __restrict__ part, int parts, int64_t n, T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T acc = Fold<T, OP>::init();
+    for (int p = 0; p < parts; ++p) acc = Fold<T, OP>::step(acc, part[p * n + i]);
+    out[i] = acc;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host dispatch
 // ---------------------------------------------------------------------------
@@ -959,6 +980,47 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
   const size_t tile_bytes = 8192;
   const size_t smem = PipeSmem<8192, kStages>::kBytes;
   using OutT = typename OutOf<T, OP>::type;
+  // Max / min whose CTAs leave resident slots idle split the axis into up
+  // to 8 parts of whole tiles (at least 8 tiles each), one CTA per (lanes,
+  // part), as many parts as fit one wave of resident CTAs (a second, partial
+  // wave costs more than it gains), and combine the parts in order
+  // (combine_parts).
+  const int64_t ctas = ((lanes + 63) / 64) * batch;
+  int64_t parts = 1, part_len = p.alen;
+  OutT* dst = (OutT*)p.out;
+  const int64_t n_out = lanes * batch;
+  auto plan_parts = [&](const void* kern, int threads, int64_t axis_tile) -> int {
+    if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+      }
+      parts = ((int64_t)per_sm * h->num_sms) / ctas;
+      const int64_t by_len = p.alen / (8 * axis_tile);
+      if (parts > by_len) parts = by_len;
+      if (parts > 8) parts = 8;
+      if (parts < 1) parts = 1;
+    }
+    part_len = ((p.alen + parts - 1) / parts + axis_tile - 1) / axis_tile * axis_tile;
+    parts = (p.alen + part_len - 1) / part_len;
+    if (parts > 1) {
+      int st;
+      dst = (OutT*)nrs_workspace(h, (size_t)(parts * n_out) * sizeof(OutT) + 256, &st);
+      if (!dst) return st;
+    }
+    return NRS_OK;
+  };
+  auto combine = [&]() -> int {
+    if (parts > 1) {
+      if constexpr (OP == NRS_MAX || OP == NRS_MIN) {
+        const int64_t blocks = (n_out + 255) / 256;
+        combine_parts<T, OP><<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, h->stream>>>(
+            (const T*)dst, (int)parts, n_out, (T*)p.out);
+      }
+    }
+    return NRS_OK;
+  };
   if (lstride == 1 && p.astride > 1) {
     // Columns: dims (lanes, axis, batch).
     const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
@@ -969,9 +1031,11 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
       return NRS_ERR_UNSUPPORTED;
     auto kern = fold_cols_tma<T, OP, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((lanes + kColLanes - 1) / kColLanes), (unsigned)batch);
-    kern<<<grid, kColLanes, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error,
-                                               (const T*)p.lane_mean, (T)p.div);
+    if (int st = plan_parts((const void*)kern, kColLanes, col_rows<T>())) return st;
+    dim3 grid((unsigned)((lanes + kColLanes - 1) / kColLanes), (unsigned)batch, (unsigned)parts);
+    kern<<<grid, kColLanes, smem, h->stream>>>(map, p.alen, lanes, dst, h->dev_error,
+                                               (const T*)p.lane_mean, (T)p.div, part_len, n_out);
+    combine();
     return nrs_after_launch(h, "fold_cols_tma");
   }
   if (p.astride == 1 && lstride > 1) {
@@ -984,9 +1048,11 @@ int launch_tma(nrs_handle* h, const AxisProblem& p) {
       return NRS_ERR_UNSUPPORTED;
     auto kern = fold_rows_tma<T, OP, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch);
-    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (OutT*)p.out, h->dev_error,
-                                        (const T*)p.lane_mean, (T)p.div);
+    if (int st = plan_parts((const void*)kern, 64, 128 / es)) return st;
+    dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch, (unsigned)parts);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, dst, h->dev_error,
+                                        (const T*)p.lane_mean, (T)p.div, part_len, n_out);
+    combine();
     return nrs_after_launch(h, "fold_rows_tma");
   }
   (void)tile_bytes;

@@ -242,10 +242,12 @@ def test_large_c2_shape_properties(K):
     del x
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("case", ["negatives", "zeros", "nans", "extremes"])
-def test_f64_extrema_bit_exact(K, ora, case):
-    """f64 max / min run on int64 keys (integer pipe) for blocks with no NaN
-    and no zero and fall back to the ordered fold otherwise: both lane
+def test_extrema_bit_exact(K, ora, case, dtype):
+    """Max / min: f64 on int64 keys (integer pipe), f32 on NaN-propagating
+    chains, blocks with a NaN or a zero on the ordered fold; at 700 x 520
+    both lane pipelines split the axis into parts combined in order. Both
     pipelines, the flattened partials and the ufunc reduce against the
     oracle bit for bit, on all-negative data (the extreme near zero), signed
     zeros, NaNs, and infinities / subnormals / the largest finite values."""
@@ -257,15 +259,17 @@ def test_f64_extrema_bit_exact(K, ora, case):
     elif case == "nans":
         x[r.random(x.shape) < 0.001] = np.nan
     elif case == "extremes":
-        for v in (-np.inf, np.inf, 5e-324, -5e-324, 1.7976931348623157e308, -1.7976931348623157e308):
+        tiny, big = (5e-324, 1.7976931348623157e308) if dtype == np.float64 else (1e-45, 3.4028235e38)
+        for v in (-np.inf, np.inf, tiny, -tiny, big, -big):
             x[r.random(x.shape) < 0.002] = v
+    x = x.astype(dtype)
     xd = _dev(x)
     for op in ("max", "min"):
         for axis in (0, 1):
             _check_axis(K, ora, x, op, axis)
             _check_axis(K, ora, x, op, axis, transposed=True)
         got = to_np(getattr(K, op)(xd))
-        want = np.array([ora.flat(op, x)], np.float64)
+        want = np.array([ora.flat(op, x)], dtype)
         assert np.isnan(got[0]) == np.isnan(want[0])
         if not np.isnan(want[0]):
             np.testing.assert_array_equal(bits(got), bits(want))
