@@ -102,6 +102,25 @@ def test_nan_placement(ora):
             assert np.isnan(ora.flat("max", e)) and np.isnan(ora.flat("min", e))
 
 
+def test_zero_ties_keep_the_first(ora):
+    """The reference's min / max fold chunks with a strict compare and
+    combines the chunk results in order (src/kernels/reduce.rs:335-364), so
+    an extreme of zero keeps the sign of the first zero: the oracle must do
+    the same, within one chunk and across the 8192-element chunk edge, for
+    the flat and the axis folds."""
+    for f in (np.float64, np.float32):
+        for first, later in ((-0.0, 0.0), (0.0, -0.0)):
+            for n, p0, p1 in ((10, 3, 7), (20000, 8190, 8195), (20000, 100, 16384)):
+                x = -np.abs(np.random.default_rng(n).standard_normal(n)).astype(f) - 1
+                x[p0], x[p1] = first, later
+                assert np.signbit(ora.flat("max", x)) == np.signbit(f(first))
+                assert np.signbit(ora.axis(O.MAX, x.reshape(-1, 1), 0)[0]) == np.signbit(f(first))
+                y = -x
+                y[p0], y[p1] = first, later
+                assert np.signbit(ora.flat("min", y)) == np.signbit(f(first))
+                assert np.signbit(ora.axis(O.MIN, y.reshape(-1, 1), 0)[0]) == np.signbit(f(first))
+
+
 def test_empty_conventions(ora):
     e = np.zeros(0, np.float64)
     assert ora.flat("sum", e) == 0 and ora.flat("mean", e) == 0 and ora.flat("max", e) == 0
