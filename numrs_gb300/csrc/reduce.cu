@@ -453,6 +453,9 @@ struct ArgOrd {
   using K = T;
   static __device__ __forceinline__ K key(T v) { return v; }
   static __device__ __forceinline__ K start(T v) { return v; }
+  // the key an axis part after the first starts from: no element strictly
+  // beats it unless it beats every non-NaN value
+  static __device__ __forceinline__ K none() { return MAX ? Lim<T>::lowest() : Lim<T>::highest(); }
 };
 template <bool MAX>
 struct ArgOrd<double, MAX> {
@@ -464,6 +467,7 @@ struct ArgOrd<double, MAX> {
     return nrs_f64_key(u);
   }
   static __device__ __forceinline__ K start(double v) { return v != v ? (MAX ? INT64_MAX : INT64_MIN) : key(v); }
+  static __device__ __forceinline__ K none() { return key(MAX ? -INFINITY : INFINITY); }
 };
 
 // argmax / argmin along lanes through the same TMA pipelines: each thread
@@ -473,7 +477,8 @@ struct ArgOrd<double, MAX> {
 template <typename T, bool MAX, bool COLS, int STAGES>
 __global__ void __launch_bounds__(64)
     arg_lane_tma(const __grid_constant__ CUtensorMap map, int64_t alen, int64_t lanes,
-                 int64_t* __restrict__ out, uint32_t* err) {
+                 int64_t* __restrict__ out, uint32_t* err, int64_t part_len,
+                 typename ArgOrd<T, MAX>::K* __restrict__ part_key) {
   constexpr int TB = COLS ? col_rows<T>() : 128 / (int)sizeof(T);  // axis positions per tile
   constexpr int TILE = 8192;
   constexpr int PER16 = 16 / sizeof(T);
@@ -485,13 +490,19 @@ __global__ void __launch_bounds__(64)
   const int t = threadIdx.x;
   const int64_t l0 = (int64_t)blockIdx.x * 64;
   const int32_t batch = blockIdx.y;
-  const int64_t n_tiles = (alen + TB - 1) / TB;
+  // axis part blockIdx.z: positions [a0, a0 + plen); with part_key set,
+  // each part writes its best key and absolute index (-1: none) for
+  // combine_arg_parts, and parts after the first start from no candidate
+  // (only the lane's own first element may be a NaN winner)
+  const int64_t a0 = (int64_t)blockIdx.z * part_len;
+  const int64_t plen = (alen - a0) < part_len ? (alen - a0) : part_len;
+  const int64_t n_tiles = (plen + TB - 1) / TB;
   auto load = [&](int s, int64_t tile) {
     mbar_arrive_expect_tx(&full[s], TILE);
     if (COLS)
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(tile * TB), batch);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)l0, (int32_t)(a0 + tile * TB), batch);
     else
-      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(tile * TB), (int32_t)l0, batch);
+      tma_load_3d(smem + s * TILE, &map, &full[s], (int32_t)(a0 + tile * TB), (int32_t)l0, batch);
   };
   if (t == 0) {
     prefetch_tensormap(&map);
@@ -505,6 +516,7 @@ __global__ void __launch_bounds__(64)
   using Ord = ArgOrd<T, MAX>;
   typename Ord::K best = typename Ord::K(0);
   int bt = 0, be = 0;  // tile and position of the best so far (32-bit selects)
+  bool found = blockIdx.z == 0;  // a later part: has any element beaten none()?
   const int sw = t & 7;
   int64_t it = 0;
   for (; it < n_tiles; ++it) {
@@ -513,7 +525,7 @@ __global__ void __launch_bounds__(64)
     __syncthreads();
     if (abort_flag) break;
     const int64_t j0 = it * TB;
-    const int cnt = (int)((alen - j0) < TB ? (alen - j0) : TB);
+    const int cnt = (int)((plen - j0) < TB ? (plen - j0) : TB);
     T v[TB];
     if (COLS) {
       const T* tile = reinterpret_cast<const T*>(smem + s * TILE);
@@ -529,7 +541,7 @@ __global__ void __launch_bounds__(64)
     // The lane's first element starts it (comparing it with itself then
     // changes nothing, NaN included), so full tiles need no per-element
     // checks beyond the compare.
-    if (it == 0) best = Ord::start(v[0]);
+    if (it == 0) best = blockIdx.z == 0 ? Ord::start(v[0]) : Ord::none();
     int bet = -1;  // position of this tile's improvement, if any
     if (cnt == TB) {
 #pragma unroll
@@ -553,6 +565,7 @@ __global__ void __launch_bounds__(64)
     if (bet >= 0) {
       bt = (int)it;
       be = bet;
+      found = true;
     }
     __syncthreads();  // every thread is done with stage s
     if (t == 0 && it + STAGES < n_tiles) load(s, it + STAGES);
@@ -566,7 +579,16 @@ __global__ void __launch_bounds__(64)
     return;
   }
   const int64_t lane = l0 + t;
-  if (lane < lanes) out[(int64_t)batch * lanes + lane] = (int64_t)bt * TB + be;
+  if (lane < lanes) {
+    const int64_t o = (int64_t)batch * lanes + lane;
+    if (!part_key) {
+      out[o] = (int64_t)bt * TB + be;
+    } else {
+      const int64_t po = (int64_t)blockIdx.z * lanes * gridDim.y + o;
+      out[po] = found ? a0 + (int64_t)bt * TB + be : -1;
+      part_key[po] = best;
+    }
+  }
 }
 
 constexpr int kStages = 8;
@@ -895,6 +917,29 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// argmax / argmin split along the axis: part 0's candidate (the lane's
+// first element seeds it, a leading NaN unbeatable), then each later part's
+// candidate, if it has one, replaces it only when strictly better, so the
+// first index of the extreme wins as in one left-to-right scan.
+template <typename K, bool MAX>
+__global__ void __launch_bounds__(256)
+    combine_arg_parts(const K* __restrict__ key, const int64_t* __restrict__ idx, int parts, int64_t n,
+                      int64_t* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    K best = key[i];
+    int64_t bi = idx[i];
+    for (int p = 1; p < parts; ++p) {
+      const int64_t j = idx[p * n + i];
+      const K k = key[p * n + i];
+      if (j >= 0 && (MAX ? (k > best) : (k < best))) {
+        best = k;
+        bi = j;
+      }
+    }
+    out[i] = bi;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host dispatch
 // ---------------------------------------------------------------------------
@@ -1072,7 +1117,44 @@ int launch_arg_tma(nrs_handle* h, const AxisProblem& p) {
   if (batch > 65535) return NRS_ERR_UNSUPPORTED;
   const size_t smem = PipeSmem<8192, kStages>::kBytes;
   CUtensorMap map;
-  dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch);
+  // Too few CTAs for one wave of resident slots: split the axis into up to
+  // 8 parts of whole tiles (at least 8 tiles each), as many as fit one wave,
+  // and combine the parts' candidates in order (combine_arg_parts).
+  using Key = typename ArgOrd<T, MAX>::K;
+  const int64_t ctas = ((lanes + 63) / 64) * batch;
+  const int64_t n_out = lanes * batch;
+  int64_t parts = 1, part_len = p.alen;
+  int64_t* idx = (int64_t*)p.out;
+  Key* pkey = nullptr;
+  auto plan_parts = [&](const void* kern, int64_t axis_tile) -> int {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 64, smem) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    parts = ((int64_t)per_sm * h->num_sms) / ctas;
+    const int64_t by_len = p.alen / (8 * axis_tile);
+    if (parts > by_len) parts = by_len;
+    if (parts > 8) parts = 8;
+    if (parts < 1) parts = 1;
+    part_len = ((p.alen + parts - 1) / parts + axis_tile - 1) / axis_tile * axis_tile;
+    parts = (p.alen + part_len - 1) / part_len;
+    if (parts > 1) {
+      int st;
+      uint8_t* ws = (uint8_t*)nrs_workspace(h, (size_t)(parts * n_out) * (sizeof(int64_t) + sizeof(Key)) + 256, &st);
+      if (!ws) return st;
+      idx = reinterpret_cast<int64_t*>(ws);
+      pkey = reinterpret_cast<Key*>(ws + (size_t)(parts * n_out) * sizeof(int64_t));
+    }
+    return NRS_OK;
+  };
+  auto combine = [&]() {
+    if (parts > 1) {
+      const int64_t blocks = (n_out + 255) / 256;
+      combine_arg_parts<Key, MAX><<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, h->stream>>>(
+          pkey, idx, (int)parts, n_out, (int64_t*)p.out);
+    }
+  };
   if (lstride == 1 && p.astride > 1) {
     const uint64_t dims[3] = {(uint64_t)lanes, (uint64_t)p.alen, (uint64_t)batch};
     const uint64_t strides[2] = {(uint64_t)p.astride * es, (uint64_t)(batch > 1 ? bstride : p.astride * p.alen) * es};
@@ -1080,7 +1162,10 @@ int launch_arg_tma(nrs_handle* h, const AxisProblem& p) {
     if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE)) return NRS_ERR_UNSUPPORTED;
     auto kern = arg_lane_tma<T, MAX, true, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (int64_t*)p.out, h->dev_error);
+    if (int st = plan_parts((const void*)kern, col_rows<T>())) return st;
+    dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch, (unsigned)parts);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, idx, h->dev_error, part_len, pkey);
+    combine();
     return nrs_after_launch(h, "arg_lane_tma");
   }
   if (p.astride == 1 && lstride > 1) {
@@ -1090,7 +1175,10 @@ int launch_arg_tma(nrs_handle* h, const AxisProblem& p) {
     if (!make_map(&map, p.dtype, p.x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B)) return NRS_ERR_UNSUPPORTED;
     auto kern = arg_lane_tma<T, MAX, false, kStages>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, (int64_t*)p.out, h->dev_error);
+    if (int st = plan_parts((const void*)kern, 128 / es)) return st;
+    dim3 grid((unsigned)((lanes + 63) / 64), (unsigned)batch, (unsigned)parts);
+    kern<<<grid, 64, smem, h->stream>>>(map, p.alen, lanes, idx, h->dev_error, part_len, pkey);
+    combine();
     return nrs_after_launch(h, "arg_lane_tma");
   }
   return NRS_ERR_UNSUPPORTED;
